@@ -1,0 +1,299 @@
+"""ctypes front end of the CPU oracle (oracle/xpcs_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of ``bench.py`` -- never by the product.
+
+Each wrapper returns numpy arrays in the reference's layouts:
+  * G2/IP/IF            float32 [D][P]   (Corr::multiTau2, src/xpcs/corr.cpp:315)
+  * g2/stderr           [D][nq]          (Corr::normalizeG2s, src/xpcs/corr.cpp:927)
+  * event lists (rows)  CSR by pixel     (SparseData/Row, src/xpcs/data_structure)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libxpcs_oracle.so"
+REF_CORR = HERE / "_ref" / "corr"
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle shared library (gcc, OpenMP, no FP contraction)."""
+    src = HERE / "xpcs_oracle.c"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(
+        src.stat().st_mtime, (HERE / "xpcs_oracle.h").stat().st_mtime
+    ):
+        LIB.parent.mkdir(parents=True, exist_ok=True)
+        subprocess.check_call(
+            ["gcc", "-std=c11", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+             "-o", str(LIB), str(src), "-lm"]
+        )
+    return LIB
+
+
+def build_reference(ref_root: str = "/root/reference", jobs: int = 8) -> Path | None:
+    """Build the upstream `corr` from its own sources into oracle/_ref (when present)."""
+    if not Path(ref_root, "src", "xpcs", "corr.cpp").exists():
+        return None
+    subprocess.check_call(
+        ["make", "-s", "-C", str(HERE / "ref_build"), f"REF={ref_root}", f"-j{jobs}"]
+    )
+    return REF_CORR
+
+
+class _QMap(C.Structure):
+    _fields_ = [
+        ("pixels", C.c_int32), ("total_static", C.c_int32), ("total_dynamic", C.c_int32),
+        ("nq", C.c_int32), ("nsb", C.c_int32), ("npix", C.c_int32),
+        ("valid", C.POINTER(C.c_int16)), ("sbin_mask", C.POINTER(C.c_int32)),
+        ("pixels_per_bin", C.POINTER(C.c_int32)), ("q_ids", C.POINTER(C.c_int32)),
+        ("q_sb_ptr", C.POINTER(C.c_int32)), ("sb_ids", C.POINTER(C.c_int32)),
+        ("sb_pix_ptr", C.POINTER(C.c_int32)), ("pix", C.POINTER(C.c_int32)),
+        ("error", C.c_int32),
+    ]
+
+
+class _FilterParams(C.Structure):
+    _fields_ = [
+        ("pixels", C.c_int32), ("frames", C.c_int32), ("real_frames", C.c_int32),
+        ("stride", C.c_int32), ("average", C.c_int32), ("static_window", C.c_int32),
+        ("total_static", C.c_int32), ("pixel_mask", C.POINTER(C.c_int16)),
+        ("sbin_mask", C.POINTER(C.c_int32)), ("flatfield", C.POINTER(C.c_double)),
+    ]
+
+
+class _Rows(C.Structure):
+    _fields_ = [
+        ("pixels", C.c_int32), ("row_ptr", C.POINTER(C.c_int64)),
+        ("frame", C.POINTER(C.c_int32)), ("value", C.POINTER(C.c_float)),
+    ]
+
+
+class _Side(C.Structure):
+    _fields_ = [
+        ("pixels_sum", C.POINTER(C.c_float)), ("frames_sum", C.POINTER(C.c_float)),
+        ("partitions_mean", C.POINTER(C.c_float)), ("partial_mean", C.POINTER(C.c_float)),
+        ("timestamp_clock", C.POINTER(C.c_double)), ("timestamp_ticks", C.POINTER(C.c_double)),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        L.xo_level_max.restype = C.c_int
+        L.xo_delays.restype = C.c_int
+        L.xo_build_qmap.restype = C.c_int
+        L.xo_sparse_filter.restype = C.c_int
+        L.xo_dense_filter.restype = C.c_int
+        L.xo_multitau2.restype = C.c_int
+        L.xo_normalize_f32.restype = C.c_int
+        L.xo_normalize_f64.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _copy(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def delays(frames: int, dpl: int) -> tuple[np.ndarray, np.ndarray]:
+    """(level, tau) of Corr::delaysPerLevel (src/xpcs/corr.cpp:1133)."""
+    cap = 4096
+    lv = np.zeros(cap, np.int32)
+    tau = np.zeros(cap, np.int32)
+    n = lib().xo_delays(frames, dpl, _p(lv, C.c_int32), _p(tau, C.c_int32), cap)
+    return lv[:n].copy(), tau[:n].copy()
+
+
+class QMap:
+    """Configuration::BuildQMap restated (src/xpcs/configuration.cpp:244)."""
+
+    def __init__(self, dqmap: np.ndarray, sqmap: np.ndarray):
+        dq = np.ascontiguousarray(dqmap, np.int32).ravel()
+        sq = np.ascontiguousarray(sqmap, np.int32).ravel()
+        self._s = _QMap()
+        lib().xo_build_qmap(_p(dq, C.c_int32), _p(sq, C.c_int32), dq.size, C.byref(self._s))
+        s = self._s
+        self.pixels = s.pixels
+        self.total_static = s.total_static
+        self.total_dynamic = s.total_dynamic
+        self.nq = s.nq
+        self.error = s.error
+        self.valid = _copy(s.valid, s.pixels, np.int16)
+        self.sbin_mask = _copy(s.sbin_mask, s.pixels, np.int32)
+        self.pixels_per_bin = _copy(s.pixels_per_bin, s.total_static, np.int32)
+        self.q_ids = _copy(s.q_ids, s.nq, np.int32)
+        self.q_sb_ptr = _copy(s.q_sb_ptr, s.nq + 1, np.int32)
+        self.sb_ids = _copy(s.sb_ids, s.nsb, np.int32)
+        self.sb_pix_ptr = _copy(s.sb_pix_ptr, s.nsb + 1, np.int32)
+        self.pix = _copy(s.pix, s.npix, np.int32)
+
+    def __del__(self):
+        try:
+            lib().xo_free_qmap(C.byref(self._s))
+        except Exception:
+            pass
+
+
+class Rows:
+    """Pixel-major event lists (CSR)."""
+
+    def __init__(self, row_ptr, frame, value):
+        self.row_ptr = np.ascontiguousarray(row_ptr, np.int64)
+        self.frame = np.ascontiguousarray(frame, np.int32)
+        self.value = np.ascontiguousarray(value, np.float32)
+        self.pixels = self.row_ptr.size - 1
+
+    def _struct(self):
+        r = _Rows()
+        r.pixels = self.pixels
+        r.row_ptr = _p(self.row_ptr, C.c_int64)
+        r.frame = _p(self.frame, C.c_int32)
+        r.value = _p(self.value, C.c_float)
+        return r
+
+
+def _filter_params(qm: QMap, frames, real_frames, stride, average, static_window, flat):
+    fp = _FilterParams()
+    fp.pixels = qm.pixels
+    fp.frames = frames
+    fp.real_frames = real_frames
+    fp.stride = stride
+    fp.average = average
+    fp.static_window = static_window
+    fp.total_static = qm.total_static
+    fp.pixel_mask = _p(qm.valid, C.c_int16)
+    fp.sbin_mask = _p(qm.sbin_mask, C.c_int32)
+    fp.flatfield = _p(flat, C.c_double)
+    return fp
+
+
+def _collect(rows_s: _Rows, side_s: _Side, fp: _FilterParams, qm: QMap, finish: bool):
+    P = rows_s.pixels
+    rp = _copy(rows_s.row_ptr, P + 1, np.int64)
+    E = int(rp[-1])
+    rows = Rows(rp, _copy(rows_s.frame, E, np.int32), _copy(rows_s.value, E, np.float32))
+    if finish:
+        lib().xo_finish_side(C.byref(fp), _p(qm.pixels_per_bin, C.c_int32), C.byref(side_s))
+    F, S, R = fp.frames, fp.total_static, fp.real_frames
+    nparts = -(-F // fp.static_window)
+    side = {
+        "pixels_sum": _copy(side_s.pixels_sum, P, np.float32),
+        "frames_sum": _copy(side_s.frames_sum, 2 * F, np.float32).reshape(2, F),
+        "partitions_mean": _copy(side_s.partitions_mean, S, np.float32),
+        "partial_mean": _copy(side_s.partial_mean, nparts * S, np.float32).reshape(nparts, S),
+        "timestamp_clock": _copy(side_s.timestamp_clock, 2 * R, np.float64).reshape(2, R),
+        "timestamp_tick": _copy(side_s.timestamp_ticks, 2 * R, np.float64).reshape(2, R),
+    }
+    lib().xo_free_rows(C.byref(rows_s))
+    lib().xo_free_side(C.byref(side_s))
+    return rows, side
+
+
+def sparse_filter(qm: QMap, nnz, idx, val, frames, real_frames=None, stride=1, average=1,
+                  static_window=None, flat=None, clock=None, ticks=None, finish=True):
+    """SparseFilter::Apply over a series (src/xpcs/filter/sparse_filter.cpp:115)."""
+    nnz = np.ascontiguousarray(nnz, np.uint32)
+    idx = np.ascontiguousarray(idx, np.int32)
+    val = np.ascontiguousarray(val, np.int16)
+    real_frames = real_frames if real_frames is not None else nnz.size
+    static_window = static_window or max(frames // 10, 1)
+    flat = np.ascontiguousarray(flat if flat is not None else np.ones(qm.pixels), np.float64)
+    fp = _filter_params(qm, frames, real_frames, stride, average, static_window, flat)
+    rows_s, side_s = _Rows(), _Side()
+    ck = np.ascontiguousarray(clock, np.float64) if clock is not None else None
+    tk = np.ascontiguousarray(ticks, np.float64) if ticks is not None else None
+    bad = lib().xo_sparse_filter(
+        C.byref(fp), _p(idx, C.c_int32), _p(val, C.c_int16), _p(nnz, C.c_uint32),
+        _p(ck, C.c_double) if ck is not None else None,
+        _p(tk, C.c_double) if tk is not None else None, C.byref(rows_s), C.byref(side_s))
+    rows, side = _collect(rows_s, side_s, fp, qm, finish)
+    side["bad_index"] = bool(bad)
+    return rows, side
+
+
+def dark_image(dark: np.ndarray, flat: np.ndarray):
+    """DarkImage::Compute (src/xpcs/data_structure/dark_image.cpp:81)."""
+    dark = np.ascontiguousarray(dark, np.int16)
+    nd, P = dark.shape
+    flat = np.ascontiguousarray(flat, np.float64)
+    avg = np.zeros(P, np.float64)
+    std = np.zeros(P, np.float64)
+    lib().xo_dark_image(_p(dark, C.c_int16), nd, P, _p(flat, C.c_double),
+                        _p(avg, C.c_double), _p(std, C.c_double))
+    return avg, std
+
+
+def dense_filter(qm: QMap, raw, frames, dark_avg=None, dark_std=None, lld=0.0, sigma=0.0,
+                 real_frames=None, stride=1, average=1, static_window=None, flat=None,
+                 clock=None, ticks=None, finish=True):
+    """DenseFilter::Apply over a series (src/xpcs/filter/dense_filter.cpp:121)."""
+    raw = np.ascontiguousarray(raw, np.int16)
+    real_frames = real_frames if real_frames is not None else raw.shape[0]
+    static_window = static_window or max(frames // 10, 1)
+    flat = np.ascontiguousarray(flat if flat is not None else np.ones(qm.pixels), np.float64)
+    fp = _filter_params(qm, frames, real_frames, stride, average, static_window, flat)
+    rows_s, side_s = _Rows(), _Side()
+    da = np.ascontiguousarray(dark_avg, np.float64) if dark_avg is not None else None
+    ds = np.ascontiguousarray(dark_std, np.float64) if dark_std is not None else None
+    lib().xo_dense_filter(
+        C.byref(fp), _p(raw, C.c_int16),
+        _p(da, C.c_double) if da is not None else None,
+        _p(ds, C.c_double) if ds is not None else None,
+        C.c_float(lld), C.c_float(sigma), None, None, C.byref(rows_s), C.byref(side_s))
+    return _collect(rows_s, side_s, fp, qm, finish)
+
+
+def multitau2(rows: Rows, frames: int, dpl: int, mode: int = 0, threads: int = 0):
+    """Corr::multiTau2 (src/xpcs/corr.cpp:315). mode 0 = reference, 1 = exact."""
+    lv, _ = delays(frames, dpl)
+    D, P = lv.size, rows.pixels
+    G2 = np.zeros((D, P), np.float32)
+    IP = np.zeros((D, P), np.float32)
+    IF = np.zeros((D, P), np.float32)
+    rs = rows._struct()
+    lib().xo_multitau2(C.byref(rs), frames, dpl, mode, threads, _p(G2, C.c_float),
+                       _p(IP, C.c_float), _p(IF, C.c_float))
+    return G2, IP, IF
+
+
+def normalize_f32(qm: QMap, G2, IP, IF):
+    """Corr::normalizeG2s in float32 (src/xpcs/corr.cpp:927)."""
+    D = G2.shape[0]
+    g2 = np.zeros((D, qm.nq), np.float32)
+    se = np.zeros((D, qm.nq), np.float32)
+    args = [np.ascontiguousarray(a, np.float32) for a in (G2, IP, IF)]
+    lib().xo_normalize_f32(C.byref(qm._s), D, *[_p(a, C.c_float) for a in args],
+                           _p(g2, C.c_float), _p(se, C.c_float))
+    return g2, se
+
+
+def normalize_f64(qm: QMap, G2, IP, IF):
+    """Corr::normalizeG2s formulas in double precision."""
+    D = G2.shape[0]
+    g2 = np.zeros((D, qm.nq), np.float64)
+    se = np.zeros((D, qm.nq), np.float64)
+    args = [np.ascontiguousarray(a, np.float32) for a in (G2, IP, IF)]
+    lib().xo_normalize_f64(C.byref(qm._s), D, *[_p(a, C.c_float) for a in args],
+                           _p(g2, C.c_double), _p(se, C.c_double))
+    return g2, se
+
+
+def cpu_count() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
