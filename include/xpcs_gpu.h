@@ -1,0 +1,178 @@
+/*
+ * xpcs_gpu.h — C ABI of the GB300 (sm_103a) multi-tau XPCS correlator.
+ *
+ * Drop-in boundary for xpcs-eigen's `corr` multi-tau path.  The reference has
+ * no plugin or FFI layer: its path is a set of static C++ calls that read their
+ * parameters from the Configuration singleton.  Each entry point below names
+ * the reference interface it replaces (file:line in xpcs-eigen).
+ *
+ * Conventions
+ *  - Every function returns an xpcs_status (XPCS_OK = 0); no C++ exception
+ *    crosses this boundary.  xpcs_last_error() gives a message for the last
+ *    failure on the calling thread.
+ *  - All array arguments are HOST pointers unless the function name ends in
+ *    _device.  Inputs are copied; output buffers are caller-owned.
+ *  - A series handle owns one CUDA stream; calls on one handle are ordered.
+ *    Distinct handles may be used from distinct threads.
+ *  - Work is enqueued asynchronously; functions that return data to the host
+ *    (xpcs_get_*, xpcs_normalize, xpcs_synchronize) wait for it and report any
+ *    error raised by earlier device work of that handle.
+ *  - Layouts follow the reference: G2/IP/IF are float32 [D][P] (tau-major, as
+ *    Corr::multiTau2 fills G2s[tauIndex*pixels + pixel], corr.cpp:392), and
+ *    g2/stderr are [D][Q] (the on-disk layout of norm-0-g2, h5_result.cpp:76-78).
+ */
+#ifndef XPCS_GPU_H
+#define XPCS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XPCS_GPU_ABI_VERSION 1
+
+typedef enum {
+  XPCS_OK = 0,
+  XPCS_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or parameter */
+  XPCS_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  XPCS_ERR_OUT_OF_MEMORY = 3,    /* device or pinned host allocation failed */
+  XPCS_ERR_STATE = 4,            /* call out of order (e.g. results before compute) */
+  XPCS_ERR_QMAP = 5,             /* partition maps the reference would index out of
+                                    bounds (quirks Q5/Q7 of BuildQMap/normalizeG2s) */
+  XPCS_ERR_INPUT = 6,            /* frame data out of range (pixel index >= W*H) */
+  XPCS_ERR_NO_DEVICE = 7         /* no usable CUDA device */
+} xpcs_status;
+
+/* Multi-tau search semantics.
+ * REFERENCE: the partner of an event is looked up with std::lower_bound over
+ *   the whole row buffer including the stale tail left by in-place level
+ *   compaction (corr.cpp:406), so a few G2 products are missed exactly as the
+ *   reference misses them.  Bit-identical to Corr::multiTau2.
+ * EXACT: the lookup covers only the live prefix (the intended semantics). */
+typedef enum { XPCS_MODE_REFERENCE = 0, XPCS_MODE_EXACT = 1 } xpcs_mode;
+
+typedef struct xpcs_series xpcs_series;
+
+/* Series description: the Configuration fields the path reads
+ * (Configuration::init, configuration.cpp:80-242). */
+typedef struct {
+  int32_t width;            /* /measurement/instrument/detector/x_dimension */
+  int32_t height;           /* /measurement/instrument/detector/y_dimension */
+  int32_t frames;           /* getFrameTodoCount(): (end-begin+1)/(stride*avg) */
+  int32_t delays_per_level; /* /xpcs/delays_per_level */
+  int32_t stride_frames;    /* /xpcs/stride_frames (>= 1) */
+  int32_t avg_frames;       /* /xpcs/avg_frames (>= 1) */
+  int32_t static_window;    /* /xpcs/static_mean_window_size (>= 1) */
+  const int32_t *dqmap;     /* [height*width] /xpcs/dqmap (final orientation) */
+  const int32_t *sqmap;     /* [height*width] /xpcs/sqmap */
+  const double *flatfield;  /* [height*width] or NULL when flatfield is disabled */
+  int32_t dense;            /* 0: sparse (compressed) IMM frames, 1: dense frames */
+  float lld;                /* dense with darks: /xpcs/lld */
+  float sigma;              /* dense with darks: /xpcs/sigma */
+  int32_t device;           /* CUDA device ordinal */
+} xpcs_series_desc;
+
+typedef struct {
+  int32_t pixels;             /* width*height */
+  int32_t delays;             /* D = number of (level, tau) pairs */
+  int32_t total_static;       /* getTotalStaticPartitions() */
+  int32_t total_dynamic;      /* getTotalDynamicPartitions() */
+  int32_t qbins;              /* rows of g2/stderr = q bins in the mapping */
+  int32_t raw_frames;         /* raw frames ingested so far */
+  int64_t raw_events;         /* raw events ingested so far */
+  int64_t events;             /* pixel events after the filter (valid after multitau) */
+  int32_t valid_pixels;       /* pixels with >= 1 event (valid after multitau) */
+  int32_t float_path_pixels;  /* pixels on the order-preserving float path */
+} xpcs_series_info;
+
+/* Device times of the last xpcs_multitau / xpcs_normalize of a handle, from
+ * CUDA events recorded on the handle's stream (milliseconds). */
+typedef struct {
+  float h2d_ms;        /* host-to-device copies of ingested frames */
+  float filter_ms;     /* K-a: mask/flat filter + pixel-major radix transpose */
+  float multitau_ms;   /* K-c: integer path + float path */
+  float normalize_ms;  /* K-d: g2/stderr (float64 and float32) */
+  float d2h_ms;        /* device-to-host copies of results */
+  float multitau_int_ms;
+  float multitau_float_ms;
+  float step_ms;       /* start of xpcs_multitau to the end of xpcs_normalize's copies */
+  int32_t launches;    /* kernels launched by the last xpcs_multitau + xpcs_normalize */
+} xpcs_stage_times;
+
+/* Library version of this header. */
+int xpcs_abi_version(void);
+
+/* Message of the last failure on this thread ("" if none). */
+const char *xpcs_last_error(void);
+
+/* Corr::calculateLevelMax + Corr::delaysPerLevel (corr.cpp:1133-1160).
+ * Writes min(D, capacity) pairs; *count = D. */
+int xpcs_delay_schedule(int32_t frames, int32_t delays_per_level, int32_t *level, int32_t *tau,
+                        int32_t capacity, int32_t *count);
+
+/* Configuration::init + BuildQMap (configuration.cpp:80-381) for one series:
+ * builds the valid-pixel mask, static/dynamic partitions and the delay
+ * schedule, and allocates device state on desc->device. */
+int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out);
+
+void xpcs_series_destroy(xpcs_series *s);
+
+/* Forget ingested frames and results; keep maps and device buffers. */
+int xpcs_series_reset(xpcs_series *s);
+
+int xpcs_series_get_info(xpcs_series *s, xpcs_series_info *info);
+
+/* Imm::NextFrames + SparseFilter::Apply input (imm.cpp:70-118,
+ * sparse_filter.cpp:115-193): append `nframes` raw sparse frames.  Frame r has
+ * nnz[r] events idx[..] (int32 pixel index) and val[..] (int16 value, read as
+ * signed like the reference); the arrays hold the frames back to back.  Frames
+ * are grouped stride*avg per filter frame in arrival order. */
+int xpcs_ingest_sparse(xpcs_series *s, const int32_t *idx, const int16_t *val,
+                       const uint32_t *nnz, int32_t nframes);
+
+/* As xpcs_ingest_sparse with idx/val already in device memory of the
+ * handle's device (nnz stays a host array). */
+int xpcs_ingest_sparse_device(xpcs_series *s, const int32_t *idx_device,
+                              const int16_t *val_device, const uint32_t *nnz, int32_t nframes);
+
+/* Corr::multiTau2 (corr.cpp:315-431), preceded by the filter's transpose of
+ * the ingested frames into pixel-major event lists.  Enqueues the work. */
+int xpcs_multitau(xpcs_series *s, int32_t mode);
+
+/* The G2/IP/IF arrays of Corr::multiTau2, float32 [D][P] each; any may be NULL. */
+int xpcs_get_g2ipif(xpcs_series *s, float *G2, float *IP, float *IF);
+
+/* Corr::normalizeG2s (corr.cpp:927-1091): per-partition g2 and standard error,
+ * [D][Q] each.  g2/stderr_: float64 evaluation; g2_f32/stderr_f32: float32
+ * evaluation in the reference's operation order (bit-identical to the
+ * reference's norm-0-g2 / norm-0-stderr).  Any pointer may be NULL. */
+int xpcs_normalize(xpcs_series *s, double *g2, double *stderr_, float *g2_f32,
+                   float *stderr_f32);
+
+/* Waits for the handle's stream; reports deferred device errors. */
+int xpcs_synchronize(xpcs_series *s);
+
+int xpcs_get_stage_times(xpcs_series *s, xpcs_stage_times *t);
+
+/* Page-lock (cudaHostRegister) / release a caller buffer so that ingest copies
+ * from it run at full host-to-device bandwidth.  No reference counterpart: the
+ * reference reads frames from disk into pageable memory (imm.cpp:70-118). */
+int xpcs_pin_host(void *ptr, uint64_t bytes);
+int xpcs_unpin_host(void *ptr);
+
+/* Direct counterpart of Corr::multiTau2(SparseData*, G2, IP, IF)
+ * (corr.h:98, corr.cpp:315-431) for callers that already hold pixel-major
+ * event lists: row_ptr [pixels+1] (int64), frame/value [row_ptr[pixels]]
+ * (Row::indxPtr / Row::valPtr, frames ascending within a row).  Outputs
+ * G2/IP/IF float32 [D][pixels] on the host.  Unlike the reference, the input
+ * rows are not modified.  Runs on `device`, synchronously. */
+int xpcs_multitau2(const int64_t *row_ptr, const int32_t *frame, const float *value,
+                   int32_t pixels, int32_t frames, int32_t delays_per_level, int32_t mode,
+                   int32_t device, float *G2, float *IP, float *IF);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -252,11 +252,14 @@ def dense_filter(qm: QMap, raw, frames, dark_avg=None, dark_std=None, lld=0.0, s
     rows_s, side_s = _Rows(), _Side()
     da = np.ascontiguousarray(dark_avg, np.float64) if dark_avg is not None else None
     ds = np.ascontiguousarray(dark_std, np.float64) if dark_std is not None else None
+    ck = np.ascontiguousarray(clock, np.float64) if clock is not None else None
+    tk = np.ascontiguousarray(ticks, np.float64) if ticks is not None else None
     lib().xo_dense_filter(
         C.byref(fp), _p(raw, C.c_int16),
         _p(da, C.c_double) if da is not None else None,
         _p(ds, C.c_double) if ds is not None else None,
-        C.c_float(lld), C.c_float(sigma), None, None, C.byref(rows_s), C.byref(side_s))
+        C.c_float(lld), C.c_float(sigma), _p(ck, C.c_double) if ck is not None else None,
+        _p(tk, C.c_double) if tk is not None else None, C.byref(rows_s), C.byref(side_s))
     return _collect(rows_s, side_s, fp, qm, finish)
 
 

@@ -1,0 +1,156 @@
+"""GPU parity through the C ABI: libxpcs_gpu against the reference's own
+outputs (golden fixtures) and against the oracle.
+
+Bars: G2/IP/IF and the float32 g2/stderr bit-identical to the reference
+(NaN positions compared as NaN); float64 g2/stderr within 1e-12 relative of
+the float64 oracle evaluated on the same G2/IP/IF."""
+import numpy as np
+import pytest
+
+import oracle
+import xpcs_gpu as xg
+import xpcs_synth as xs
+from fixtures import (SPARSE_CASES, frames_of, load, max_rel_err, oracle_run, same_bits,
+                      same_bits_nan)
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-12
+
+
+def series_for(fx):
+    return xg.Series(fx["W"], fx["H"], fx["F"], fx["dpl"], fx["dqmap"], fx["sqmap"],
+                     flatfield=fx["flatfield"], stride=fx["stride"], average=fx["avg"],
+                     static_window=fx["swin"])
+
+
+def run_gpu(fx, mode=xg.MODE_REFERENCE, chunks=1):
+    with series_for(fx) as s:
+        for nnz, idx, val in frames_of(fx, chunks):
+            s.ingest_sparse(nnz, idx, val)
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+        info = s.info()
+    return dict(G2=G2, IP=IP, IF=IF, g64=g64, s64=s64, g32=g32, s32=s32, info=info)
+
+
+@pytest.mark.parametrize("case", SPARSE_CASES)
+def test_g2ipif_bit_exact_vs_reference(case):
+    fx = load(case)
+    r = run_gpu(fx)
+    for k in ("G2", "IP", "IF"):
+        assert same_bits(r[k], fx["ref_" + k]), k
+
+
+@pytest.mark.parametrize("case", SPARSE_CASES)
+def test_normalize_f32_bit_exact_vs_reference(case):
+    fx = load(case)
+    r = run_gpu(fx)
+    assert same_bits_nan(r["g32"], fx["ref_norm_0_g2"])
+    assert same_bits_nan(r["s32"], fx["ref_norm_0_stderr"])
+
+
+@pytest.mark.parametrize("case", SPARSE_CASES)
+def test_normalize_f64_vs_oracle(case):
+    fx = load(case)
+    r = run_gpu(fx)
+    qm = oracle.QMap(fx["dqmap"], fx["sqmap"])
+    g64, s64 = oracle.normalize_f64(qm, fx["ref_G2"], fx["ref_IP"], fx["ref_IF"])
+    assert max_rel_err(r["g64"], g64) <= F64_TOL
+    assert max_rel_err(r["s64"], s64) <= F64_TOL
+
+
+def test_exact_mode_vs_oracle():
+    fx = load("sparse_quirk")
+    r = run_gpu(fx, mode=xg.MODE_EXACT)
+    o = oracle_run(fx, mode=1)
+    for k in ("G2", "IP", "IF"):
+        assert same_bits(r[k], o[k]), k
+    assert (r["G2"] != fx["ref_G2"]).sum() > 0  # quirk Q1 is exercised
+
+
+@pytest.mark.parametrize("case", SPARSE_CASES)
+@pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
+def test_multitau2_on_caller_rows(case, mode):
+    fx = load(case)
+    _, rows, _ = __import__("fixtures").oracle_filter(fx)
+    G2, IP, IF = xg.multitau2(rows.row_ptr, rows.frame, rows.value, fx["F"], fx["dpl"], mode)
+    oG2, oIP, oIF = oracle.multitau2(rows, fx["F"], fx["dpl"], mode)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
+def test_chunked_ingest_and_reset_are_identical():
+    fx = load("sparse_stride_avg")
+    a = run_gpu(fx, chunks=1)
+    b = run_gpu(fx, chunks=7)
+    for k in ("G2", "IP", "IF", "g32", "s32"):
+        assert same_bits(a[k], b[k]), k
+    with series_for(fx) as s:
+        for _ in range(2):
+            s.reset()
+            for nnz, idx, val in frames_of(fx, 3):
+                s.ingest_sparse(nnz, idx, val)
+            s.multitau()
+            G2, IP, IF = s.g2ipif()
+            assert same_bits(G2, a["G2"]) and same_bits(IF, a["IF"])
+
+
+@pytest.mark.parametrize("case", SPARSE_CASES)
+def test_event_counts_match_oracle(case):
+    fx = load(case)
+    r = run_gpu(fx)
+    _, rows, _ = __import__("fixtures").oracle_filter(fx)
+    n = np.diff(rows.row_ptr)
+    assert r["info"].events == int(n.sum())
+    assert r["info"].valid_pixels == int((n > 0).sum())
+
+
+def test_float_path_is_used_for_hot_and_flatfield_pixels():
+    assert run_gpu(load("sparse_hot"))["info"].float_path_pixels >= 3
+    assert run_gpu(load("sparse_flat"))["info"].float_path_pixels > 0
+    assert run_gpu(load("sparse_basic"))["info"].float_path_pixels == 0
+
+
+def test_pixel_index_out_of_range_is_an_input_error():
+    fx = load("sparse_basic")
+    with series_for(fx) as s:
+        idx = fx["idx"].copy()
+        idx[5] = fx["W"] * fx["H"] + 3
+        s.ingest_sparse(fx["nnz"], idx, fx["val"])
+        s.multitau()
+        with pytest.raises(xg.XpcsError) as e:
+            s.g2ipif()
+        assert e.value.code == 6
+
+
+def test_no_frames_gives_zero_correlations():
+    fx = load("sparse_basic")
+    with series_for(fx) as s:
+        s.multitau()
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+    assert not G2.any() and not IP.any() and not IF.any()
+    qm = oracle.QMap(fx["dqmap"], fx["sqmap"])
+    og, os_ = oracle.normalize_f32(qm, G2, IP, IF)
+    assert same_bits_nan(g32, og) and same_bits_nan(s32, os_)
+
+
+def test_config0_full_size_vs_oracle():
+    """512x512, 1000 frames, dpl 4 (the reference's CPU-runnable case)."""
+    acq = xs.preset("c0")
+    dq, sq, _, _ = xs.maps(acq)
+    nnz, idx, val = xs.sparse_frames(acq)
+    with xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau()
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, acq.frames)
+    oG2, oIP, oIF = oracle.multitau2(rows, acq.frames, acq.dpl, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+    og, os_ = oracle.normalize_f32(qm, oG2, oIP, oIF)
+    assert same_bits_nan(g32, og) and same_bits_nan(s32, os_)
+    o64, s64o = oracle.normalize_f64(qm, oG2, oIP, oIF)
+    assert max_rel_err(g64, o64) <= F64_TOL and max_rel_err(s64, s64o) <= F64_TOL

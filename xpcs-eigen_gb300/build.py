@@ -1,0 +1,95 @@
+"""Build recipe for the native parts of xpcs-eigen_gb300.
+
+  libxpcs_gpu.so    CUDA kernels + C ABI (include/xpcs_gpu.h), sm_103a only
+  libxpcs_synth.so  seeded synthetic acquisitions (benchmark/test inputs)
+  corr              C++ command-line driver with the reference's flags
+
+Everything is compiled in-tree into xpcs-eigen_gb300/_build/.  Translation
+units are compiled in parallel; no cmake.  Float code is compiled without
+fused multiply-add contraction (-fmad=false, -ffp-contract=off) because the
+kernels reproduce the reference's float arithmetic bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+BUILD = PKG / "_build"
+OBJ = BUILD / "obj"
+INCLUDE = ROOT / "include"
+CSRC = PKG / "csrc"
+
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+                     "-I", str(INCLUDE), "-I", str(CSRC)]
+GPU_SOURCES = ["abi.cu", "scan.cu", "k_transpose.cu", "k_multitau.cu", "k_normalize.cu",
+               "qmap.cpp"]
+
+LIB_GPU = BUILD / "libxpcs_gpu.so"
+LIB_SYNTH = BUILD / "libxpcs_synth.so"
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(map(str, cmd)) + "\n" + r.stdout + r.stderr)
+    return r
+
+
+def _stale(target: Path, deps) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def build_gpu(force: bool = False, verbose: bool = False) -> Path:
+    OBJ.mkdir(parents=True, exist_ok=True)
+    headers = [INCLUDE / "xpcs_gpu.h", CSRC / "xpcs_internal.h"]
+    jobs = []
+    objs = []
+    for src in GPU_SOURCES:
+        s = CSRC / src
+        o = OBJ / (s.stem + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            cmd = [NVCC] + NVCC_FLAGS + (["-Xptxas", "-v"] if verbose else []) + [
+                "-c", str(s), "-o", str(o)]
+            if src.endswith(".cpp"):
+                cmd = [NVCC] + NVCC_FLAGS + ["-x", "cu", "-c", str(s), "-o", str(o)]
+            jobs.append(cmd)
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            for r in ex.map(_run, jobs):
+                if verbose and r.stderr:
+                    print(r.stderr, file=sys.stderr)
+    if force or _stale(LIB_GPU, objs):
+        _run([NVCC] + ARCH + ["-shared", "-o", str(LIB_GPU)] + [str(o) for o in objs])
+    return LIB_GPU
+
+
+def build_synth(force: bool = False) -> Path:
+    BUILD.mkdir(parents=True, exist_ok=True)
+    src = PKG / "synth" / "xpcs_synth.cpp"
+    if force or _stale(LIB_SYNTH, [src, PKG / "synth" / "xpcs_synth.h"]):
+        _run(["g++", "-std=c++17", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+              "-o", str(LIB_SYNTH), str(src)])
+    return LIB_SYNTH
+
+
+def build_all(force: bool = False) -> None:
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        futs = [ex.submit(build_gpu, force), ex.submit(build_synth, force)]
+        for f in futs:
+            f.result()
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv)
+    print("built", LIB_GPU, LIB_SYNTH)

@@ -1,0 +1,425 @@
+// C ABI of libxpcs_gpu (include/xpcs_gpu.h): series lifecycle, ingest,
+// multi-tau, normalisation, results and the per-stage CUDA-event tracer.
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "xpcs_internal.h"
+
+using namespace xg;
+
+namespace xg {
+thread_local int64_t tl_launches = 0;
+}
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    f();
+    g_last_error.clear();
+    return XPCS_OK;
+  } catch (const Error &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return XPCS_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return XPCS_ERR_INVALID_ARGUMENT;
+  }
+}
+
+void need(bool ok, const char *msg) {
+  if (!ok) throw Error(XPCS_ERR_INVALID_ARGUMENT, msg);
+}
+
+template <class T>
+void upload(DBuf<T> &b, const std::vector<T> &v, cudaStream_t st) {
+  b.reserve(v.size() ? v.size() : 1, st);
+  if (!v.empty())
+    XG_CUDA(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+}
+
+// Wait for the stream and turn device error words into a status.
+void sync_and_check(Series &s) {
+  XG_CUDA(cudaStreamSynchronize(s.stream));
+  if (s.stats.p) {
+    DevStats st{};
+    XG_CUDA(cudaMemcpy(&st, s.stats.p, sizeof(DevStats), cudaMemcpyDeviceToHost));
+    if (st.error & DEVERR_PIXEL_INDEX)
+      throw Error(XPCS_ERR_INPUT, "a sparse frame holds a pixel index outside the detector");
+  }
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) XG_CUDA(cudaSetDevice(dev));
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+void init_series(Series &s) {
+  XG_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+  for (auto &e : s.ev) XG_CUDA(cudaEventCreate(&e));
+  s.cap = multitau_cap(s.D);
+}
+
+void free_series(Series *s) {
+  if (!s) return;
+  if (s->stream) {
+    DeviceGuard g(s->device);
+    cudaStream_t st = s->stream;
+    cudaStreamSynchronize(st);
+    DBuf<int32_t> *i32[] = {&s->raw_idx, &s->frA, &s->frB, &s->cnt, &s->row_len,
+                            &s->flist, &s->ev_frame, &s->sc_frame, &s->n_q_entry_ptr,
+                            &s->n_entry_sbin, &s->n_entry_pix_ptr, &s->n_pix, &s->n_q_row};
+    for (auto *b : i32) b->release(st);
+    DBuf<float> *f32[] = {&s->vA, &s->vB, &s->ev_val, &s->pixels_sum, &s->sc_val, &s->G2,
+                          &s->IP, &s->IF, &s->n_ratio32, &s->n_g2f, &s->n_sef};
+    for (auto *b : f32) b->release(st);
+    s->raw_val.release(st);
+    s->d_frame_off.release(st);
+    s->row_ptr.release(st);
+    s->d_mask.release(st);
+    s->pclass.release(st);
+    s->scan_tmp.release(st);
+    s->plan.release(st);
+    s->d_flat.release(st);
+    s->n_ratio64.release(st);
+    s->n_g2.release(st);
+    s->n_se.release(st);
+    s->keyA.release(st);
+    s->keyB.release(st);
+    s->hist.release(st);
+    s->hist_scan.release(st);
+    s->stats.release(st);
+    cudaStreamSynchronize(st);
+    for (auto &e : s->ev)
+      if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(st);
+  }
+  delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xpcs_abi_version(void) { return XPCS_GPU_ABI_VERSION; }
+
+const char *xpcs_last_error(void) { return g_last_error.c_str(); }
+
+int xpcs_delay_schedule(int32_t frames, int32_t dpl, int32_t *level, int32_t *tau,
+                        int32_t capacity, int32_t *count) {
+  return guarded([&] {
+    need(frames >= 0 && dpl >= 0 && capacity >= 0, "negative argument");
+    DelaySchedule d = delay_schedule(frames, dpl);
+    int n = (int)d.level.size();
+    for (int k = 0; k < n && k < capacity; k++) {
+      if (level) level[k] = d.level[k];
+      if (tau) tau[k] = d.tau[k];
+    }
+    if (count) *count = n;
+  });
+}
+
+int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out) {
+  Series *s = nullptr;
+  int rc = guarded([&] {
+    need(desc && out, "null argument");
+    need(desc->width > 0 && desc->height > 0, "detector size must be positive");
+    need((int64_t)desc->width * desc->height < (int64_t)1 << 30, "detector too large");
+    need(desc->frames >= 0, "frame count must be non-negative");
+    need(desc->delays_per_level >= 0, "delays_per_level must be non-negative");
+    need(desc->stride_frames >= 1 && desc->avg_frames >= 1, "stride/avg must be >= 1");
+    need(desc->static_window >= 1, "static_window must be >= 1");
+    need(desc->dqmap && desc->sqmap, "dqmap and sqmap are required");
+    need(desc->dense == 0, "dense frames are not supported by this build of the series API");
+    s = new Series();
+    s->desc = *desc;
+    s->desc.dqmap = nullptr;
+    s->desc.sqmap = nullptr;
+    s->desc.flatfield = nullptr;
+    s->device = desc->device;
+    s->P = desc->width * desc->height;
+    s->F = desc->frames;
+    s->R_in = desc->stride_frames * desc->avg_frames;
+    s->delays = delay_schedule(s->F, desc->delays_per_level);
+    s->D = (int32_t)s->delays.level.size();
+    s->qmap = build_qmap(desc->dqmap, desc->sqmap, s->P);
+    if (!s->qmap.error.empty()) throw Error(XPCS_ERR_QMAP, s->qmap.error);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      throw Error(XPCS_ERR_NO_DEVICE, "no CUDA device");
+    need(desc->device >= 0 && desc->device < ndev, "device ordinal out of range");
+    DeviceGuard g(s->device);
+    init_series(*s);
+    cudaStream_t st = s->stream;
+    upload(s->d_mask, s->qmap.valid, st);
+    if (desc->flatfield) {
+      std::vector<double> flat(desc->flatfield, desc->flatfield + s->P);
+      upload(s->d_flat, flat, st);
+      s->has_flat = true;
+    }
+    const QMap &q = s->qmap;
+    upload(s->n_q_entry_ptr, q.q_entry_ptr, st);
+    upload(s->n_entry_sbin, q.entry_sbin, st);
+    upload(s->n_entry_pix_ptr, q.entry_pix_ptr, st);
+    upload(s->n_pix, q.pix, st);
+    std::vector<int32_t> rows(q.q_ids.size());
+    for (size_t k = 0; k < rows.size(); k++) rows[k] = q.q_ids[k] - 1;
+    upload(s->n_q_row, rows, st);
+    XG_CUDA(cudaStreamSynchronize(st));
+    *out = (xpcs_series *)s;
+  });
+  if (rc != XPCS_OK && s) free_series(s);
+  return rc;
+}
+
+void xpcs_series_destroy(xpcs_series *h) { free_series((Series *)h); }
+
+int xpcs_series_reset(xpcs_series *h) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    XG_CUDA(cudaStreamSynchronize(s.stream));
+    s.frame_off.assign(1, 0);
+    s.raw_events = 0;
+    s.raw_frames = 0;
+    s.frame_off_dirty = true;
+    s.have_multitau = false;
+    s.timed_h2d = false;
+    s.h2d_ms_acc = 0.f;
+  });
+}
+
+int xpcs_series_get_info(xpcs_series *h, xpcs_series_info *info) {
+  return guarded([&] {
+    need(h && info, "null argument");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    sync_and_check(s);
+    std::memset(info, 0, sizeof(*info));
+    info->pixels = s.P;
+    info->delays = s.D;
+    info->total_static = s.qmap.total_static;
+    info->total_dynamic = s.qmap.total_dynamic;
+    info->qbins = s.qmap.nq();
+    info->raw_frames = s.raw_frames;
+    info->raw_events = s.raw_events;
+    if (s.have_multitau && s.stats.p) {
+      DevStats st{};
+      XG_CUDA(cudaMemcpy(&st, s.stats.p, sizeof(st), cudaMemcpyDeviceToHost));
+      info->events = (int64_t)st.events;
+      info->valid_pixels = st.nvalid;
+      info->float_path_pixels = st.nfloat;
+    }
+  });
+}
+
+static void ingest_common(Series &s, const int32_t *idx, const int16_t *val, const uint32_t *nnz,
+                          int32_t nframes, bool on_device) {
+  need(nframes >= 0, "negative frame count");
+  need(nnz || nframes == 0, "null nnz");
+  DeviceGuard g(s.device);
+  cudaStream_t st = s.stream;
+  int64_t add = 0;
+  for (int32_t r = 0; r < nframes; r++) add += nnz[r];
+  need(add == 0 || (idx && val), "null event arrays");
+  const int64_t old = s.raw_events, tot = old + add;
+  need(tot < ((int64_t)1 << 32), "more than 2^32 raw events in one series");
+  s.raw_idx.grow((size_t)(tot ? tot : 1), (size_t)old, st);
+  s.raw_val.grow((size_t)(tot ? tot : 1), (size_t)old, st);
+  if (!s.timed_h2d) {
+    XG_CUDA(cudaEventRecord(s.ev[0], st));
+    s.timed_h2d = true;
+  }
+  if (add) {
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    XG_CUDA(cudaMemcpyAsync(s.raw_idx.p + old, idx, sizeof(int32_t) * add, kind, st));
+    XG_CUDA(cudaMemcpyAsync(s.raw_val.p + old, val, sizeof(int16_t) * add, kind, st));
+  }
+  XG_CUDA(cudaEventRecord(s.ev[1], st));
+  for (int32_t r = 0; r < nframes; r++) s.frame_off.push_back(s.frame_off.back() + nnz[r]);
+  s.raw_events = tot;
+  s.raw_frames += nframes;
+  s.frame_off_dirty = true;
+  s.have_multitau = false;
+}
+
+int xpcs_ingest_sparse(xpcs_series *h, const int32_t *idx, const int16_t *val,
+                       const uint32_t *nnz, int32_t nframes) {
+  return guarded([&] {
+    need(h, "null handle");
+    ingest_common(*(Series *)h, idx, val, nnz, nframes, false);
+  });
+}
+
+int xpcs_ingest_sparse_device(xpcs_series *h, const int32_t *idx, const int16_t *val,
+                              const uint32_t *nnz, int32_t nframes) {
+  return guarded([&] {
+    need(h, "null handle");
+    ingest_common(*(Series *)h, idx, val, nnz, nframes, true);
+  });
+}
+
+int xpcs_multitau(xpcs_series *h, int32_t mode) {
+  return guarded([&] {
+    need(h, "null handle");
+    need(mode == XPCS_MODE_REFERENCE || mode == XPCS_MODE_EXACT, "unknown mode");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    const int64_t l0 = tl_launches;
+    XG_CUDA(cudaEventRecord(s.ev[2], s.stream));
+    run_filter_transpose(s);
+    XG_CUDA(cudaEventRecord(s.ev[3], s.stream));
+    run_multitau(s, mode);
+    s.launches = (int32_t)(tl_launches - l0);
+    s.have_multitau = true;
+    s.timed_h2d = false;
+  });
+}
+
+int xpcs_get_g2ipif(xpcs_series *h, float *G2, float *IP, float *IF) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if (!s.have_multitau) throw Error(XPCS_ERR_STATE, "xpcs_multitau has not run");
+    DeviceGuard g(s.device);
+    const size_t n = (size_t)s.D * s.P;
+    XG_CUDA(cudaEventRecord(s.ev[9], s.stream));
+    if (G2 && n) XG_CUDA(cudaMemcpyAsync(G2, s.G2.p, 4 * n, cudaMemcpyDeviceToHost, s.stream));
+    if (IP && n) XG_CUDA(cudaMemcpyAsync(IP, s.IP.p, 4 * n, cudaMemcpyDeviceToHost, s.stream));
+    if (IF && n) XG_CUDA(cudaMemcpyAsync(IF, s.IF.p, 4 * n, cudaMemcpyDeviceToHost, s.stream));
+    XG_CUDA(cudaEventRecord(s.ev[10], s.stream));
+    sync_and_check(s);
+  });
+}
+
+int xpcs_normalize(xpcs_series *h, double *g2, double *se, float *g2f, float *sef) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if (!s.have_multitau) throw Error(XPCS_ERR_STATE, "xpcs_multitau has not run");
+    DeviceGuard g(s.device);
+    cudaStream_t st = s.stream;
+    const bool w64 = g2 || se, w32 = g2f || sef;
+    const int64_t l0 = tl_launches;
+    XG_CUDA(cudaEventRecord(s.ev[7], st));
+    run_normalize(s, w64, w32);
+    s.launches += (int32_t)(tl_launches - l0);
+    XG_CUDA(cudaEventRecord(s.ev[8], st));
+    const size_t n = (size_t)s.D * s.qmap.nq();
+    if (n) {
+      if (g2) XG_CUDA(cudaMemcpyAsync(g2, s.n_g2.p, 8 * n, cudaMemcpyDeviceToHost, st));
+      if (se) XG_CUDA(cudaMemcpyAsync(se, s.n_se.p, 8 * n, cudaMemcpyDeviceToHost, st));
+      if (g2f) XG_CUDA(cudaMemcpyAsync(g2f, s.n_g2f.p, 4 * n, cudaMemcpyDeviceToHost, st));
+      if (sef) XG_CUDA(cudaMemcpyAsync(sef, s.n_sef.p, 4 * n, cudaMemcpyDeviceToHost, st));
+    }
+    XG_CUDA(cudaEventRecord(s.ev[11], st));
+    sync_and_check(s);
+  });
+}
+
+int xpcs_synchronize(xpcs_series *h) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    sync_and_check(s);
+  });
+}
+
+int xpcs_get_stage_times(xpcs_series *h, xpcs_stage_times *t) {
+  return guarded([&] {
+    need(h && t, "null argument");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    XG_CUDA(cudaStreamSynchronize(s.stream));
+    auto el = [&](int a, int b) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, s.ev[a], s.ev[b]) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.f;
+      }
+      return ms;
+    };
+    std::memset(t, 0, sizeof(*t));
+    t->h2d_ms = el(0, 1);
+    t->filter_ms = el(2, 3);
+    t->multitau_ms = el(3, 6);
+    t->multitau_int_ms = el(4, 5);
+    t->multitau_float_ms = el(5, 6);
+    t->normalize_ms = el(7, 8);
+    t->d2h_ms = el(8, 11);
+    t->step_ms = el(2, 11);
+    t->launches = s.launches;
+  });
+}
+
+int xpcs_pin_host(void *ptr, uint64_t bytes) {
+  return guarded([&] {
+    need(ptr && bytes > 0, "null or empty buffer");
+    XG_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+  });
+}
+
+int xpcs_unpin_host(void *ptr) {
+  return guarded([&] {
+    need(ptr, "null buffer");
+    XG_CUDA(cudaHostUnregister(ptr));
+  });
+}
+
+int xpcs_multitau2(const int64_t *row_ptr, const int32_t *frame, const float *value,
+                   int32_t pixels, int32_t frames, int32_t dpl, int32_t mode, int32_t device,
+                   float *G2, float *IP, float *IF) {
+  Series *s = nullptr;
+  int rc = guarded([&] {
+    need(row_ptr && pixels > 0 && frames >= 0 && dpl >= 0, "bad argument");
+    need(mode == XPCS_MODE_REFERENCE || mode == XPCS_MODE_EXACT, "unknown mode");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      throw Error(XPCS_ERR_NO_DEVICE, "no CUDA device");
+    need(device >= 0 && device < ndev, "device ordinal out of range");
+    const int64_t E = row_ptr[pixels];
+    need(E >= 0 && row_ptr[0] == 0, "row_ptr must start at 0");
+    need(E == 0 || (frame && value), "null event arrays");
+    for (int32_t p = 0; p < pixels; p++)
+      need(row_ptr[p + 1] >= row_ptr[p], "row_ptr must be non-decreasing");
+    s = new Series();
+    s->device = device;
+    DeviceGuard g(device);
+    s->P = pixels;
+    s->F = frames;
+    s->desc.delays_per_level = dpl;
+    s->delays = delay_schedule(frames, dpl);
+    s->D = (int32_t)s->delays.level.size();
+    init_series(*s);
+    multitau_rows_upload(*s, row_ptr, frame, value, E);
+    run_multitau(*s, mode);
+    const size_t n = (size_t)s->D * pixels;
+    if (n) {
+      if (G2) XG_CUDA(cudaMemcpyAsync(G2, s->G2.p, 4 * n, cudaMemcpyDeviceToHost, s->stream));
+      if (IP) XG_CUDA(cudaMemcpyAsync(IP, s->IP.p, 4 * n, cudaMemcpyDeviceToHost, s->stream));
+      if (IF) XG_CUDA(cudaMemcpyAsync(IF, s->IF.p, 4 * n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    XG_CUDA(cudaStreamSynchronize(s->stream));
+  });
+  free_series(s);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,413 @@
+// K-a: sparse-frame filter and pixel-major transpose.
+//
+// Replaces SparseFilter::Apply (src/xpcs/filter/sparse_filter.cpp:115-193),
+// which walks every frame and pushes (frame, value) onto per-pixel std::vector
+// rows.  Here the raw frame-major event stream (int32 pixel index, int16 value)
+// is filtered and stably sorted by pixel with an LSD radix sort, so that every
+// pixel's events come out contiguous and in stream order (frame order).
+//
+//   pass 0   reads the raw events directly: per event it derives the filter
+//            frame (raw frame / (stride*avg)), drops masked pixels, unused
+//            stride sub-frames and frames past the end (key = P, sorts last),
+//            and forms v = (float)(value * flatfield) as the reference does
+//            (sparse_filter.cpp:149-153).
+//   pass k   8-bit digit k of the pixel index: tile histograms -> digit-major
+//            exclusive scan -> stable scatter.  Ranking inside a tile uses
+//            warp match_any + per-warp digit counters, so equal digits keep
+//            stream order (tile, warp, round, lane).
+//   merge    one thread per pixel sums events of the same filter frame in
+//            stream order, divides by avg (sparse_filter.cpp:160-172),
+//            accumulates pixelSum in frame order and classifies the pixel for
+//            the multi-tau kernels.
+#include "xpcs_internal.h"
+
+namespace xg {
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_IPT = 16;                      // items per lane
+constexpr int RS_TILE = RS_THREADS * RS_IPT;    // 4096
+constexpr int RS_DIGITS = 256;
+
+struct RawCfg {
+  const int32_t *idx;
+  const int16_t *val;
+  const int64_t *frame_off;  // [nframes+1]
+  int32_t nframes;
+  int64_t n;
+  int32_t P, F, R_in, stride;
+  const uint8_t *mask;
+  const double *flat;  // may be null
+  DevStats *stats;
+};
+
+struct PassCfg {
+  const uint32_t *key_in;
+  const int32_t *fr_in;
+  const float *v_in;
+  uint32_t *key_out;  // null on the last pass
+  int32_t *fr_out;
+  float *v_out;
+  int64_t n;
+  int shift;
+  int ntiles;
+  uint32_t sentinel;
+};
+
+// first raw frame r with frame_off[r+1] > i
+__device__ __forceinline__ int32_t frame_of(const RawCfg &c, int64_t i) {
+  int32_t lo = 0, hi = c.nframes - 1;
+  while (lo < hi) {
+    int32_t mid = (lo + hi + 1) >> 1;
+    if (c.frame_off[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r, uint32_t &key,
+                                         int32_t &frame, float &v) {
+  while (c.frame_off[r + 1] <= i) r++;
+  const int32_t k = r / c.R_in;
+  const int32_t sub = r - k * c.R_in;
+  const int32_t p = c.idx[i];
+  const float raw = (float)c.val[i];
+  frame = k;
+  if (p < 0 || p >= c.P) {
+    c.stats->error |= DEVERR_PIXEL_INDEX;
+    key = (uint32_t)c.P;
+    v = 0.f;
+    return;
+  }
+  key = (k < c.F && (sub % c.stride) == 0 && c.mask[p]) ? (uint32_t)p : (uint32_t)c.P;
+  v = c.flat ? __double2float_rn(__dmul_rn((double)raw, c.flat[p])) : raw;
+}
+
+// Item i of a tile in warp-striped order: warp w owns [w*32*IPT, (w+1)*32*IPT),
+// round k, lane l -> w*32*IPT + k*32 + l.
+__device__ __forceinline__ int64_t item_index(int tile, int w, int k, int lane) {
+  return (int64_t)tile * RS_TILE + (int64_t)w * 32 * RS_IPT + k * 32 + lane;
+}
+
+template <bool FIRST>
+__global__ void __launch_bounds__(RS_THREADS)
+k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restrict__ cnt) {
+  __shared__ uint32_t h[RS_DIGITS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
+  for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS) h[d] = 0;
+  __syncthreads();
+  int32_t r = 0;
+  if (FIRST) {
+    int64_t i0 = item_index(tile, w, 0, lane);
+    r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
+  }
+#pragma unroll 4
+  for (int k = 0; k < RS_IPT; k++) {
+    int64_t i = item_index(tile, w, k, lane);
+    if (i >= pc.n) break;
+    uint32_t key;
+    if (FIRST) {
+      int32_t fr;
+      float v;
+      raw_item(rc, i, r, key, fr, v);
+      if (key != pc.sentinel) atomicAdd(&cnt[key], 1);
+    } else {
+      key = pc.key_in[i];
+    }
+    atomicAdd(&h[(key >> pc.shift) & (RS_DIGITS - 1)], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
+    hist[(int64_t)d * pc.ntiles + tile] = h[d];
+}
+
+template <bool FIRST, bool LAST>
+__global__ void __launch_bounds__(RS_THREADS)
+k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
+  __shared__ uint32_t wcnt[RS_WARPS][RS_DIGITS];
+  __shared__ uint32_t toff[RS_DIGITS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
+  for (int d = lane; d < RS_DIGITS; d += 32) wcnt[w][d] = 0;
+  for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
+    toff[d] = offsets[(int64_t)d * pc.ntiles + tile];
+  __syncwarp();
+
+  uint32_t key[RS_IPT];
+  int32_t fr[RS_IPT];
+  float v[RS_IPT];
+  uint32_t rank[RS_IPT];
+  int32_t r = 0;
+  if (FIRST) {
+    int64_t i0 = item_index(tile, w, 0, lane);
+    r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
+  }
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    int64_t i = item_index(tile, w, k, lane);
+    bool ok = i < pc.n;
+    if (ok) {
+      if (FIRST) {
+        raw_item(rc, i, r, key[k], fr[k], v[k]);
+      } else {
+        key[k] = pc.key_in[i];
+        fr[k] = pc.fr_in[i];
+        v[k] = pc.v_in[i];
+      }
+    } else {
+      key[k] = 0xffffffffu;
+    }
+    uint32_t d = ok ? ((key[k] >> pc.shift) & (RS_DIGITS - 1)) : RS_DIGITS;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (ok && lane == leader) {
+      base = wcnt[w][d];
+      wcnt[w][d] = base + __popc(peers);
+    }
+    base = __shfl_sync(0xffffffffu, base, leader);
+    rank[k] = base + __popc(peers & lt);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int ww = 0; ww < RS_WARPS; ww++) {
+      uint32_t c = wcnt[ww][d];
+      wcnt[ww][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    if (key[k] == 0xffffffffu) continue;
+    if (LAST && key[k] == pc.sentinel) continue;
+    uint32_t d = (key[k] >> pc.shift) & (RS_DIGITS - 1);
+    uint32_t pos = toff[d] + wcnt[w][d] + rank[k];
+    if (!LAST) pc.key_out[pos] = key[k];
+    pc.fr_out[pos] = fr[k];
+    pc.v_out[pos] = v[k];
+  }
+}
+
+// One thread per pixel: merge events of the same filter frame (stream order,
+// float sums exactly as pixels_value_[pix] += v, then / avg), accumulate
+// pixelSum in frame order, classify for the multi-tau kernels.
+__global__ void k_merge_classify(int32_t P, int32_t avg, int32_t cap, const int32_t *__restrict__ cnt,
+                                 const int64_t *__restrict__ row_ptr, int32_t *__restrict__ fr,
+                                 float *__restrict__ val, int32_t *__restrict__ row_len,
+                                 uint8_t *__restrict__ pclass, int32_t *__restrict__ flist,
+                                 float *__restrict__ pixels_sum, DevStats *__restrict__ stats) {
+  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int32_t n = cnt[p];
+  if (n == 0) {
+    row_len[p] = 0;
+    pclass[p] = PCLASS_EMPTY;
+    pixels_sum[p] = 0.f;
+    return;
+  }
+  const int64_t b = row_ptr[p];
+  const float favg = (float)avg;
+  int32_t out = 0, i = 0;
+  float psum = 0.f;
+  bool integral = true;
+  long long total = 0;
+  while (i < n) {
+    int32_t f = fr[b + i];
+    float acc = 0.f;
+    do {
+      acc = __fadd_rn(acc, val[b + i]);
+      i++;
+    } while (i < n && fr[b + i] == f);
+    float x = __fdiv_rn(acc, favg);
+    fr[b + out] = f;
+    val[b + out] = x;
+    out++;
+    psum = __fadd_rn(psum, x);
+    if (integral) {
+      if (x == truncf(x) && fabsf(x) < 16777216.f)
+        total += llabs((long long)x);
+      else
+        integral = false;
+    }
+  }
+  row_len[p] = out;
+  pixels_sum[p] = psum;
+  // integer path: exact while every partial sum stays below 2^24, which
+  // sum|v| < 4096 guarantees for IP, IF, merged values and G2 products
+  bool int_ok = integral && total < 4096 && out <= cap;
+  pclass[p] = int_ok ? PCLASS_INT : PCLASS_FLOAT;
+  if (!int_ok) flist[atomicAdd(&stats->nfloat, 1)] = p;
+  atomicAdd(&stats->nvalid, 1);
+  atomicAdd(&stats->events, (unsigned long long)out);
+}
+
+}  // namespace
+
+void run_filter_transpose(Series &s) {
+  cudaStream_t st = s.stream;
+  const int64_t n = s.raw_events;
+  const int32_t P = s.P;
+  s.cnt.reserve(P, st);
+  s.row_ptr.reserve((size_t)P + 1, st);
+  s.row_len.reserve(P, st);
+  s.pclass.reserve(P, st);
+  s.flist.reserve(P, st);
+  s.pixels_sum.reserve(P, st);
+  s.stats.reserve(1, st);
+  XG_CUDA(cudaMemsetAsync(s.cnt.p, 0, sizeof(int32_t) * P, st));
+  XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
+  size_t nalloc = n > 0 ? (size_t)n : 1;
+  s.ev_frame.reserve(nalloc, st);
+  s.ev_val.reserve(nalloc, st);
+
+  if (s.frame_off_dirty) {
+    s.d_frame_off.reserve(s.frame_off.size(), st);
+    XG_CUDA(cudaMemcpyAsync(s.d_frame_off.p, s.frame_off.data(),
+                            sizeof(int64_t) * s.frame_off.size(), cudaMemcpyHostToDevice, st));
+    s.frame_off_dirty = false;
+  }
+
+  if (n > 0) {
+    int nbits = 32 - __builtin_clz((unsigned)P);  // bits to hold P (the drop key)
+    int passes = (nbits + 7) / 8;
+    int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+    s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
+    s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);
+    size_t ws = scan_workspace_bytes((int64_t)RS_DIGITS * ntiles);
+    size_t ws2 = scan_workspace_bytes(P);
+    s.scan_tmp.reserve(ws > ws2 ? ws : ws2, st);
+    if (passes > 1) {
+      s.keyA.reserve(n, st);
+      s.frA.reserve(n, st);
+      s.vA.reserve(n, st);
+    }
+    if (passes > 2) {
+      s.keyB.reserve(n, st);
+      s.frB.reserve(n, st);
+      s.vB.reserve(n, st);
+    }
+    RawCfg rc{s.raw_idx.p, s.raw_val.p, s.d_frame_off.p, s.raw_frames, n, P, s.F, s.R_in,
+              s.desc.stride_frames, s.d_mask.p, s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
+    uint32_t *kbuf[2] = {s.keyA.p, s.keyB.p};
+    int32_t *fbuf[2] = {s.frA.p, s.frB.p};
+    float *vbuf[2] = {s.vA.p, s.vB.p};
+    for (int pass = 0; pass < passes; pass++) {
+      bool first = pass == 0, last = pass == passes - 1;
+      PassCfg pc{};
+      pc.n = n;
+      pc.shift = 8 * pass;
+      pc.ntiles = ntiles;
+      pc.sentinel = (uint32_t)P;
+      if (!first) {
+        pc.key_in = kbuf[(pass - 1) & 1];
+        pc.fr_in = fbuf[(pass - 1) & 1];
+        pc.v_in = vbuf[(pass - 1) & 1];
+      }
+      if (last) {
+        pc.key_out = nullptr;
+        pc.fr_out = s.ev_frame.p;
+        pc.v_out = s.ev_val.p;
+      } else {
+        pc.key_out = kbuf[pass & 1];
+        pc.fr_out = fbuf[pass & 1];
+        pc.v_out = vbuf[pass & 1];
+      }
+      if (first)
+        k_upsweep<true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+      else
+        k_upsweep<false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+      XG_CHECK_LAUNCH();
+      exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
+      if (first && last)
+        k_downsweep<true, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+      else if (first)
+        k_downsweep<true, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+      else if (last)
+        k_downsweep<false, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+      else
+        k_downsweep<false, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+      XG_CHECK_LAUNCH();
+    }
+  } else {
+    s.scan_tmp.reserve(scan_workspace_bytes(P), st);
+  }
+  exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
+  int bs = 256;
+  k_merge_classify<<<(P + bs - 1) / bs, bs, 0, st>>>(
+      P, s.desc.avg_frames, s.cap, s.cnt.p, s.row_ptr.p, s.ev_frame.p, s.ev_val.p, s.row_len.p,
+      s.pclass.p, s.flist.p, s.pixels_sum.p, s.stats.p);
+  XG_CHECK_LAUNCH();
+}
+
+}  // namespace xg
+
+namespace xg {
+namespace {
+
+// Caller-held rows (xpcs_multitau2): rows stay as given; a pixel takes the
+// integer path only if its frames are strictly increasing within [0, F), its
+// values are integers and sum |v| < 4096.
+__global__ void k_classify_rows(int32_t P, int32_t F, int32_t cap, const int64_t *__restrict__ row_ptr,
+                                const int32_t *__restrict__ fr, const float *__restrict__ val,
+                                int32_t *__restrict__ row_len, uint8_t *__restrict__ pclass,
+                                int32_t *__restrict__ flist, DevStats *__restrict__ stats) {
+  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int64_t b = row_ptr[p];
+  const int32_t n = (int32_t)(row_ptr[p + 1] - b);
+  row_len[p] = n;
+  if (n == 0) {
+    pclass[p] = PCLASS_EMPTY;
+    return;
+  }
+  bool ok = n <= cap;
+  long long total = 0;
+  int32_t prev = -1;
+  for (int32_t i = 0; i < n && ok; i++) {
+    int32_t f = fr[b + i];
+    float x = val[b + i];
+    ok = f > prev && f < F && x == truncf(x) && fabsf(x) < 16777216.f;
+    if (ok) total += llabs((long long)x);
+    prev = f;
+  }
+  ok = ok && total < 4096;
+  pclass[p] = ok ? PCLASS_INT : PCLASS_FLOAT;
+  if (!ok) flist[atomicAdd(&stats->nfloat, 1)] = p;
+  atomicAdd(&stats->nvalid, 1);
+  atomicAdd(&stats->events, (unsigned long long)n);
+}
+
+}  // namespace
+
+void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *frame,
+                          const float *value, int64_t events) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P;
+  size_t ne = events > 0 ? (size_t)events : 1;
+  s.row_ptr.reserve((size_t)P + 1, st);
+  s.row_len.reserve(P, st);
+  s.pclass.reserve(P, st);
+  s.flist.reserve(P, st);
+  s.stats.reserve(1, st);
+  s.ev_frame.reserve(ne, st);
+  s.ev_val.reserve(ne, st);
+  s.raw_events = events;
+  XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
+  XG_CUDA(cudaMemcpyAsync(s.row_ptr.p, row_ptr, sizeof(int64_t) * ((size_t)P + 1),
+                          cudaMemcpyHostToDevice, st));
+  if (events > 0) {
+    XG_CUDA(cudaMemcpyAsync(s.ev_frame.p, frame, sizeof(int32_t) * events, cudaMemcpyHostToDevice, st));
+    XG_CUDA(cudaMemcpyAsync(s.ev_val.p, value, sizeof(float) * events, cudaMemcpyHostToDevice, st));
+  }
+  const int bs = 256;
+  k_classify_rows<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.F, s.cap, s.row_ptr.p, s.ev_frame.p,
+                                                     s.ev_val.p, s.row_len.p, s.pclass.p,
+                                                     s.flist.p, s.stats.p);
+  XG_CHECK_LAUNCH();
+}
+
+}  // namespace xg

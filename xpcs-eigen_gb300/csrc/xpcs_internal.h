@@ -1,0 +1,215 @@
+// Internal declarations of libxpcs_gpu (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "xpcs_gpu.h"
+
+namespace xg {
+
+// ---------------------------------------------------------------- errors
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define XG_CUDA(call)                                                                 \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      throw ::xg::Error(e_ == cudaErrorMemoryAllocation ? XPCS_ERR_OUT_OF_MEMORY      \
+                                                        : XPCS_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));          \
+  } while (0)
+
+// Kernels launched by this thread (the stage tracer reports per-call deltas).
+extern thread_local int64_t tl_launches;
+#define XG_CHECK_LAUNCH()          \
+  do {                             \
+    ::xg::tl_launches++;           \
+    XG_CUDA(cudaGetLastError());   \
+  } while (0)
+
+// Device error word bits (set by kernels, read at synchronisation points).
+enum : int32_t { DEVERR_PIXEL_INDEX = 1 };
+
+// ------------------------------------------------------------ device buffers
+
+// A stream-ordered device allocation that grows on demand.
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  void reserve(size_t n, cudaStream_t st) {
+    if (n <= cap) return;
+    T *q = nullptr;
+    XG_CUDA(cudaMallocAsync((void **)&q, sizeof(T) * n, st));
+    if (p) XG_CUDA(cudaFreeAsync(p, st));
+    p = q;
+    cap = n;
+  }
+  // grow keeping the first `keep` elements
+  void grow(size_t n, size_t keep, cudaStream_t st) {
+    if (n <= cap) return;
+    size_t c = cap ? cap : 1;
+    while (c < n) c *= 2;
+    T *q = nullptr;
+    XG_CUDA(cudaMallocAsync((void **)&q, sizeof(T) * c, st));
+    if (p && keep) XG_CUDA(cudaMemcpyAsync(q, p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, st));
+    if (p) XG_CUDA(cudaFreeAsync(p, st));
+    p = q;
+    cap = c;
+  }
+  void release(cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// ------------------------------------------------------- delays and q-maps
+
+struct DelaySchedule {
+  std::vector<int32_t> level, tau;  // Corr::delaysPerLevel order
+};
+DelaySchedule delay_schedule(int frames, int dpl);
+
+// Configuration::BuildQMap result, flattened in the reference's iteration
+// order (q ascending, sbin ascending, pixels in raster order).
+struct QMap {
+  int32_t pixels = 0, total_static = 0, total_dynamic = 0;
+  std::vector<uint8_t> valid;       // m_validPixelMask
+  std::vector<int32_t> sbin;        // m_sbin (1-based, 0 none)
+  std::vector<int32_t> pixels_per_bin;
+  std::vector<int32_t> q_ids;       // mapping keys
+  std::vector<int32_t> q_entry_ptr; // [nq+1] into entry_*
+  std::vector<int32_t> entry_sbin;  // 1-based sbin of each (q, sbin) entry
+  std::vector<int32_t> entry_pix_ptr;  // [nentries+1]
+  std::vector<int32_t> pix;
+  std::string error;                // non-empty: reference would index out of bounds
+  int32_t nq() const { return (int32_t)q_ids.size(); }
+  int32_t nentries() const { return (int32_t)entry_sbin.size(); }
+};
+QMap build_qmap(const int32_t *dq, const int32_t *sq, int32_t pixels);
+
+// ---------------------------------------------------------- multi-tau plan
+
+constexpr int MAX_LEVELS = 48;
+
+struct McLevel {
+  int32_t level;      // multi-tau level L
+  int32_t first;      // index of its first delay
+  int32_t count;      // delays at this level
+  int32_t lastframe;  // lastframe while this level's delays are evaluated
+  int32_t tau_lo;     // first delay in level units (delays are consecutive)
+  int32_t compact;    // 1: the reference compacts the rows before this level
+};
+
+// Kernel-side description of a multi-tau run; lives in device memory.
+struct McPlan {
+  int32_t P, D, F, nlev, mode, cap;
+  McLevel lv[MAX_LEVELS];
+  // followed in device memory by: int32 tau_lvl[D], float denom[D]
+};
+
+// Pixel classes assigned by the filter's merge pass.
+enum : uint8_t { PCLASS_EMPTY = 0, PCLASS_INT = 1, PCLASS_FLOAT = 2 };
+
+// Counters written by device passes.
+struct DevStats {
+  int32_t error;
+  int32_t nfloat;
+  int32_t nvalid;
+  int32_t pad;
+  unsigned long long events;
+};
+
+// --------------------------------------------------------------- a series
+
+struct Series {
+  xpcs_series_desc desc{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int32_t P = 0, F = 0, D = 0, R_in = 1;
+  DelaySchedule delays;
+  QMap qmap;
+
+  // ingested raw frames
+  std::vector<int64_t> frame_off{0};  // host copy, [raw_frames+1]
+  DBuf<int32_t> raw_idx;
+  DBuf<int16_t> raw_val;
+  DBuf<int64_t> d_frame_off;
+  int64_t raw_events = 0;
+  int32_t raw_frames = 0;
+  bool frame_off_dirty = true;
+
+  // per-pixel constant data
+  DBuf<uint8_t> d_mask;
+  DBuf<double> d_flat;
+  bool has_flat = false;
+
+  // transpose / event lists
+  DBuf<uint32_t> keyA, keyB;
+  DBuf<int32_t> frA, frB;
+  DBuf<float> vA, vB;
+  DBuf<uint32_t> hist, hist_scan;
+  DBuf<int32_t> cnt;        // raw events per pixel
+  DBuf<int64_t> row_ptr;    // [P+1]
+  DBuf<int32_t> row_len;    // events per pixel after merging duplicates
+  DBuf<uint8_t> pclass;
+  DBuf<int32_t> flist;      // pixels of the float path
+  DBuf<int32_t> ev_frame;   // final pixel-major lists
+  DBuf<float> ev_val;
+  DBuf<float> pixels_sum;
+  DBuf<int32_t> sc_frame;   // float-path scratch rows
+  DBuf<float> sc_val;
+  DBuf<uint8_t> scan_tmp;
+  DBuf<DevStats> stats;
+
+  // multi-tau
+  DBuf<uint8_t> plan;       // McPlan + tau_lvl[D] + denom[D]
+  DBuf<float> G2, IP, IF;
+  bool have_multitau = false;
+  int32_t cap = 0;
+
+  // normalisation
+  DBuf<int32_t> n_q_entry_ptr, n_entry_sbin, n_entry_pix_ptr, n_pix, n_q_row;
+  DBuf<float> n_ratio32;
+  DBuf<double> n_ratio64;
+  DBuf<double> n_g2, n_se;
+  DBuf<float> n_g2f, n_sef;
+
+  // tracer
+  cudaEvent_t ev[12] = {};
+  int32_t launches = 0;     // kernels launched since the last xpcs_multitau began
+  bool timed_h2d = false;
+  float h2d_ms_acc = 0.f;
+
+  // host staging for pageable ingests
+  void *pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+
+// Scans (scan.cu)
+size_t scan_workspace_bytes(int64_t n);
+void exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, void *ws, cudaStream_t st);
+void exclusive_scan_i32_i64(const int32_t *in, int64_t *out, int64_t n, void *ws,
+                            cudaStream_t st);
+
+// Kernel launchers
+void run_filter_transpose(Series &s);                       // k_transpose.cu
+void run_multitau(Series &s, int mode);                      // k_multitau.cu
+void run_normalize(Series &s, bool want64, bool want32);     // k_normalize.cu
+int multitau_cap(int D);                                     // int-path row capacity
+
+// Upload caller-held pixel-major rows and classify their pixels (xpcs_multitau2)
+void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *frame,
+                          const float *value, int64_t events);
+
+}  // namespace xg

@@ -1,0 +1,229 @@
+"""Python front end of libxpcs_gpu through its C ABI (include/xpcs_gpu.h).
+
+This is a thin ctypes binding: every call goes to the CUDA library, and the
+import fails loudly when the library cannot be loaded -- there is no CPU
+fallback.  The structure mirrors the reference's `corr` flow:
+
+    s = Series(width, height, frames, dpl, dqmap, sqmap, ...)  # Configuration::init
+    s.ingest_sparse(nnz, idx, val)                             # Imm + SparseFilter
+    s.multitau(MODE_REFERENCE)                                 # Corr::multiTau2
+    G2, IP, IF = s.g2ipif()                                    # --g2out datasets
+    g2, se, g2f, sef = s.normalize()                           # Corr::normalizeG2s
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libxpcs_gpu.so"
+
+MODE_REFERENCE = 0
+MODE_EXACT = 1
+
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "STATE", 5: "QMAP",
+          6: "INPUT", 7: "NO_DEVICE"}
+
+# Exported symbols of include/xpcs_gpu.h (checked by the CPU test suite).
+EXPORTS = [
+    "xpcs_abi_version", "xpcs_last_error", "xpcs_delay_schedule", "xpcs_series_create",
+    "xpcs_series_destroy", "xpcs_series_reset", "xpcs_series_get_info", "xpcs_ingest_sparse",
+    "xpcs_ingest_sparse_device", "xpcs_multitau", "xpcs_get_g2ipif", "xpcs_normalize",
+    "xpcs_synchronize", "xpcs_get_stage_times", "xpcs_multitau2", "xpcs_pin_host",
+    "xpcs_unpin_host",
+]
+
+
+class XpcsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"xpcs {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SeriesDesc(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32), ("frames", C.c_int32),
+        ("delays_per_level", C.c_int32), ("stride_frames", C.c_int32), ("avg_frames", C.c_int32),
+        ("static_window", C.c_int32), ("dqmap", C.POINTER(C.c_int32)),
+        ("sqmap", C.POINTER(C.c_int32)), ("flatfield", C.POINTER(C.c_double)),
+        ("dense", C.c_int32), ("lld", C.c_float), ("sigma", C.c_float), ("device", C.c_int32),
+    ]
+
+
+class SeriesInfo(C.Structure):
+    _fields_ = [
+        ("pixels", C.c_int32), ("delays", C.c_int32), ("total_static", C.c_int32),
+        ("total_dynamic", C.c_int32), ("qbins", C.c_int32), ("raw_frames", C.c_int32),
+        ("raw_events", C.c_int64), ("events", C.c_int64), ("valid_pixels", C.c_int32),
+        ("float_path_pixels", C.c_int32),
+    ]
+
+
+class StageTimes(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("h2d_ms", "filter_ms", "multitau_ms", "normalize_ms",
+                                         "d2h_ms", "multitau_int_ms", "multitau_float_ms",
+                                         "step_ms")] + [("launches", C.c_int32)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libxpcs_gpu.so (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            import sys
+            sys.path.insert(0, str(HERE))
+            from build import build_gpu
+            build_gpu()
+        L = C.CDLL(str(LIB))
+        L.xpcs_last_error.restype = C.c_char_p
+        L.xpcs_series_create.argtypes = [C.POINTER(SeriesDesc), C.POINTER(C.c_void_p)]
+        L.xpcs_series_destroy.argtypes = [C.c_void_p]
+        for name in ("xpcs_series_reset", "xpcs_synchronize"):
+            getattr(L, name).argtypes = [C.c_void_p]
+        L.xpcs_series_get_info.argtypes = [C.c_void_p, C.POINTER(SeriesInfo)]
+        L.xpcs_get_stage_times.argtypes = [C.c_void_p, C.POINTER(StageTimes)]
+        L.xpcs_ingest_sparse.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+        L.xpcs_ingest_sparse_device.argtypes = L.xpcs_ingest_sparse.argtypes
+        L.xpcs_multitau.argtypes = [C.c_void_p, C.c_int32]
+        L.xpcs_get_g2ipif.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.xpcs_normalize.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.xpcs_pin_host.argtypes = [C.c_void_p, C.c_uint64]
+        L.xpcs_unpin_host.argtypes = [C.c_void_p]
+        L.xpcs_multitau2.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                     C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def check(rc: int):
+    if rc != 0:
+        raise XpcsError(rc, lib().xpcs_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def delay_schedule(frames: int, dpl: int):
+    cap = 4096
+    lv = np.zeros(cap, np.int32)
+    tau = np.zeros(cap, np.int32)
+    n = C.c_int32(0)
+    check(lib().xpcs_delay_schedule(frames, dpl, _ptr(lv), _ptr(tau), cap, C.byref(n)))
+    return lv[:n.value].copy(), tau[:n.value].copy()
+
+
+class Series:
+    """One XPCS series on one GPU (an xpcs_series handle)."""
+
+    def __init__(self, width, height, frames, dpl, dqmap, sqmap, flatfield=None, stride=1,
+                 average=1, static_window=None, device=0):
+        self._dq = np.ascontiguousarray(dqmap, np.int32).ravel()
+        self._sq = np.ascontiguousarray(sqmap, np.int32).ravel()
+        self._flat = (None if flatfield is None
+                      else np.ascontiguousarray(flatfield, np.float64).ravel())
+        d = SeriesDesc()
+        d.width, d.height, d.frames, d.delays_per_level = width, height, frames, dpl
+        d.stride_frames, d.avg_frames = stride, average
+        d.static_window = static_window or max(frames // 10, 1)
+        d.dqmap = self._dq.ctypes.data_as(C.POINTER(C.c_int32))
+        d.sqmap = self._sq.ctypes.data_as(C.POINTER(C.c_int32))
+        d.flatfield = (self._flat.ctypes.data_as(C.POINTER(C.c_double))
+                       if self._flat is not None else None)
+        d.device = device
+        self._h = C.c_void_p()
+        check(lib().xpcs_series_create(C.byref(d), C.byref(self._h)))
+        self.width, self.height, self.frames = width, height, frames
+        self.info()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().xpcs_series_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> SeriesInfo:
+        i = SeriesInfo()
+        check(lib().xpcs_series_get_info(self._h, C.byref(i)))
+        self.P, self.D, self.nq = i.pixels, i.delays, i.qbins
+        return i
+
+    def reset(self):
+        check(lib().xpcs_series_reset(self._h))
+
+    def ingest_sparse(self, nnz, idx, val):
+        nnz = np.ascontiguousarray(nnz, np.uint32)
+        idx = np.ascontiguousarray(idx, np.int32)
+        val = np.ascontiguousarray(val, np.int16)
+        check(lib().xpcs_ingest_sparse(self._h, _ptr(idx), _ptr(val), _ptr(nnz), nnz.size))
+
+    def ingest_sparse_device(self, nnz, idx_dev_ptr: int, val_dev_ptr: int):
+        nnz = np.ascontiguousarray(nnz, np.uint32)
+        check(lib().xpcs_ingest_sparse_device(self._h, C.c_void_p(idx_dev_ptr),
+                                              C.c_void_p(val_dev_ptr), _ptr(nnz), nnz.size))
+
+    def multitau(self, mode=MODE_REFERENCE):
+        check(lib().xpcs_multitau(self._h, mode))
+
+    def synchronize(self):
+        check(lib().xpcs_synchronize(self._h))
+
+    def g2ipif(self, out=None):
+        if out is None:
+            out = tuple(np.empty((self.D, self.P), np.float32) for _ in range(3))
+        check(lib().xpcs_get_g2ipif(self._h, *[_ptr(a) for a in out]))
+        return out
+
+    def normalize(self, f64=True, f32=True, out=None):
+        if out is None:
+            shp = (self.D, self.nq)
+            out = (np.empty(shp, np.float64) if f64 else None,
+                   np.empty(shp, np.float64) if f64 else None,
+                   np.empty(shp, np.float32) if f32 else None,
+                   np.empty(shp, np.float32) if f32 else None)
+        check(lib().xpcs_normalize(self._h, *[_ptr(a) for a in out]))
+        return out
+
+    def stage_times(self) -> dict:
+        t = StageTimes()
+        check(lib().xpcs_get_stage_times(self._h, C.byref(t)))
+        return {n: getattr(t, n) for n, _ in StageTimes._fields_}
+
+
+def pin(a: np.ndarray) -> np.ndarray:
+    """Page-lock a numpy array in place (xpcs_pin_host); returns it."""
+    if a.nbytes:
+        check(lib().xpcs_pin_host(a.ctypes.data_as(C.c_void_p), a.nbytes))
+    return a
+
+
+def unpin(a: np.ndarray) -> None:
+    if a.nbytes:
+        check(lib().xpcs_unpin_host(a.ctypes.data_as(C.c_void_p)))
+
+
+def multitau2(row_ptr, frame, value, frames, dpl, mode=MODE_REFERENCE, device=0):
+    """Corr::multiTau2 on caller-held pixel-major rows (xpcs_multitau2)."""
+    row_ptr = np.ascontiguousarray(row_ptr, np.int64)
+    frame = np.ascontiguousarray(frame, np.int32)
+    value = np.ascontiguousarray(value, np.float32)
+    P = row_ptr.size - 1
+    lv, _ = delay_schedule(frames, dpl)
+    out = tuple(np.empty((lv.size, P), np.float32) for _ in range(3))
+    check(lib().xpcs_multitau2(_ptr(row_ptr), _ptr(frame), _ptr(value), P, frames, dpl, mode,
+                               device, *[_ptr(a) for a in out]))
+    return out
