@@ -72,7 +72,6 @@ struct DeviceGuard {
 void init_series(Series &s) {
   XG_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
   for (auto &e : s.ev) XG_CUDA(cudaEventCreate(&e));
-  s.cap = multitau_cap(s.D);
 }
 
 void free_series(Series *s) {
@@ -82,8 +81,9 @@ void free_series(Series *s) {
     cudaStream_t st = s->stream;
     cudaStreamSynchronize(st);
     DBuf<int32_t> *i32[] = {&s->raw_idx, &s->frA, &s->frB, &s->cnt, &s->row_len,
-                            &s->flist, &s->ev_frame, &s->sc_frame, &s->n_q_entry_ptr,
-                            &s->n_entry_sbin, &s->n_entry_pix_ptr, &s->n_pix, &s->n_q_row};
+                            &s->flist, &s->wlist, &s->ev_frame, &s->sc_frame, &s->n_q_entry_ptr,
+                            &s->n_entry_sbin, &s->n_entry_pix_ptr, &s->n_pix, &s->n_q_row,
+                            &s->n_ch_k0, &s->n_ch_k1, &s->n_e_chunk_ptr};
     for (auto *b : i32) b->release(st);
     DBuf<float> *f32[] = {&s->vA, &s->vB, &s->ev_val, &s->pixels_sum, &s->sc_val, &s->G2,
                           &s->IP, &s->IF, &s->n_ratio32, &s->n_g2f, &s->n_sef};
@@ -96,7 +96,7 @@ void free_series(Series *s) {
     s->scan_tmp.release(st);
     s->plan.release(st);
     s->d_flat.release(st);
-    s->n_ratio64.release(st);
+    s->n_part.release(st);
     s->n_g2.release(st);
     s->n_se.release(st);
     s->keyA.release(st);
@@ -180,6 +180,7 @@ int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out) {
     std::vector<int32_t> rows(q.q_ids.size());
     for (size_t k = 0; k < rows.size(); k++) rows[k] = q.q_ids[k] - 1;
     upload(s->n_q_row, rows, st);
+    build_norm_chunks(*s);
     XG_CUDA(cudaStreamSynchronize(st));
     *out = (xpcs_series *)s;
   });

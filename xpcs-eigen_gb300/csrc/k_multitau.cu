@@ -2,31 +2,39 @@
 //
 // Replaces Corr::multiTau2 (src/xpcs/corr.cpp:315-431).  For every pixel with
 // events and every delay (level L, tau):
-//   on a level change, lastframe halves (odd -> -1 first) and the row is
+//   on a level change lastframe halves (odd -> -1 first) and the row is
 //   compacted in place: index/2, equal neighbours merged by addition, indices
 //   >= lastframe dropped, every live value halved (:349-390);
 //   IP  = sum of v over events with t < lastframe - tau,
-//   G2  = sum of v(t) * v(t + tau) with the partner found by std::lower_bound
-//         over the row buffer (:406),
+//   G2  = sum of v(t) * v(t + tau), the partner found by std::lower_bound over
+//         the row buffer (:406),
 //   IF  = sum of v over events with tau <= t < lastframe,
 //   each divided by (lastframe - tau) (:420-424).
 //
-// Integer path (pixels whose values are integers with sum |v| < 4096): one
-// warp per pixel keeps the row in shared memory as integer numerators
-// (value at level L = N / 2^L).  Every float partial sum of the reference is
-// then exact, so integer sums scaled by 2^-L (2^-2L for G2) and one IEEE
-// division reproduce the reference bit for bit.  IP and IF come from a prefix
-// sum and two binary searches per delay; G2 from an event-parallel scan of
-// the pairs within the level's delay window.  In REFERENCE mode a pair counts
-// only if lower_bound over the whole row buffer (live prefix + the stale tail
-// the in-place compaction leaves behind) lands on the partner, exactly as in
-// the reference; when the buffer is globally sorted that always holds.
-// Results are staged per 32-pixel tile in shared memory and written as
-// coalesced 128-byte rows of the [D][P] outputs.
-//
-// Float path (all other pixels): one thread per pixel replays the reference's
-// float operations in the reference's order (no fused multiply-add), on a
-// scratch copy of its row.
+// Integer paths (values are integers, sum |v| < 4096): a level-L value is an
+// integer numerator N over 2^L, every float partial sum of the reference is
+// exact, so integer sums scaled by 2^-L (2^-2L for G2) followed by one IEEE
+// division reproduce the reference bit for bit.
+//   * IP and IF do not depend on the compaction: level L keeps exactly the
+//     events with frame < lastframe << L, so IP(tau) = S(t_ip) and
+//     IF(tau) = S(lastframe << L) - S(tau_frames), S(T) = sum of v over
+//     original events with frame < T.  Two merge sweeps over the sorted row
+//     and the (monotone) per-delay thresholds give all of them.
+//   * G2 needs the compacted rows: per level the row is compacted in place
+//     (the same buffer the reference keeps, stale tail included) and the
+//     pairs whose bin distance lies in the level's delay window are scanned
+//     with a second pointer.  In REFERENCE mode a pair counts only when
+//     lower_bound over the whole buffer lands on the partner; that always
+//     holds while the buffer is globally sorted, which is tracked per level
+//     from the junction between the new prefix and the stale tail.
+// k_mt_thread: one thread per pixel, rows packed (frame << 16 | int16 value)
+//   in shared memory with a lane-interleaved layout (conflict-free), outputs
+//   written straight to [D][P] (32 consecutive pixels per warp = coalesced).
+//   Pixels of other classes get zeros here and are rewritten by the kernels
+//   below.
+// k_mt_warp:   one warp per pixel for rows of up to 256 events.
+// k_mt_float:  one thread per pixel replaying the reference's float
+//   operations in its order (no fused multiply-add) on a scratch copy.
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -36,20 +44,8 @@
 namespace xg {
 namespace {
 
-constexpr int MC_WARPS = 8;
-constexpr int MC_THREADS = MC_WARPS * 32;
-constexpr int MC_TILE = 32;
-constexpr int MC_ACC = 64;  // max delays per level on the integer path (2*dpl <= 64)
-constexpr int MC_CAP = 256; // max events per pixel on the integer path
-
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
-__host__ __device__ inline size_t plan_bytes(int D) {
-  return align16(sizeof(McPlan) + (size_t)D * sizeof(int32_t) + (size_t)D * sizeof(float));
-}
-__host__ __device__ inline size_t warp_bytes(int cap) { return (size_t)(3 * cap + MC_ACC) * sizeof(int32_t); }
-inline size_t int_smem_bytes(int D, int cap) {
-  return plan_bytes(D) + MC_WARPS * warp_bytes(cap) + (size_t)3 * D * MC_TILE * sizeof(float);
-}
+constexpr int MT_WARPS = 2;  // warps per block of the thread-per-pixel kernel
+constexpr int WP_WARPS = 8;  // warps per block of the warp-per-pixel kernel
 
 // std::lower_bound as libstdc++ implements it (halving the remaining length).
 __device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t x) {
@@ -66,7 +62,188 @@ __device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t 
   return first;
 }
 
+// The same search over lane-interleaved packed words (frame in the high half).
+__device__ __forceinline__ int lower_bound_packed(const uint32_t *row, int n, int32_t x) {
+  int first = 0, len = n;
+  while (len > 0) {
+    int half = len >> 1;
+    if ((int32_t)(row[(first + half) * 32] >> 16) < x) {
+      first += half + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  return first;
+}
+
 __device__ __forceinline__ float pow2_neg(int e) { return __int_as_float((127 - e) << 23); }
+
+// (float)num * 2^-shift / den as the reference's float arithmetic produces it.
+__device__ __forceinline__ float scaled_quotient(int num, int shift, float den) {
+  if (num == 0) return 0.f;
+  float x = __fmul_rn((float)num, pow2_neg(shift));
+  return den > 0.f ? __fdiv_rn(x, den) : x;
+}
+
+__device__ __forceinline__ int32_t pk_t(uint32_t w) { return (int32_t)(w >> 16); }
+__device__ __forceinline__ int32_t pk_v(uint32_t w) { return (int32_t)(int16_t)(w & 0xffffu); }
+__device__ __forceinline__ uint32_t pk(int32_t t, int32_t v) {
+  return ((uint32_t)t << 16) | ((uint32_t)v & 0xffffu);
+}
+
+__device__ __forceinline__ void copy_plan(uint8_t *dst, const uint8_t *src, size_t bytes) {
+  for (int k = threadIdx.x; k < (int)(bytes / 4); k += blockDim.x)
+    ((int32_t *)dst)[k] = ((const int32_t *)src)[k];
+}
+
+// ------------------------------------------------------ thread per pixel
+
+__global__ void __launch_bounds__(MT_WARPS * 32)
+k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
+            const int32_t *__restrict__ row_len, const uint8_t *__restrict__ pclass,
+            const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
+            float *__restrict__ G2, float *__restrict__ IP, float *__restrict__ IF) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int D = ((const McPlan *)plan_g)->D;
+  const size_t pb = mc_plan_bytes(D);
+  copy_plan(smem, plan_g, pb);
+  __syncthreads();
+  const McPlan *pl = (const McPlan *)smem;
+  const McArrays ar = mc_arrays(smem, D);
+  const int P = pl->P, nlev = pl->nlev, mode = pl->mode;
+  const int scr = max(pl->acc, nlev);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *wbase = (uint32_t *)(smem + pb) + (size_t)warp * (MT_THREAD_CAP + scr) * 32;
+  uint32_t *row = wbase + lane;
+  int32_t *acc = (int32_t *)(row + MT_THREAD_CAP * 32);  // scratch, also S(t_end) per level
+
+  const int p0 = (blockIdx.x * MT_WARPS + warp) * 32;
+  if (p0 >= P) return;
+  const int p = p0 + lane;
+  const bool mine = p < P && pclass[p] == PCLASS_THREAD;
+  const int n0 = mine ? row_len[p] : 0;
+
+  // cooperative, coalesced load of the warp's rows (consecutive pixels have
+  // consecutive rows), scattered to the owning lane's slots
+  {
+    const int plast = min(p0 + 32, P);
+    const int64_t e0 = row_ptr[p0], e1 = row_ptr[plast];
+    const int64_t my_b = p < P ? row_ptr[p] : e1;
+    for (int64_t base = e0; base < e1; base += 32) {
+      const int64_t e = base + lane;
+      int owner = 0;  // last lane whose row starts at or before e
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const int cand = owner + o;
+        const int64_t cb = __shfl_sync(0xffffffffu, my_b, cand & 31);
+        if (cand < 32 && cb <= e) owner = cand;
+      }
+      const int64_t ob = __shfl_sync(0xffffffffu, my_b, owner);
+      const int olen = __shfl_sync(0xffffffffu, n0, owner);
+      if (e < e1) {
+        const int slot = (int)(e - ob);
+        if (slot < olen) wbase[slot * 32 + owner] = pk(ev_frame[e], __float2int_rn(ev_val[e]));
+      }
+    }
+  }
+  __syncwarp();
+
+  // total and S(t_end) per level (sweep from the end; t_end non-increasing)
+  int total = 0;
+  for (int i = 0; i < n0; i++) total += pk_v(row[i * 32]);
+  {
+    int j = n0 - 1, rsum = 0;
+    for (int g = 0; g < nlev; g++) {
+      const int te = pl->lv[g].t_end;
+      while (j >= 0 && pk_t(row[j * 32]) >= te) {
+        rsum += pk_v(row[j * 32]);
+        j--;
+      }
+      acc[g * 32] = total - rsum;
+    }
+  }
+  // IP: thresholds t_ip strictly decreasing with the delay index
+  {
+    int j = n0 - 1, rsum = 0;
+    for (int d = 0; d < D; d++) {
+      const int T = ar.t_ip[d];
+      while (j >= 0 && pk_t(row[j * 32]) >= T) {
+        rsum += pk_v(row[j * 32]);
+        j--;
+      }
+      const int lvl = pl->lv[ar.gi[d]].level;
+      if (p < P) IP[(size_t)d * P + p] = mine ? scaled_quotient(total - rsum, lvl, ar.denom[d]) : 0.f;
+    }
+  }
+  // IF: thresholds tau (in frames) increasing with the delay index
+  {
+    int j = 0, ssum = 0;
+    for (int d = 0; d < D; d++) {
+      const int T = ar.tau_abs[d];
+      while (j < n0 && pk_t(row[j * 32]) < T) {
+        ssum += pk_v(row[j * 32]);
+        j++;
+      }
+      const int g = ar.gi[d];
+      const int lvl = pl->lv[g].level;
+      if (p < P)
+        IF[(size_t)d * P + p] = mine ? scaled_quotient(acc[g * 32] - ssum, lvl, ar.denom[d]) : 0.f;
+    }
+  }
+
+  // G2: level by level on the compacted buffer
+  int m = n0;
+  bool J = true, U = true;  // junction at m sorted; stale suffix [m, n0) sorted
+  for (int g = 0; g < nlev; g++) {
+    const McLevel L = pl->lv[g];
+    if (L.compact && m > 0) {
+      const int lf = L.lastframe;
+      int index = -1, prev = INT_MIN;
+      for (int i = 0; i < m; i++) {
+        const uint32_t w = row[i * 32];
+        const int t = pk_t(w) >> 1;
+        if (t >= lf) break;
+        if (t == prev) {
+          const uint32_t h = row[index * 32];
+          row[index * 32] = pk(t, pk_v(h) + pk_v(w));
+        } else {
+          row[++index * 32] = pk(t, pk_v(w));
+          prev = t;
+        }
+      }
+      const int m2 = index + 1;
+      U = (m2 < m) ? (J && U) : U;
+      J = (m2 == 0 || m2 >= n0) ? true : (pk_t(row[(m2 - 1) * 32]) <= pk_t(row[m2 * 32]));
+      m = m2;
+    }
+    const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
+    for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
+    const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
+    int jlo = 1;
+    for (int i = 0; i < m; i++) {
+      const uint32_t wi = row[i * 32];
+      const int ti = pk_t(wi), vi = pk_v(wi);
+      if (jlo <= i) jlo = i + 1;
+      while (jlo < m && pk_t(row[jlo * 32]) - ti < tlo) jlo++;
+      for (int j = jlo; j < m; j++) {
+        const uint32_t wj = row[j * 32];
+        const int d = pk_t(wj) - ti;
+        if (d > thi) break;
+        if (!sorted && lower_bound_packed(row, n0, pk_t(wj)) != j) continue;
+        acc[(d - tlo) * 32] += vi * pk_v(wj);
+      }
+    }
+    if (p < P) {
+      for (int k = 0; k < L.count; k++) {
+        const int d = L.first + k;
+        G2[(size_t)d * P + p] = mine ? scaled_quotient(acc[k * 32], 2 * L.level, ar.denom[d]) : 0.f;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- warp per pixel
 
 // In-place compaction of the live prefix t[0..m), v[0..m) (warp-cooperative).
 // Returns the new live length; entries at and beyond it are left untouched.
@@ -99,38 +276,29 @@ __device__ int compact_warp(int32_t *t, int32_t *v, int m, int lastframe, int la
   return gbase;
 }
 
-__global__ void __launch_bounds__(MC_THREADS)
-k_multitau_int(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
-               const int32_t *__restrict__ row_len, const uint8_t *__restrict__ pclass,
-               const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
-               float *__restrict__ G2, float *__restrict__ IP, float *__restrict__ IF) {
+__global__ void __launch_bounds__(WP_WARPS * 32)
+k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ wlist,
+          const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
+          const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
+          const float *__restrict__ ev_val, float *__restrict__ G2, float *__restrict__ IP,
+          float *__restrict__ IF) {
   extern __shared__ __align__(16) uint8_t smem[];
-  const McPlan *gp = (const McPlan *)plan_g;
-  const int D = gp->D, P = gp->P, cap = gp->cap, mode = gp->mode;
-  const size_t pb = plan_bytes(D);
-  {
-    const int32_t *src = (const int32_t *)plan_g;
-    int32_t *dst = (int32_t *)smem;
-    for (int k = threadIdx.x; k < (int)(pb / 4); k += MC_THREADS) dst[k] = src[k];
-  }
-  const McPlan *pl = (const McPlan *)smem;
-  const int32_t *tau_lvl = (const int32_t *)(smem + sizeof(McPlan));
-  const float *denom = (const float *)(tau_lvl + D);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int32_t *t = (int32_t *)(smem + pb + warp * warp_bytes(cap));
-  int32_t *v = t + cap;
-  int32_t *S = v + cap;
-  int32_t *acc = S + cap;
-  float *stg = (float *)(smem + pb + MC_WARPS * warp_bytes(cap));
-  const int nst = 3 * D * MC_TILE;
-  for (int k = threadIdx.x; k < nst; k += MC_THREADS) stg[k] = 0.f;
+  const int D = ((const McPlan *)plan_g)->D;
+  const size_t pb = mc_plan_bytes(D);
+  copy_plan(smem, plan_g, pb);
   __syncthreads();
-
-  const int tile0 = blockIdx.x * MC_TILE;
+  const McPlan *pl = (const McPlan *)smem;
+  const McArrays ar = mc_arrays(smem, D);
+  const int P = pl->P, mode = pl->mode, ACC = pl->acc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t *t = (int32_t *)(smem + pb) + (size_t)warp * (3 * MT_WARP_CAP + ACC);
+  int32_t *v = t + MT_WARP_CAP;
+  int32_t *S = v + MT_WARP_CAP;
+  int32_t *acc = S + MT_WARP_CAP;
   const unsigned FULL = 0xffffffffu;
-  for (int lp = warp; lp < MC_TILE; lp += MC_WARPS) {
-    const int p = tile0 + lp;
-    if (p >= P || pclass[p] != PCLASS_INT) continue;
+  const int nw = stats->nwarp;
+  for (int q = blockIdx.x * WP_WARPS + warp; q < nw; q += gridDim.x * WP_WARPS) {
+    const int p = wlist[q];
     const int64_t b = row_ptr[p];
     const int n0 = row_len[p];
     for (int i = lane; i < n0; i += 32) {
@@ -142,15 +310,13 @@ k_multitau_int(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ r
     for (int gi = 0; gi < pl->nlev; gi++) {
       const McLevel L = pl->lv[gi];
       const int lastframe = L.lastframe;
-      if (L.compact) m = compact_warp(t, v, m, lastframe, lane);
-      if (m == 0) break;  // nothing live: every remaining output stays 0
+      if (L.compact && m > 0) m = compact_warp(t, v, m, lastframe, lane);
       bool sorted = true;
-      if (mode == XPCS_MODE_REFERENCE) {
+      if (mode == XPCS_MODE_REFERENCE && m > 0) {
         bool ok = true;
         for (int i = lane; i + 1 < n0; i += 32) ok &= t[i] <= t[i + 1];
         sorted = __all_sync(FULL, ok);
       }
-      // inclusive prefix sums of the live values
       int carry = 0;
       for (int c0 = 0; c0 < m; c0 += 32) {
         int i = c0 + lane;
@@ -179,58 +345,36 @@ k_multitau_int(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ r
         }
       }
       __syncwarp();
-      const float s1 = pow2_neg(L.level), s2 = pow2_neg(2 * L.level);
-      const int total = S[m - 1];
+      const int total = m > 0 ? S[m - 1] : 0;
       for (int k = lane; k < L.count; k += 32) {
         const int tau = tlo + k;
-        const int cip = lower_bound_i32(t, m, lastframe - tau);
-        const int cif = lower_bound_i32(t, m, tau);
+        const int cip = m > 0 ? lower_bound_i32(t, m, lastframe - tau) : 0;
+        const int cif = m > 0 ? lower_bound_i32(t, m, tau) : 0;
         const int ip = cip ? S[cip - 1] : 0;
         const int iff = total - (cif ? S[cif - 1] : 0);
-        float fg = __fmul_rn((float)acc[k], s2);
-        float fi = __fmul_rn((float)ip, s1);
-        float ff = __fmul_rn((float)iff, s1);
-        const float den = denom[L.first + k];
-        if (den > 0.f) {
-          fg = __fdiv_rn(fg, den);
-          fi = __fdiv_rn(fi, den);
-          ff = __fdiv_rn(ff, den);
-        }
-        const int o = (L.first + k) * MC_TILE + lp;
-        stg[o] = fg;
-        stg[D * MC_TILE + o] = fi;
-        stg[2 * D * MC_TILE + o] = ff;
+        const int d = L.first + k;
+        const float den = ar.denom[d];
+        G2[(size_t)d * P + p] = scaled_quotient(acc[k], 2 * L.level, den);
+        IP[(size_t)d * P + p] = scaled_quotient(ip, L.level, den);
+        IF[(size_t)d * P + p] = scaled_quotient(iff, L.level, den);
       }
       __syncwarp();
-    }
-    __syncwarp();
-  }
-  __syncthreads();
-  // coalesced write-out of the tile: rows of 32 consecutive pixels
-  for (int k = threadIdx.x; k < nst; k += MC_THREADS) {
-    const int a = k / (D * MC_TILE);
-    const int rem = k - a * D * MC_TILE;
-    const int d = rem / MC_TILE, lp = rem - d * MC_TILE;
-    const int p = tile0 + lp;
-    if (p < P) {
-      float *dst = a == 0 ? G2 : (a == 1 ? IP : IF);
-      dst[(size_t)d * P + p] = stg[k];
     }
   }
 }
 
-// Order-preserving float replay of Corr::multiTau2 for one pixel per thread.
+// --------------------------------------------------------- float replay
+
 __global__ void __launch_bounds__(128)
-k_multitau_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
-                 const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
-                 const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
-                 const float *__restrict__ ev_val, int32_t *__restrict__ sc_frame,
-                 float *__restrict__ sc_val, float *__restrict__ G2, float *__restrict__ IP,
-                 float *__restrict__ IF) {
+k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
+           const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
+           const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
+           const float *__restrict__ ev_val, int32_t *__restrict__ sc_frame,
+           float *__restrict__ sc_val, float *__restrict__ G2, float *__restrict__ IP,
+           float *__restrict__ IF) {
   const McPlan *pl = (const McPlan *)plan_g;
   const int D = pl->D, P = pl->P, mode = pl->mode;
-  const int32_t *tau_lvl = (const int32_t *)(plan_g + sizeof(McPlan));
-  const float *denom = (const float *)(tau_lvl + D);
+  const McArrays ar = mc_arrays(plan_g, D);
   const int nf = stats->nfloat;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nf; q += gridDim.x * blockDim.x) {
     const int p = flist[q];
@@ -271,7 +415,7 @@ k_multitau_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__
       const int sn = mode == XPCS_MODE_REFERENCE ? n0 : lastIndex;
       for (int k = 0; k < L.count; k++) {
         const int d = L.first + k;
-        const int tau = tau_lvl[d];
+        const int tau = ar.tau_lvl[d];
         float g2 = 0.f, ip = 0.f, iff = 0.f;
         for (int r = 0; r < lastIndex; r++) {
           const int src = idx[r];
@@ -283,7 +427,7 @@ k_multitau_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__
           }
           if (src >= tau && src < lastframe) iff = __fadd_rn(iff, val[r]);
         }
-        const float den = denom[d];
+        const float den = ar.denom[d];
         if (den > 0.f) {
           g2 = __fdiv_rn(g2, den);
           ip = __fdiv_rn(ip, den);
@@ -297,24 +441,21 @@ k_multitau_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__
   }
 }
 
-}  // namespace
-
-int multitau_cap(int) { return MC_CAP; }
-
 // Host-side plan: level groups of the delay schedule with the lastframe each
 // sees and whether the reference compacts before it (corr.cpp:341-391).
-static std::vector<uint8_t> make_plan(const Series &s, int mode) {
+std::vector<uint8_t> make_plan(const Series &s, int mode) {
   const int D = s.D;
-  std::vector<uint8_t> buf(plan_bytes(D), 0);
+  std::vector<uint8_t> buf(mc_plan_bytes(D), 0);
   McPlan *pl = (McPlan *)buf.data();
-  int32_t *tau_lvl = (int32_t *)(buf.data() + sizeof(McPlan));
-  float *denom = (float *)(tau_lvl + D);
+  int32_t *base = (int32_t *)(buf.data() + sizeof(McPlan));
+  int32_t *tau_lvl = base;
+  float *denom = (float *)(base + D);
+  int32_t *tau_abs = base + 2 * D, *t_ip = base + 3 * D, *gi = base + 4 * D;
   pl->P = s.P;
   pl->D = D;
   pl->F = s.F;
   pl->mode = mode;
-  pl->cap = s.cap;
-  int ll = 0, lastframe = s.F, nlev = 0;
+  int ll = 0, lastframe = s.F, nlev = 0, acc = 1;
   for (int k = 0; k < D; k++) {
     int level = s.delays.level[k];
     bool newgroup = (k == 0) || level != s.delays.level[k - 1];
@@ -327,7 +468,9 @@ static std::vector<uint8_t> make_plan(const Series &s, int mode) {
     // tau / pow(2, level) truncated to int (corr.cpp:393-394)
     int tau = level > 0 ? (int)(s.delays.tau[k] / std::pow(2.0, level)) : s.delays.tau[k];
     tau_lvl[k] = tau;
+    tau_abs[k] = s.delays.tau[k];
     denom[k] = (lastframe - tau) > 0 ? (float)(lastframe - tau) : 0.f;
+    t_ip[k] = (int32_t)std::max<int64_t>(0, (int64_t)(lastframe - tau) << level);
     if (newgroup) {
       if (nlev >= MAX_LEVELS) throw Error(XPCS_ERR_INVALID_ARGUMENT, "too many multi-tau levels");
       McLevel &L = pl->lv[nlev++];
@@ -337,24 +480,41 @@ static std::vector<uint8_t> make_plan(const Series &s, int mode) {
       L.lastframe = lastframe;
       L.tau_lo = tau;
       L.compact = compact;
+      L.t_end = (int32_t)((int64_t)lastframe << level);
     }
     McLevel &L = pl->lv[nlev - 1];
     if (tau != L.tau_lo + L.count)
       throw Error(XPCS_ERR_INVALID_ARGUMENT, "non-consecutive delays within a level");
     L.count++;
+    acc = std::max(acc, L.count);
+    gi[k] = nlev - 1;
     ll = level;
   }
   pl->nlev = nlev;
+  pl->acc = acc;
+  for (int k = 1; k < D; k++)
+    if (t_ip[k] >= t_ip[k - 1] || tau_abs[k] <= tau_abs[k - 1])
+      throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay thresholds are not monotone");
+  for (int g = 1; g < nlev; g++)
+    if (pl->lv[g].t_end > pl->lv[g - 1].t_end)
+      throw Error(XPCS_ERR_INVALID_ARGUMENT, "level end thresholds are not monotone");
   return buf;
 }
+
+size_t thread_smem(int D, int scr) {
+  return mc_plan_bytes(D) + (size_t)MT_WARPS * (MT_THREAD_CAP + scr) * 32 * sizeof(uint32_t);
+}
+size_t warp_smem(int D, int acc) {
+  return mc_plan_bytes(D) + (size_t)WP_WARPS * (3 * MT_WARP_CAP + acc) * sizeof(int32_t);
+}
+
+}  // namespace
 
 void run_multitau(Series &s, int mode) {
   cudaStream_t st = s.stream;
   const int D = s.D, P = s.P;
   std::vector<uint8_t> plan = make_plan(s, mode);
-  int maxcount = 0;
-  for (int g = 0; g < ((McPlan *)plan.data())->nlev; g++)
-    maxcount = std::max(maxcount, ((McPlan *)plan.data())->lv[g].count);
+  const McPlan *hp = (const McPlan *)plan.data();
   s.plan.reserve(plan.size(), st);
   XG_CUDA(cudaMemcpyAsync(s.plan.p, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
   const size_t nD = (size_t)D * P;
@@ -362,26 +522,32 @@ void run_multitau(Series &s, int mode) {
   s.IP.reserve(nD ? nD : 1, st);
   s.IF.reserve(nD ? nD : 1, st);
   if (D == 0 || P == 0) return;
-  size_t smem = int_smem_bytes(D, s.cap);
-  if (smem > 227 * 1024 || maxcount > MC_ACC)
-    throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay schedule too large for the multi-tau kernel");
-  XG_CUDA(cudaFuncSetAttribute(k_multitau_int, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem));
+  const int scr = std::max(hp->acc, hp->nlev);
+  const size_t smt = thread_smem(D, scr), smw = warp_smem(D, hp->acc);
+  if (smt > 227 * 1024 || smw > 227 * 1024)
+    throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay schedule too large for the multi-tau kernels");
+  XG_CUDA(cudaFuncSetAttribute(k_mt_thread, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
+  XG_CUDA(cudaFuncSetAttribute(k_mt_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw));
+  int sms = 0;
+  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
   XG_CUDA(cudaEventRecord(s.ev[4], st));
-  k_multitau_int<<<(P + MC_TILE - 1) / MC_TILE, MC_THREADS, smem, st>>>(
+  const int per_block = MT_WARPS * 32;
+  k_mt_thread<<<(P + per_block - 1) / per_block, per_block, smt, st>>>(
       s.plan.p, s.row_ptr.p, s.row_len.p, s.pclass.p, s.ev_frame.p, s.ev_val.p, s.G2.p, s.IP.p,
       s.IF.p);
+  XG_CHECK_LAUNCH();
+  k_mt_warp<<<sms * 2, WP_WARPS * 32, smw, st>>>(s.plan.p, s.wlist.p, s.stats.p, s.row_ptr.p,
+                                                 s.row_len.p, s.ev_frame.p, s.ev_val.p, s.G2.p,
+                                                 s.IP.p, s.IF.p);
   XG_CHECK_LAUNCH();
   XG_CUDA(cudaEventRecord(s.ev[5], st));
   size_t ne = s.raw_events > 0 ? (size_t)s.raw_events : 1;
   s.sc_frame.reserve(ne, st);
   s.sc_val.reserve(ne, st);
-  int dev_sms = 0;
-  XG_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s.device));
-  int grid = std::max(1, std::min((P + 127) / 128, dev_sms * 8));
-  k_multitau_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p,
-                                         s.row_len.p, s.ev_frame.p, s.ev_val.p, s.sc_frame.p,
-                                         s.sc_val.p, s.G2.p, s.IP.p, s.IF.p);
+  int grid = std::max(1, std::min((P + 127) / 128, sms * 8));
+  k_mt_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p,
+                                   s.ev_frame.p, s.ev_val.p, s.sc_frame.p, s.sc_val.p, s.G2.p,
+                                   s.IP.p, s.IF.p);
   XG_CHECK_LAUNCH();
   XG_CUDA(cudaEventRecord(s.ev[6], st));
 }

@@ -1,26 +1,88 @@
 // K-d: per-partition normalisation of G2/IP/IF into g2 and its standard error.
 //
-// Replaces Corr::normalizeG2s (src/xpcs/corr.cpp:927-1091).  The q -> sbin ->
-// pixel mapping of BuildQMap is flattened into entries (one per (q, sbin),
-// q ascending, sbin ascending, pixels in raster order).
+// Replaces Corr::normalizeG2s (src/xpcs/corr.cpp:927-1091).  BuildQMap's
+// q -> sbin -> pixel mapping is flattened into entries (one per (q, sbin): q
+// ascending, sbin ascending, pixels in raster order) and every entry's pixel
+// range is cut into chunks of at most NCH pixels.
 //
-// float64 evaluation (the reported result):
-//   k_entry_f64: one block per (entry, tau) reduces sum G2, sum IP, sum IF over
-//                the entry's pixels; ratio = (G2/n) / ((IP/n) (IF/n)) (:966-1013).
-//   k_q_f64:     one block per (q, tau): g2 = mean of the non-NaN entry ratios
-//                (:1018-1040); stderr over the q's pixels of x = G2/(IP IF) with
-//                NaN -> 0 still counted (quirk Q8), two passes (mean, then sum
-//                of squared deviations), sqrt(1/n) sqrt(M2/n) (:1043-1087).
-// float32 evaluation (bit-identical to the reference's float output):
-//   k_entry_f32 / k_q_f32: one thread per (entry or q, tau) replays the
-//   reference's sequential float operations in its order, including the
-//   running-mean / M2 update of every pixel.
+// float64 result (the reported one):
+//   k_norm_chunk   one block per (chunk, tau) reads G2/IP/IF of the chunk's
+//                  pixels once and produces, for the chunk: sum G2, sum IP,
+//                  sum IF, sum x and sum (x - mean_chunk)^2 with
+//                  x = G2 / (IP IF), NaN -> 0 and still counted (quirk Q8).
+//                  Per-element arithmetic is double-word ("float-float") on
+//                  the FP32 pipes -- TwoSum, FMA-based TwoProd and the
+//                  double-word add/multiply of Joldes, Muller & Popescu
+//                  (ACM TOMS 2017), ~2^-46 relative -- because GB300's FP64
+//                  rate is a small fraction of its FP32 rate; block totals and
+//                  everything after are FP64.
+//   k_norm_finish  one thread per (q, tau): entry ratio (G2/n)/((IP/n)(IF/n))
+//                  (:966-1013), g2 = mean of the non-NaN ratios (:1018-1040),
+//                  and the chunks' (n, mean, M2) merged in order with Chan's
+//                  pairwise update; stderr = sqrt(1/n) sqrt(M2/n) (:1043-1087).
+// float32 result (optional, bit-identical to the reference's float output):
+//   k_entry_f32 / k_q_f32 replay the reference's sequential float operations
+//   in its order, including the running-mean/M2 update of every pixel.
 #include "xpcs_internal.h"
 
 namespace xg {
 namespace {
 
-constexpr int NB = 256;
+constexpr int NB = 256;          // threads per chunk block
+constexpr int NIPT = 8;          // pixels per thread
+constexpr int NCH = NB * NIPT;   // pixels per chunk
+
+// ------------------------------------------------ double-word arithmetic
+
+struct dw {
+  float h, l;
+};
+
+__device__ __forceinline__ dw two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ dw fast_two_sum(float a, float b) {  // |a| >= |b|
+  float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dw two_prod(float a, float b) {
+  float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+// double-word + float (DWPlusFP)
+__device__ __forceinline__ dw dw_add_f(dw x, float y) {
+  dw s = two_sum(x.h, y);
+  return fast_two_sum(s.h, __fadd_rn(x.l, s.l));
+}
+// double-word + double-word (AccurateDWPlusDW)
+__device__ __forceinline__ dw dw_add(dw x, dw y) {
+  dw s = two_sum(x.h, y.h), t = two_sum(x.l, y.l);
+  dw v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+  return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
+}
+// double-word * double-word (DWTimesDW)
+__device__ __forceinline__ dw dw_mul(dw x, dw y) {
+  dw c = two_prod(x.h, y.h);
+  float t = __fmaf_rn(x.l, y.h, __fmaf_rn(x.h, y.l, __fmul_rn(x.l, y.l)));
+  return fast_two_sum(c.h, __fadd_rn(c.l, t));
+}
+// float / double-word: one correctly rounded quotient plus the quotient of
+// the (FMA-exact) remainder
+__device__ __forceinline__ dw f_div_dw(float a, dw b) {
+  float q = __fdiv_rn(a, b.h);
+  if (!isfinite(q) || q == 0.f) return {q, 0.f};
+  float r = __fmaf_rn(-q, b.h, a);
+  r = __fmaf_rn(-q, b.l, r);
+  return fast_two_sum(q, __fdiv_rn(r, b.h));
+}
+__device__ __forceinline__ dw dw_from_double(double x) {
+  float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double to_double(dw x) { return (double)x.h + (double)x.l; }
 
 __device__ __forceinline__ double block_sum(double x, double *sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -33,80 +95,106 @@ __device__ __forceinline__ double block_sum(double x, double *sh) {
     r = threadIdx.x < NB / 32 ? sh[threadIdx.x] : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-    if (threadIdx.x == 0) sh[0] = r;
+    if (threadIdx.x == 0) sh[NB / 32] = r;
   }
   __syncthreads();
-  r = sh[0];
+  r = sh[NB / 32];
   __syncthreads();
   return r;
 }
 
+// part layout: [chunk][tau][5] = sum G2, sum IP, sum IF, sum x, M2 about the chunk mean
 __global__ void __launch_bounds__(NB)
-k_entry_f64(int D, int P, const int32_t *__restrict__ epp, const int32_t *__restrict__ pix,
-            const float *__restrict__ G2, const float *__restrict__ IP,
-            const float *__restrict__ IF, double *__restrict__ ratio) {
-  __shared__ double sh[NB / 32];
-  const int e = blockIdx.x / D, t = blockIdx.x - e * D;
-  const int k0 = epp[e], k1 = epp[e + 1];
+k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__restrict__ ch_k1,
+             const int32_t *__restrict__ pix, const float *__restrict__ G2,
+             const float *__restrict__ IP, const float *__restrict__ IF, double *__restrict__ part) {
+  __shared__ double sh[NB / 32 + 1];
+  __shared__ float xh[NCH], xl[NCH];
+  const int c = blockIdx.x, t = blockIdx.y;
+  const int k0 = ch_k0[c], k1 = ch_k1[c];
   const size_t o = (size_t)t * P;
-  double sg = 0, si = 0, sf = 0;
-  for (int k = k0 + threadIdx.x; k < k1; k += NB) {
-    int p = pix[k];
-    sg += (double)G2[o + p];
-    si += (double)IP[o + p];
-    sf += (double)IF[o + p];
+  dw sg{0.f, 0.f}, si{0.f, 0.f}, sf{0.f, 0.f}, sx{0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < NIPT; j++) {
+    const int k = k0 + j * NB + threadIdx.x;
+    if (k < k1) {
+      const int p = pix[k];
+      const float g = G2[o + p], a = IP[o + p], b = IF[o + p];
+      sg = dw_add_f(sg, g);
+      si = dw_add_f(si, a);
+      sf = dw_add_f(sf, b);
+      dw x = f_div_dw(g, two_prod(a, b));
+      if (isnan(x.h) || isnan(x.l)) x = {0.f, 0.f};
+      sx = dw_add(sx, x);
+      xh[j * NB + threadIdx.x] = x.h;
+      xl[j * NB + threadIdx.x] = x.l;
+    }
   }
-  sg = block_sum(sg, sh);
-  si = block_sum(si, sh);
-  sf = block_sum(sf, sh);
+  const double n = (double)(k1 - k0);
+  const double Sg = block_sum(to_double(sg), sh);
+  const double Si = block_sum(to_double(si), sh);
+  const double Sf = block_sum(to_double(sf), sh);
+  const double Sx = block_sum(to_double(sx), sh);
+  const dw mean = dw_from_double(Sx / n);
+  const dw nmean{-mean.h, -mean.l};
+  dw m2{0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < NIPT; j++) {
+    const int k = k0 + j * NB + threadIdx.x;
+    if (k < k1) {
+      dw d = dw_add(dw{xh[j * NB + threadIdx.x], xl[j * NB + threadIdx.x]}, nmean);
+      m2 = dw_add(m2, dw_mul(d, d));
+    }
+  }
+  const double M2 = block_sum(to_double(m2), sh);
   if (threadIdx.x == 0) {
-    double c = (double)(k1 - k0);
-    sg /= c;
-    si /= c;
-    sf /= c;
-    ratio[(size_t)e * D + t] = sg / (si * sf);
+    double *q = part + ((size_t)c * D + t) * 5;
+    q[0] = Sg;
+    q[1] = Si;
+    q[2] = Sf;
+    q[3] = Sx;
+    q[4] = M2;
   }
 }
 
-__global__ void __launch_bounds__(NB)
-k_q_f64(int D, int P, int NQ, const int32_t *__restrict__ qep, const int32_t *__restrict__ qrow,
-        const int32_t *__restrict__ epp, const int32_t *__restrict__ pix,
-        const double *__restrict__ ratio, const float *__restrict__ G2,
-        const float *__restrict__ IP, const float *__restrict__ IF, double *__restrict__ g2,
-        double *__restrict__ se) {
-  __shared__ double sh[NB / 32];
-  const int qi = blockIdx.x / D, t = blockIdx.x - qi * D;
-  const int e0 = qep[qi], e1 = qep[qi + 1];
-  const int k0 = epp[e0], k1 = epp[e1];
-  const size_t o = (size_t)t * P;
-  const int row = qrow[qi];
-  if (threadIdx.x == 0) {
-    double acc = 0.0, cnt = 0.0;
-    for (int e = e0; e < e1; e++) {
-      double r = ratio[(size_t)e * D + t];
-      acc += isnan(r) ? 0.0 : r;
-      cnt += isnan(r) ? 0.0 : 1.0;
+__global__ void k_norm_finish(int NQ, int D, const int32_t *__restrict__ qep,
+                              const int32_t *__restrict__ qrow,
+                              const int32_t *__restrict__ e_chunk_ptr,
+                              const int32_t *__restrict__ ch_k0, const int32_t *__restrict__ ch_k1,
+                              const double *__restrict__ part, double *__restrict__ g2,
+                              double *__restrict__ se) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= NQ * D) return;
+  const int qi = idx / D, t = idx - qi * D;
+  double gacc = 0.0, gcnt = 0.0;
+  double n = 0.0, mean = 0.0, M2 = 0.0;
+  for (int e = qep[qi]; e < qep[qi + 1]; e++) {
+    double sg = 0.0, si = 0.0, sf = 0.0, ne = 0.0;
+    for (int c = e_chunk_ptr[e]; c < e_chunk_ptr[e + 1]; c++) {
+      const double *q = part + ((size_t)c * D + t) * 5;
+      const double nc = (double)(ch_k1[c] - ch_k0[c]);
+      sg += q[0];
+      si += q[1];
+      sf += q[2];
+      ne += nc;
+      // Chan et al.: merge (n, mean, M2) of the chunk into the running one
+      const double mc = q[3] / nc;
+      const double nn = n + nc;
+      const double delta = mc - mean;
+      mean = n == 0.0 ? mc : mean + delta * (nc / nn);
+      M2 = n == 0.0 ? q[4] : M2 + q[4] + delta * delta * (n * nc / nn);
+      n = nn;
     }
-    g2[(size_t)t * NQ + row] = acc / cnt;
+    const double r = (sg / ne) / ((si / ne) * (sf / ne));
+    gacc += isnan(r) ? 0.0 : r;
+    gcnt += isnan(r) ? 0.0 : 1.0;
   }
-  double s = 0.0;
-  for (int k = k0 + threadIdx.x; k < k1; k += NB) {
-    int p = pix[k];
-    double x = (double)G2[o + p] / ((double)IP[o + p] * (double)IF[o + p]);
-    s += isnan(x) ? 0.0 : x;
-  }
-  const double n = (double)(k1 - k0);
-  const double mean = block_sum(s, sh) / n;
-  double m2 = 0.0;
-  for (int k = k0 + threadIdx.x; k < k1; k += NB) {
-    int p = pix[k];
-    double x = (double)G2[o + p] / ((double)IP[o + p] * (double)IF[o + p]);
-    x = isnan(x) ? 0.0 : x;
-    m2 += (x - mean) * (x - mean);
-  }
-  m2 = block_sum(m2, sh);
-  if (threadIdx.x == 0) se[(size_t)t * NQ + row] = sqrt(1.0 / n) * sqrt(m2 / n);
+  const int row = qrow[qi];
+  g2[(size_t)t * NQ + row] = gacc / gcnt;
+  se[(size_t)t * NQ + row] = sqrt(1.0 / n) * sqrt(M2 / n);
 }
+
+// ------------------------------------------------ float32, reference order
 
 __global__ void k_entry_f32(int NE, int D, int P, const int32_t *__restrict__ epp,
                             const int32_t *__restrict__ pix, const float *__restrict__ G2,
@@ -117,27 +205,45 @@ __global__ void k_entry_f32(int NE, int D, int P, const int32_t *__restrict__ ep
   const int e = idx / D, t = idx - e * D;
   const size_t o = (size_t)t * P;
   float sg = 0.f, si = 0.f, sf = 0.f;
-  for (int k = epp[e]; k < epp[e + 1]; k++) {
-    int p = pix[k];
+  const int k0 = epp[e], k1 = epp[e + 1];
+  int k = k0;
+  for (; k + 8 <= k1; k += 8) {  // loads ahead of the three dependent sums
+    float g[8], a[8], b[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int p = pix[k + j];
+      g[j] = G2[o + p];
+      a[j] = IP[o + p];
+      b[j] = IF[o + p];
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      sg = __fadd_rn(sg, g[j]);
+      si = __fadd_rn(si, a[j]);
+      sf = __fadd_rn(sf, b[j]);
+    }
+  }
+  for (; k < k1; k++) {
+    const int p = pix[k];
     sg = __fadd_rn(sg, G2[o + p]);
     si = __fadd_rn(si, IP[o + p]);
     sf = __fadd_rn(sf, IF[o + p]);
   }
-  const float c = (float)(epp[e + 1] - epp[e]);
+  const float c = (float)(k1 - k0);
   sg = __fdiv_rn(sg, c);
   si = __fdiv_rn(si, c);
   sf = __fdiv_rn(sf, c);
   ratio[(size_t)e * D + t] = __fdiv_rn(sg, __fmul_rn(si, sf));
 }
 
-__global__ void k_q_f32(int NQ_, int D, int P, int NQ, const int32_t *__restrict__ qep,
+__global__ void k_q_f32(int NQ, int D, int P, const int32_t *__restrict__ qep,
                         const int32_t *__restrict__ qrow, const int32_t *__restrict__ epp,
                         const int32_t *__restrict__ pix, const float *__restrict__ ratio,
                         const float *__restrict__ G2, const float *__restrict__ IP,
                         const float *__restrict__ IF, float *__restrict__ g2,
                         float *__restrict__ se) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= NQ_ * D) return;
+  if (idx >= NQ * D) return;
   const int qi = idx / D, t = idx - qi * D;
   const int row = qrow[qi];
   const size_t o = (size_t)t * P;
@@ -149,55 +255,91 @@ __global__ void k_q_f32(int NQ_, int D, int P, int NQ, const int32_t *__restrict
   }
   g2[(size_t)t * NQ + row] = __fdiv_rn(acc, cnt);
   float avg = 0.f, sd = 0.f, samples = 0.f;
-  for (int k = epp[qep[qi]]; k < epp[qep[qi + 1]]; k++) {
-    int p = pix[k];
-    float tmpAvg = avg;
-    float x = __fdiv_rn(G2[o + p], __fmul_rn(IP[o + p], IF[o + p]));
-    x = isnan(x) ? 0.f : x;
-    samples = __fadd_rn(samples, 1.f);
-    float tmp0 = __fsub_rn(x, tmpAvg);
-    float tmp00 = __fdiv_rn(tmp0, samples);
-    tmp00 = isnan(tmp00) ? 0.f : tmp00;
-    avg = __fadd_rn(avg, tmp00);
-    float tmp3 = __fmul_rn(__fsub_rn(x, tmpAvg), __fsub_rn(x, avg));
-    sd = __fadd_rn(sd, tmp3);
+  const int k0 = epp[qep[qi]], k1 = epp[qep[qi + 1]];
+  for (int k = k0; k < k1; k += 8) {
+    float xs[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {  // x of the next pixels ahead of the chain
+      xs[j] = 0.f;
+      if (k + j < k1) {
+        const int p = pix[k + j];
+        float x = __fdiv_rn(G2[o + p], __fmul_rn(IP[o + p], IF[o + p]));
+        xs[j] = isnan(x) ? 0.f : x;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (k + j >= k1) break;
+      const float x = xs[j];
+      const float tmpAvg = avg;
+      samples = __fadd_rn(samples, 1.f);
+      float tmp00 = __fdiv_rn(__fsub_rn(x, tmpAvg), samples);
+      tmp00 = isnan(tmp00) ? 0.f : tmp00;
+      avg = __fadd_rn(avg, tmp00);
+      sd = __fadd_rn(sd, __fmul_rn(__fsub_rn(x, tmpAvg), __fsub_rn(x, avg)));
+    }
   }
-  float stdNorm = __fdiv_rn(sd, samples);
-  float inv = __fdiv_rn(1.f, samples);
+  const float stdNorm = __fdiv_rn(sd, samples);
+  const float inv = __fdiv_rn(1.f, samples);
   se[(size_t)t * NQ + row] = __fmul_rn(__fsqrt_rn(inv), __fsqrt_rn(stdNorm));
 }
 
 }  // namespace
+
+void build_norm_chunks(Series &s) {
+  const QMap &q = s.qmap;
+  std::vector<int32_t> k0, k1, eptr(1, 0);
+  for (int e = 0; e < q.nentries(); e++) {
+    for (int a = q.entry_pix_ptr[e]; a < q.entry_pix_ptr[e + 1]; a += NCH) {
+      k0.push_back(a);
+      k1.push_back(std::min(a + NCH, q.entry_pix_ptr[e + 1]));
+    }
+    eptr.push_back((int32_t)k0.size());
+  }
+  s.n_chunks = (int32_t)k0.size();
+  cudaStream_t st = s.stream;
+  auto up = [&](DBuf<int32_t> &b, const std::vector<int32_t> &v) {
+    b.reserve(v.size() ? v.size() : 1, st);
+    if (!v.empty())
+      XG_CUDA(cudaMemcpyAsync(b.p, v.data(), 4 * v.size(), cudaMemcpyHostToDevice, st));
+  };
+  up(s.n_ch_k0, k0);
+  up(s.n_ch_k1, k1);
+  up(s.n_e_chunk_ptr, eptr);
+}
 
 void run_normalize(Series &s, bool want64, bool want32) {
   cudaStream_t st = s.stream;
   const int D = s.D, P = s.P, NQ = s.qmap.nq(), NE = s.qmap.nentries();
   if (D == 0 || NQ == 0) return;
   if (want64) {
-    s.n_ratio64.reserve((size_t)(NE > 0 ? NE : 1) * D, st);
     s.n_g2.reserve((size_t)NQ * D, st);
     s.n_se.reserve((size_t)NQ * D, st);
-    if (NE > 0) {
-      k_entry_f64<<<NE * D, NB, 0, st>>>(D, P, s.n_entry_pix_ptr.p, s.n_pix.p, s.G2.p, s.IP.p,
-                                         s.IF.p, s.n_ratio64.p);
+    const int NC = s.n_chunks;
+    s.n_part.reserve((size_t)(NC > 0 ? NC : 1) * D * 5, st);
+    if (NC > 0) {
+      k_norm_chunk<<<dim3(NC, D), NB, 0, st>>>(D, P, s.n_ch_k0.p, s.n_ch_k1.p, s.n_pix.p, s.G2.p,
+                                              s.IP.p, s.IF.p, s.n_part.p);
       XG_CHECK_LAUNCH();
     }
-    k_q_f64<<<NQ * D, NB, 0, st>>>(D, P, NQ, s.n_q_entry_ptr.p, s.n_q_row.p, s.n_entry_pix_ptr.p,
-                                   s.n_pix.p, s.n_ratio64.p, s.G2.p, s.IP.p, s.IF.p, s.n_g2.p,
-                                   s.n_se.p);
+    const int bs = 128;
+    k_norm_finish<<<(NQ * D + bs - 1) / bs, bs, 0, st>>>(NQ, D, s.n_q_entry_ptr.p, s.n_q_row.p,
+                                                        s.n_e_chunk_ptr.p, s.n_ch_k0.p,
+                                                        s.n_ch_k1.p, s.n_part.p, s.n_g2.p,
+                                                        s.n_se.p);
     XG_CHECK_LAUNCH();
   }
   if (want32) {
     s.n_ratio32.reserve((size_t)(NE > 0 ? NE : 1) * D, st);
     s.n_g2f.reserve((size_t)NQ * D, st);
     s.n_sef.reserve((size_t)NQ * D, st);
-    const int bs = 64;
+    const int bs = 32;
     if (NE > 0) {
       k_entry_f32<<<(NE * D + bs - 1) / bs, bs, 0, st>>>(NE, D, P, s.n_entry_pix_ptr.p, s.n_pix.p,
                                                          s.G2.p, s.IP.p, s.IF.p, s.n_ratio32.p);
       XG_CHECK_LAUNCH();
     }
-    k_q_f32<<<(NQ * D + bs - 1) / bs, bs, 0, st>>>(NQ, D, P, NQ, s.n_q_entry_ptr.p, s.n_q_row.p,
+    k_q_f32<<<(NQ * D + bs - 1) / bs, bs, 0, st>>>(NQ, D, P, s.n_q_entry_ptr.p, s.n_q_row.p,
                                                   s.n_entry_pix_ptr.p, s.n_pix.p, s.n_ratio32.p,
                                                   s.G2.p, s.IP.p, s.IF.p, s.n_g2f.p, s.n_sef.p);
     XG_CHECK_LAUNCH();

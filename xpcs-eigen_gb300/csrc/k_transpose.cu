@@ -195,11 +195,22 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
 // One thread per pixel: merge events of the same filter frame (stream order,
 // float sums exactly as pixels_value_[pix] += v, then / avg), accumulate
 // pixelSum in frame order, classify for the multi-tau kernels.
-__global__ void k_merge_classify(int32_t P, int32_t avg, int32_t cap, const int32_t *__restrict__ cnt,
+__device__ __forceinline__ void record_class(int32_t p, uint8_t c, int32_t n, uint8_t *pclass,
+                                             int32_t *wlist, int32_t *flist, DevStats *stats) {
+  pclass[p] = c;
+  if (c == PCLASS_EMPTY) return;
+  if (c == PCLASS_WARP) wlist[atomicAdd(&stats->nwarp, 1)] = p;
+  if (c == PCLASS_FLOAT) flist[atomicAdd(&stats->nfloat, 1)] = p;
+  atomicAdd(&stats->nvalid, 1);
+  atomicAdd(&stats->events, (unsigned long long)n);
+}
+
+__global__ void k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ cnt,
                                  const int64_t *__restrict__ row_ptr, int32_t *__restrict__ fr,
                                  float *__restrict__ val, int32_t *__restrict__ row_len,
-                                 uint8_t *__restrict__ pclass, int32_t *__restrict__ flist,
-                                 float *__restrict__ pixels_sum, DevStats *__restrict__ stats) {
+                                 uint8_t *__restrict__ pclass, int32_t *__restrict__ wlist,
+                                 int32_t *__restrict__ flist, float *__restrict__ pixels_sum,
+                                 DevStats *__restrict__ stats) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const int32_t n = cnt[p];
@@ -236,13 +247,7 @@ __global__ void k_merge_classify(int32_t P, int32_t avg, int32_t cap, const int3
   }
   row_len[p] = out;
   pixels_sum[p] = psum;
-  // integer path: exact while every partial sum stays below 2^24, which
-  // sum|v| < 4096 guarantees for IP, IF, merged values and G2 products
-  bool int_ok = integral && total < 4096 && out <= cap;
-  pclass[p] = int_ok ? PCLASS_INT : PCLASS_FLOAT;
-  if (!int_ok) flist[atomicAdd(&stats->nfloat, 1)] = p;
-  atomicAdd(&stats->nvalid, 1);
-  atomicAdd(&stats->events, (unsigned long long)out);
+  record_class(p, pixel_class(out, integral, total, F), out, pclass, wlist, flist, stats);
 }
 
 }  // namespace
@@ -256,6 +261,7 @@ void run_filter_transpose(Series &s) {
   s.row_len.reserve(P, st);
   s.pclass.reserve(P, st);
   s.flist.reserve(P, st);
+  s.wlist.reserve(P, st);
   s.pixels_sum.reserve(P, st);
   s.stats.reserve(1, st);
   XG_CUDA(cudaMemsetAsync(s.cnt.p, 0, sizeof(int32_t) * P, st));
@@ -338,8 +344,8 @@ void run_filter_transpose(Series &s) {
   exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
   int bs = 256;
   k_merge_classify<<<(P + bs - 1) / bs, bs, 0, st>>>(
-      P, s.desc.avg_frames, s.cap, s.cnt.p, s.row_ptr.p, s.ev_frame.p, s.ev_val.p, s.row_len.p,
-      s.pclass.p, s.flist.p, s.pixels_sum.p, s.stats.p);
+      P, s.F, s.desc.avg_frames, s.cnt.p, s.row_ptr.p, s.ev_frame.p, s.ev_val.p, s.row_len.p,
+      s.pclass.p, s.wlist.p, s.flist.p, s.pixels_sum.p, s.stats.p);
   XG_CHECK_LAUNCH();
 }
 
@@ -351,10 +357,11 @@ namespace {
 // Caller-held rows (xpcs_multitau2): rows stay as given; a pixel takes the
 // integer path only if its frames are strictly increasing within [0, F), its
 // values are integers and sum |v| < 4096.
-__global__ void k_classify_rows(int32_t P, int32_t F, int32_t cap, const int64_t *__restrict__ row_ptr,
+__global__ void k_classify_rows(int32_t P, int32_t F, const int64_t *__restrict__ row_ptr,
                                 const int32_t *__restrict__ fr, const float *__restrict__ val,
                                 int32_t *__restrict__ row_len, uint8_t *__restrict__ pclass,
-                                int32_t *__restrict__ flist, DevStats *__restrict__ stats) {
+                                int32_t *__restrict__ wlist, int32_t *__restrict__ flist,
+                                DevStats *__restrict__ stats) {
   int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const int64_t b = row_ptr[p];
@@ -364,7 +371,7 @@ __global__ void k_classify_rows(int32_t P, int32_t F, int32_t cap, const int64_t
     pclass[p] = PCLASS_EMPTY;
     return;
   }
-  bool ok = n <= cap;
+  bool ok = n <= MT_WARP_CAP;
   long long total = 0;
   int32_t prev = -1;
   for (int32_t i = 0; i < n && ok; i++) {
@@ -374,11 +381,7 @@ __global__ void k_classify_rows(int32_t P, int32_t F, int32_t cap, const int64_t
     if (ok) total += llabs((long long)x);
     prev = f;
   }
-  ok = ok && total < 4096;
-  pclass[p] = ok ? PCLASS_INT : PCLASS_FLOAT;
-  if (!ok) flist[atomicAdd(&stats->nfloat, 1)] = p;
-  atomicAdd(&stats->nvalid, 1);
-  atomicAdd(&stats->events, (unsigned long long)n);
+  record_class(p, pixel_class(n, ok, total, F), n, pclass, wlist, flist, stats);
 }
 
 }  // namespace
@@ -392,6 +395,7 @@ void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *fram
   s.row_len.reserve(P, st);
   s.pclass.reserve(P, st);
   s.flist.reserve(P, st);
+  s.wlist.reserve(P, st);
   s.stats.reserve(1, st);
   s.ev_frame.reserve(ne, st);
   s.ev_val.reserve(ne, st);
@@ -404,9 +408,9 @@ void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *fram
     XG_CUDA(cudaMemcpyAsync(s.ev_val.p, value, sizeof(float) * events, cudaMemcpyHostToDevice, st));
   }
   const int bs = 256;
-  k_classify_rows<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.F, s.cap, s.row_ptr.p, s.ev_frame.p,
+  k_classify_rows<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.F, s.row_ptr.p, s.ev_frame.p,
                                                      s.ev_val.p, s.row_len.p, s.pclass.p,
-                                                     s.flist.p, s.stats.p);
+                                                     s.wlist.p, s.flist.p, s.stats.p);
   XG_CHECK_LAUNCH();
 }
 

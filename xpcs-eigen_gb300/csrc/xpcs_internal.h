@@ -109,24 +109,55 @@ struct McLevel {
   int32_t lastframe;  // lastframe while this level's delays are evaluated
   int32_t tau_lo;     // first delay in level units (delays are consecutive)
   int32_t compact;    // 1: the reference compacts the rows before this level
+  int32_t t_end;      // lastframe << level: frames >= t_end are dropped by this level
 };
 
 // Kernel-side description of a multi-tau run; lives in device memory.
 struct McPlan {
-  int32_t P, D, F, nlev, mode, cap;
+  int32_t P, D, F, nlev, mode, acc;
   McLevel lv[MAX_LEVELS];
-  // followed in device memory by: int32 tau_lvl[D], float denom[D]
+  // followed in device memory by the per-delay arrays (McArrays)
 };
 
-// Pixel classes assigned by the filter's merge pass.
-enum : uint8_t { PCLASS_EMPTY = 0, PCLASS_INT = 1, PCLASS_FLOAT = 2 };
+// Per-delay arrays stored after McPlan.
+struct McArrays {
+  const int32_t *tau_lvl;  // delay in level units
+  const float *denom;      // (float)(lastframe - tau), 0 = no division
+  const int32_t *tau_abs;  // delay in frames = first frame counted by IF
+  const int32_t *t_ip;     // (lastframe - tau) << level: IP counts frames below it
+  const int32_t *gi;       // level group of the delay
+};
+__host__ __device__ inline size_t mc_align16(size_t x) { return (x + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t mc_plan_bytes(int D) {
+  return mc_align16(sizeof(McPlan) + (size_t)D * 5 * sizeof(int32_t));
+}
+__host__ __device__ inline McArrays mc_arrays(const void *plan, int D) {
+  const int32_t *b = (const int32_t *)((const uint8_t *)plan + sizeof(McPlan));
+  return McArrays{b, (const float *)(b + D), b + 2 * D, b + 3 * D, b + 4 * D};
+}
+
+// Pixel classes assigned by the filter's merge pass.  The integer kernels
+// need integer values with sum |v| < 4096 (every float partial sum of the
+// reference is then exact); the thread-per-pixel kernel also needs frames
+// below 65536 and at most MT_THREAD_CAP events.
+constexpr int MT_THREAD_CAP = 96;
+constexpr int MT_WARP_CAP = 256;
+enum : uint8_t { PCLASS_EMPTY = 0, PCLASS_THREAD = 1, PCLASS_WARP = 2, PCLASS_FLOAT = 3 };
+
+__host__ __device__ inline uint8_t pixel_class(int n, bool integral, long long total, int F) {
+  if (n == 0) return PCLASS_EMPTY;
+  if (!integral || total >= 4096) return PCLASS_FLOAT;
+  if (n <= MT_THREAD_CAP && F <= 65536) return PCLASS_THREAD;
+  if (n <= MT_WARP_CAP) return PCLASS_WARP;
+  return PCLASS_FLOAT;
+}
 
 // Counters written by device passes.
 struct DevStats {
   int32_t error;
   int32_t nfloat;
   int32_t nvalid;
-  int32_t pad;
+  int32_t nwarp;
   unsigned long long events;
 };
 
@@ -164,6 +195,7 @@ struct Series {
   DBuf<int32_t> row_len;    // events per pixel after merging duplicates
   DBuf<uint8_t> pclass;
   DBuf<int32_t> flist;      // pixels of the float path
+  DBuf<int32_t> wlist;      // pixels of the warp-per-pixel integer path
   DBuf<int32_t> ev_frame;   // final pixel-major lists
   DBuf<float> ev_val;
   DBuf<float> pixels_sum;
@@ -176,12 +208,13 @@ struct Series {
   DBuf<uint8_t> plan;       // McPlan + tau_lvl[D] + denom[D]
   DBuf<float> G2, IP, IF;
   bool have_multitau = false;
-  int32_t cap = 0;
 
   // normalisation
   DBuf<int32_t> n_q_entry_ptr, n_entry_sbin, n_entry_pix_ptr, n_pix, n_q_row;
   DBuf<float> n_ratio32;
-  DBuf<double> n_ratio64;
+  DBuf<int32_t> n_ch_k0, n_ch_k1, n_e_chunk_ptr;  // pixel chunks of every entry
+  int32_t n_chunks = 0;
+  DBuf<double> n_part;                            // [chunk][tau][5] partial sums
   DBuf<double> n_g2, n_se;
   DBuf<float> n_g2f, n_sef;
 
@@ -206,7 +239,7 @@ void exclusive_scan_i32_i64(const int32_t *in, int64_t *out, int64_t n, void *ws
 void run_filter_transpose(Series &s);                       // k_transpose.cu
 void run_multitau(Series &s, int mode);                      // k_multitau.cu
 void run_normalize(Series &s, bool want64, bool want32);     // k_normalize.cu
-int multitau_cap(int D);                                     // int-path row capacity
+void build_norm_chunks(Series &s);                           // k_normalize.cu
 
 // Upload caller-held pixel-major rows and classify their pixels (xpcs_multitau2)
 void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *frame,
