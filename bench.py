@@ -194,7 +194,9 @@ def run_reference_arm(args, dist):
 # ------------------------------------------------------------------- GPU
 
 def algorithmic_bytes(P, D, Q, npix, raw_events, events):
-    """Compulsory bytes per launch of each stage."""
+    """Compulsory bytes per launch of each stage: K-a reads 6 B per raw event and writes
+    8 B per event + 12 B per pixel of offsets; K-c reads the lists and writes 12 B per
+    (pixel, delay); K-d reads 12 B per (mapped pixel, delay) and writes 24 B per (q, delay)."""
     ka = 6 * raw_events + 8 * events + 12 * P          # read idx+val, write lists + offsets
     kc = 8 * events + 12 * P + 12 * D * P              # read lists + offsets, write G2/IP/IF
     kd = 12 * D * npix + 24 * D * Q                    # read G2/IP/IF of mapped pixels, write g2/se
