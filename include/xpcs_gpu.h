@@ -171,6 +171,33 @@ int xpcs_multitau2(const int64_t *row_ptr, const int32_t *frame, const float *va
                    int32_t pixels, int32_t frames, int32_t delays_per_level, int32_t mode,
                    int32_t device, float *G2, float *IP, float *IF);
 
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- code that runs inside another framework's memory pool, a process
+ * whose GPU memory budget is fixed up front, or an acquisition loop that must
+ * never call cudaMalloc/cudaFree because they synchronise the device.  It
+ * computes the same G2/IP/IF as xpcs_multitau2 (Corr::multiTau2 semantics,
+ * bit-identical for any rows) but every array argument is a DEVICE pointer the
+ * caller owns: row_ptr [pixels+1] (int64, row_ptr[pixels] == events),
+ * frame/value [events], G2/IP/IF [D][pixels].  It allocates nothing: its
+ * scratch (the working copy of the rows, the level plan and a status word) is
+ * one fixed static device array of 16 KiB + 8 bytes x XPCS_NOALLOC_MAX_EVENTS
+ * (about 32 MiB), which every GPU that loads this library holds until the
+ * process exits.
+ *  - events > XPCS_NOALLOC_MAX_EVENTS is rejected with XPCS_ERR_INVALID_ARGUMENT.
+ *  - Runs on the calling thread's current device, on `stream` (a cudaStream_t;
+ *    NULL = the default stream), and waits for its own work to finish.
+ *  - The first call on a device looks up the scratch's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - All calls on a device share the one scratch array, so calls that overlap
+ *    on the GPU (other host threads, other streams) race: serialise them.
+ *  - Rows whose row_ptr lies outside [0, events] get zero outputs and the call
+ *    returns XPCS_ERR_INPUT. */
+#define XPCS_NOALLOC_MAX_EVENTS 4194304
+int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *frame, const float *value,
+                           int32_t pixels, int64_t events, int32_t frames,
+                           int32_t delays_per_level, int32_t mode, float *G2, float *IP,
+                           float *IF, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

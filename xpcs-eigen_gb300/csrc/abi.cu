@@ -8,13 +8,16 @@
 
 using namespace xg;
 
+namespace {
+thread_local std::string g_last_error;
+}
+
 namespace xg {
 thread_local int64_t tl_launches = 0;
+void xpcs_set_last_error(const char *msg) { g_last_error.assign(msg); }
 }
 
 namespace {
-
-thread_local std::string g_last_error;
 
 template <class F>
 int guarded(F &&f) {

@@ -229,6 +229,9 @@ struct Series {
   size_t pinned_cap = 0;
 };
 
+// Sets the message xpcs_last_error() returns on this thread (abi.cu).
+void xpcs_set_last_error(const char *msg);
+
 // Scans (scan.cu)
 size_t scan_workspace_bytes(int64_t n);
 void exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, void *ws, cudaStream_t st);

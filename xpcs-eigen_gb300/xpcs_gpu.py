@@ -32,8 +32,10 @@ EXPORTS = [
     "xpcs_series_destroy", "xpcs_series_reset", "xpcs_series_get_info", "xpcs_ingest_sparse",
     "xpcs_ingest_sparse_device", "xpcs_multitau", "xpcs_get_g2ipif", "xpcs_normalize",
     "xpcs_synchronize", "xpcs_get_stage_times", "xpcs_multitau2", "xpcs_pin_host",
-    "xpcs_unpin_host",
+    "xpcs_unpin_host", "xpcs_multitau2_noalloc",
 ]
+
+NOALLOC_MAX_EVENTS = 4194304
 
 
 class XpcsError(RuntimeError):
@@ -92,6 +94,9 @@ def lib() -> C.CDLL:
         L.xpcs_multitau.argtypes = [C.c_void_p, C.c_int32]
         L.xpcs_get_g2ipif.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_normalize.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                             C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_pin_host.argtypes = [C.c_void_p, C.c_uint64]
         L.xpcs_unpin_host.argtypes = [C.c_void_p]
         L.xpcs_multitau2.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
@@ -227,3 +232,14 @@ def multitau2(row_ptr, frame, value, frames, dpl, mode=MODE_REFERENCE, device=0)
     check(lib().xpcs_multitau2(_ptr(row_ptr), _ptr(frame), _ptr(value), P, frames, dpl, mode,
                                device, *[_ptr(a) for a in out]))
     return out
+
+
+def multitau2_noalloc(row_ptr_dev: int, frame_dev: int, value_dev: int, pixels: int,
+                      events: int, frames: int, dpl: int, mode: int, G2_dev: int, IP_dev: int,
+                      IF_dev: int, stream: int = 0) -> None:
+    """xpcs_multitau2_noalloc on device buffers the caller owns (raw device
+    addresses); allocates nothing on the device.  Raises XpcsError on failure."""
+    check(lib().xpcs_multitau2_noalloc(
+        C.c_void_p(row_ptr_dev), C.c_void_p(frame_dev), C.c_void_p(value_dev), pixels, events,
+        frames, dpl, mode, C.c_void_p(G2_dev), C.c_void_p(IP_dev), C.c_void_p(IF_dev),
+        C.c_void_p(stream or None)))
