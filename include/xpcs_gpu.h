@@ -136,6 +136,27 @@ int xpcs_ingest_sparse(xpcs_series *s, const int32_t *idx, const int16_t *val,
 int xpcs_ingest_sparse_device(xpcs_series *s, const int32_t *idx_device,
                               const int16_t *val_device, const uint32_t *nnz, int32_t nframes);
 
+/* DarkImage::Compute (dark_image.cpp:81-106) for a dense series: `ndark` raw
+ * int16 frames [ndark][width*height] (the first frames of the file, main.cpp:
+ * 227-239).  Sets the per-pixel dark mean and standard deviation used by
+ * xpcs_ingest_dense.  Call before ingesting frames; without it dense frames are
+ * kept when their value is > 0 (DenseFilter without a dark image). */
+int xpcs_set_dark(xpcs_series *s, const int16_t *dark, int32_t ndark);
+
+/* Imm::NextFrames + DenseFilter::Apply input (imm.cpp:70-118,
+ * dense_filter.cpp:121-210): append `nframes` dense int16 frames
+ * [nframes][width*height] (values read as signed, like the reference).
+ * Dark subtraction, threshold lld + sigma*std and flatfield are applied on the
+ * GPU as frames arrive; only kept pixels are stored. */
+int xpcs_ingest_dense(xpcs_series *s, const int16_t *frames, int32_t nframes);
+
+/* As xpcs_ingest_dense with the frames already in device memory. */
+int xpcs_ingest_dense_device(xpcs_series *s, const int16_t *frames_device, int32_t nframes);
+
+/* The --darkout datasets DarkAvg / DarkStd (main.cpp:459-478): float64
+ * [height*width] each; either may be NULL. */
+int xpcs_get_dark(xpcs_series *s, double *avg, double *std_);
+
 /* Corr::multiTau2 (corr.cpp:315-431), preceded by the filter's transpose of
  * the ingested frames into pixel-major event lists.  Enqueues the work. */
 int xpcs_multitau(xpcs_series *s, int32_t mode);

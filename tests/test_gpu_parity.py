@@ -154,3 +154,74 @@ def test_config0_full_size_vs_oracle():
     assert same_bits_nan(g32, og) and same_bits_nan(s32, os_)
     o64, s64o = oracle.normalize_f64(qm, oG2, oIP, oIF)
     assert max_rel_err(g64, o64) <= F64_TOL and max_rel_err(s64, s64o) <= F64_TOL
+
+
+# ------------------------------------------------------------------ dense frames
+
+def run_gpu_dense(fx, mode=xg.MODE_REFERENCE, chunks=1):
+    nd = fx["ndark"]
+    raw = fx["raw"]
+    with xg.Series(fx["W"], fx["H"], fx["F"], fx["dpl"], fx["dqmap"], fx["sqmap"],
+                   flatfield=fx["flatfield"], stride=fx["stride"], average=fx["avg"],
+                   static_window=fx["swin"], dense=True, lld=float(fx["lld_sigma"][0]),
+                   sigma=float(fx["lld_sigma"][1])) as s:
+        if nd:
+            s.set_dark(raw[:nd])
+        data = raw[nd:]
+        for part in np.array_split(data, chunks):
+            s.ingest_dense(part)
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+        avg, std = s.dark() if nd else (None, None)
+        info = s.info()
+    return dict(G2=G2, IP=IP, IF=IF, g64=g64, s64=s64, g32=g32, s32=s32, avg=avg, std=std,
+                info=info)
+
+
+def test_dense_bit_exact_vs_reference():
+    fx = load("dense_dark")
+    r = run_gpu_dense(fx)
+    for k in ("G2", "IP", "IF"):
+        assert same_bits(r[k], fx["ref_" + k]), k
+    assert same_bits_nan(r["g32"], fx["ref_norm_0_g2"])
+    assert same_bits_nan(r["s32"], fx["ref_norm_0_stderr"])
+    assert r["info"].float_path_pixels > 0
+
+
+def test_dense_dark_image_and_chunked_ingest():
+    fx = load("dense_dark")
+    nd = fx["ndark"]
+    flat = fx["flatfield"].ravel() if fx["flatfield"] is not None else np.ones(fx["W"] * fx["H"])
+    avg, std = oracle.dark_image(fx["raw"][:nd], flat)
+    r = run_gpu_dense(fx, chunks=5)
+    assert same_bits(r["avg"], avg) and same_bits(r["std"], std)
+    one = run_gpu_dense(fx, chunks=1)
+    for k in ("G2", "IP", "IF"):
+        assert same_bits(r[k], one[k]), k
+
+
+def test_dense_medium_vs_oracle():
+    acq = xs.Acquisition(width=96, height=80, frames=700, n_static=12, n_dynamic=6, mean=0.05,
+                         tau_min=5, tau_max=80, seed=31, dpl=8, dense=True, dark_frames=40,
+                         gain_min=0.9, gain_max=1.1)
+    dq, sq, flat, _ = xs.maps(acq)
+    ds = xs.DenseStream(acq)
+    raw = ds.next(acq.dark_frames + acq.frames)
+    ds.close()
+    lld, sigma = 0.0, 3.0
+    with xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, flatfield=flat,
+                   dense=True, lld=lld, sigma=sigma) as s:
+        s.set_dark(raw[:acq.dark_frames])
+        s.ingest_dense(raw[acq.dark_frames:])
+        s.multitau()
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+    qm = oracle.QMap(dq, sq)
+    da, dsd = oracle.dark_image(raw[:acq.dark_frames], flat.ravel())
+    rows, _ = oracle.dense_filter(qm, raw[acq.dark_frames:], acq.frames, da, dsd, lld, sigma,
+                                  flat=flat.ravel())
+    oG2, oIP, oIF = oracle.multitau2(rows, acq.frames, acq.dpl, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+    og, os_ = oracle.normalize_f32(qm, oG2, oIP, oIF)
+    assert same_bits_nan(g32, og) and same_bits_nan(s32, os_)

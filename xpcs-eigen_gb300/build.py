@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-I", str(INCLUDE), "-I", str(CSRC)]
 GPU_SOURCES = ["abi.cu", "scan.cu", "k_transpose.cu", "k_multitau.cu", "k_normalize.cu",
-               "qmap.cpp", "noalloc.cu"]
+               "qmap.cpp", "noalloc.cu", "k_dense.cu"]
 
 LIB_GPU = BUILD / "libxpcs_gpu.so"
 LIB_SYNTH = BUILD / "libxpcs_synth.so"

@@ -92,6 +92,12 @@ void free_series(Series *s) {
                           &s->IP, &s->IF, &s->n_ratio32, &s->n_g2f, &s->n_sef};
     for (auto *b : f32) b->release(st);
     s->raw_val.release(st);
+    s->raw_valf.release(st);
+    s->dark_avg.release(st);
+    s->dark_std.release(st);
+    s->rmin.release(st);
+    s->dn_counts.release(st);
+    s->dn_offsets.release(st);
     s->d_frame_off.release(st);
     s->row_ptr.release(st);
     s->d_mask.release(st);
@@ -148,7 +154,7 @@ int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out) {
     need(desc->stride_frames >= 1 && desc->avg_frames >= 1, "stride/avg must be >= 1");
     need(desc->static_window >= 1, "static_window must be >= 1");
     need(desc->dqmap && desc->sqmap, "dqmap and sqmap are required");
-    need(desc->dense == 0, "dense frames are not supported by this build of the series API");
+    need(desc->dense == 0 || desc->dense == 1, "dense must be 0 or 1");
     s = new Series();
     s->desc = *desc;
     s->desc.dqmap = nullptr;
@@ -201,6 +207,7 @@ int xpcs_series_reset(xpcs_series *h) {
     XG_CUDA(cudaStreamSynchronize(s.stream));
     s.frame_off.assign(1, 0);
     s.raw_events = 0;
+    s.rmin_ready = s.rmin_ready && s.has_dark;
     s.raw_frames = 0;
     s.frame_off_dirty = true;
     s.have_multitau = false;
@@ -267,6 +274,7 @@ int xpcs_ingest_sparse(xpcs_series *h, const int32_t *idx, const int16_t *val,
                        const uint32_t *nnz, int32_t nframes) {
   return guarded([&] {
     need(h, "null handle");
+    if (((Series *)h)->desc.dense) throw Error(XPCS_ERR_STATE, "series was created for dense frames");
     ingest_common(*(Series *)h, idx, val, nnz, nframes, false);
   });
 }
@@ -275,7 +283,53 @@ int xpcs_ingest_sparse_device(xpcs_series *h, const int32_t *idx, const int16_t 
                               const uint32_t *nnz, int32_t nframes) {
   return guarded([&] {
     need(h, "null handle");
+    if (((Series *)h)->desc.dense) throw Error(XPCS_ERR_STATE, "series was created for dense frames");
     ingest_common(*(Series *)h, idx, val, nnz, nframes, true);
+  });
+}
+
+int xpcs_set_dark(xpcs_series *h, const int16_t *dark, int32_t ndark) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if (!s.desc.dense) throw Error(XPCS_ERR_STATE, "darks apply to dense series only");
+    if (s.raw_frames > 0) throw Error(XPCS_ERR_STATE, "set the darks before ingesting frames");
+    need(ndark >= 0 && (ndark == 0 || dark), "bad dark frames");
+    DeviceGuard g(s.device);
+    dense_set_dark(s, dark, ndark);
+  });
+}
+
+static int ingest_dense_common(xpcs_series *h, const int16_t *frames, int32_t nframes, bool dev) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if (!s.desc.dense) throw Error(XPCS_ERR_STATE, "series was created for sparse frames");
+    need(nframes >= 0 && (nframes == 0 || frames), "bad frames");
+    DeviceGuard g(s.device);
+    if (!s.timed_h2d) {
+      XG_CUDA(cudaEventRecord(s.ev[0], s.stream));
+      s.timed_h2d = true;
+    }
+    dense_ingest(s, frames, nframes, dev);
+    XG_CUDA(cudaEventRecord(s.ev[1], s.stream));
+  });
+}
+
+int xpcs_ingest_dense(xpcs_series *h, const int16_t *frames, int32_t nframes) {
+  return ingest_dense_common(h, frames, nframes, false);
+}
+
+int xpcs_ingest_dense_device(xpcs_series *h, const int16_t *frames, int32_t nframes) {
+  return ingest_dense_common(h, frames, nframes, true);
+}
+
+int xpcs_get_dark(xpcs_series *h, double *avg, double *std_) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    dense_get_dark(s, avg, std_);
   });
 }
 

@@ -32,7 +32,8 @@ constexpr int RS_DIGITS = 256;
 
 struct RawCfg {
   const int32_t *idx;
-  const int16_t *val;
+  const int16_t *val;   // sparse series: raw values (flatfield applied here)
+  const float *valf;    // dense series: values already filtered by K-b
   const int64_t *frame_off;  // [nframes+1]
   int32_t nframes;
   int64_t n;
@@ -72,7 +73,6 @@ __device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r,
   const int32_t k = r / c.R_in;
   const int32_t sub = r - k * c.R_in;
   const int32_t p = c.idx[i];
-  const float raw = (float)c.val[i];
   frame = k;
   if (p < 0 || p >= c.P) {
     c.stats->error |= DEVERR_PIXEL_INDEX;
@@ -81,7 +81,12 @@ __device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r,
     return;
   }
   key = (k < c.F && (sub % c.stride) == 0 && c.mask[p]) ? (uint32_t)p : (uint32_t)c.P;
-  v = c.flat ? __double2float_rn(__dmul_rn((double)raw, c.flat[p])) : raw;
+  if (c.valf) {
+    v = c.valf[i];
+  } else {
+    const float raw = (float)c.val[i];
+    v = c.flat ? __double2float_rn(__dmul_rn((double)raw, c.flat[p])) : raw;
+  }
 }
 
 // Item i of a tile in warp-striped order: warp w owns [w*32*IPT, (w+1)*32*IPT),
@@ -296,8 +301,10 @@ void run_filter_transpose(Series &s) {
       s.frB.reserve(n, st);
       s.vB.reserve(n, st);
     }
-    RawCfg rc{s.raw_idx.p, s.raw_val.p, s.d_frame_off.p, s.raw_frames, n, P, s.F, s.R_in,
-              s.desc.stride_frames, s.d_mask.p, s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
+    const bool dense = s.desc.dense != 0;
+    RawCfg rc{s.raw_idx.p, dense ? nullptr : s.raw_val.p, dense ? s.raw_valf.p : nullptr,
+              s.d_frame_off.p, s.raw_frames, n, P, s.F, s.R_in, s.desc.stride_frames, s.d_mask.p,
+              s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
     uint32_t *kbuf[2] = {s.keyA.p, s.keyB.p};
     int32_t *fbuf[2] = {s.frA.p, s.frB.p};
     float *vbuf[2] = {s.vA.p, s.vB.p};

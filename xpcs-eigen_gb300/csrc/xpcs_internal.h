@@ -174,7 +174,8 @@ struct Series {
   // ingested raw frames
   std::vector<int64_t> frame_off{0};  // host copy, [raw_frames+1]
   DBuf<int32_t> raw_idx;
-  DBuf<int16_t> raw_val;
+  DBuf<int16_t> raw_val;    // sparse series: raw int16 values
+  DBuf<float> raw_valf;     // dense series: filtered float values
   DBuf<int64_t> d_frame_off;
   int64_t raw_events = 0;
   int32_t raw_frames = 0;
@@ -184,6 +185,13 @@ struct Series {
   DBuf<uint8_t> d_mask;
   DBuf<double> d_flat;
   bool has_flat = false;
+
+  // dense frames: dark statistics and the per-pixel keep threshold
+  DBuf<double> dark_avg, dark_std;
+  DBuf<int32_t> rmin;
+  bool has_dark = false, rmin_ready = false;
+  DBuf<int32_t> dn_counts;
+  DBuf<int64_t> dn_offsets;
 
   // transpose / event lists
   DBuf<uint32_t> keyA, keyB;
@@ -243,6 +251,11 @@ void run_filter_transpose(Series &s);                       // k_transpose.cu
 void run_multitau(Series &s, int mode);                      // k_multitau.cu
 void run_normalize(Series &s, bool want64, bool want32);     // k_normalize.cu
 void build_norm_chunks(Series &s);                           // k_normalize.cu
+
+// Dense frames (k_dense.cu)
+void dense_set_dark(Series &s, const int16_t *dark_host, int32_t ndark);
+void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_device);
+void dense_get_dark(Series &s, double *avg, double *sd);
 
 // Upload caller-held pixel-major rows and classify their pixels (xpcs_multitau2)
 void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *frame,

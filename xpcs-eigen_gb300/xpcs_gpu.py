@@ -32,7 +32,8 @@ EXPORTS = [
     "xpcs_series_destroy", "xpcs_series_reset", "xpcs_series_get_info", "xpcs_ingest_sparse",
     "xpcs_ingest_sparse_device", "xpcs_multitau", "xpcs_get_g2ipif", "xpcs_normalize",
     "xpcs_synchronize", "xpcs_get_stage_times", "xpcs_multitau2", "xpcs_pin_host",
-    "xpcs_unpin_host", "xpcs_multitau2_noalloc",
+    "xpcs_unpin_host", "xpcs_multitau2_noalloc", "xpcs_set_dark", "xpcs_ingest_dense",
+    "xpcs_ingest_dense_device", "xpcs_get_dark",
 ]
 
 NOALLOC_MAX_EVENTS = 4194304
@@ -92,6 +93,10 @@ def lib() -> C.CDLL:
         L.xpcs_ingest_sparse.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
         L.xpcs_ingest_sparse_device.argtypes = L.xpcs_ingest_sparse.argtypes
         L.xpcs_multitau.argtypes = [C.c_void_p, C.c_int32]
+        L.xpcs_set_dark.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+        L.xpcs_ingest_dense.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+        L.xpcs_ingest_dense_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+        L.xpcs_get_dark.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_get_g2ipif.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_normalize.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
@@ -128,7 +133,7 @@ class Series:
     """One XPCS series on one GPU (an xpcs_series handle)."""
 
     def __init__(self, width, height, frames, dpl, dqmap, sqmap, flatfield=None, stride=1,
-                 average=1, static_window=None, device=0):
+                 average=1, static_window=None, device=0, dense=False, lld=0.0, sigma=0.0):
         self._dq = np.ascontiguousarray(dqmap, np.int32).ravel()
         self._sq = np.ascontiguousarray(sqmap, np.int32).ravel()
         self._flat = (None if flatfield is None
@@ -142,6 +147,7 @@ class Series:
         d.flatfield = (self._flat.ctypes.data_as(C.POINTER(C.c_double))
                        if self._flat is not None else None)
         d.device = device
+        d.dense, d.lld, d.sigma = int(dense), lld, sigma
         self._h = C.c_void_p()
         check(lib().xpcs_series_create(C.byref(d), C.byref(self._h)))
         self.width, self.height, self.frames = width, height, frames
@@ -180,6 +186,22 @@ class Series:
         nnz = np.ascontiguousarray(nnz, np.uint32)
         check(lib().xpcs_ingest_sparse_device(self._h, C.c_void_p(idx_dev_ptr),
                                               C.c_void_p(val_dev_ptr), _ptr(nnz), nnz.size))
+
+    def set_dark(self, dark):
+        dark = np.ascontiguousarray(dark, np.int16)
+        n = dark.shape[0] if dark.ndim > 1 else (1 if dark.size else 0)
+        check(lib().xpcs_set_dark(self._h, _ptr(dark), n))
+
+    def ingest_dense(self, frames):
+        frames = np.ascontiguousarray(frames, np.int16)
+        n = frames.size // (self.width * self.height)
+        check(lib().xpcs_ingest_dense(self._h, _ptr(frames), n))
+
+    def dark(self):
+        avg = np.empty(self.width * self.height, np.float64)
+        std = np.empty_like(avg)
+        check(lib().xpcs_get_dark(self._h, _ptr(avg), _ptr(std)))
+        return avg, std
 
     def multitau(self, mode=MODE_REFERENCE):
         check(lib().xpcs_multitau(self._h, mode))
