@@ -102,25 +102,33 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS) h[d] = 0;
   __syncthreads();
-  int32_t r = 0;
+  uint32_t key[RS_IPT];
+  // all loads first, so that they are in flight together
   if (FIRST) {
     int64_t i0 = item_index(tile, w, 0, lane);
-    r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
-  }
-#pragma unroll 4
-  for (int k = 0; k < RS_IPT; k++) {
-    int64_t i = item_index(tile, w, k, lane);
-    if (i >= pc.n) break;
-    uint32_t key;
-    if (FIRST) {
-      int32_t fr;
-      float v;
-      raw_item(rc, i, r, key, fr, v);
-      if (key != pc.sentinel) atomicAdd(&cnt[key], 1);
-    } else {
-      key = pc.key_in[i];
+    int32_t r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
+#pragma unroll
+    for (int k = 0; k < RS_IPT; k++) {
+      int64_t i = item_index(tile, w, k, lane);
+      key[k] = 0xffffffffu;
+      if (i < pc.n) {
+        int32_t fr;
+        float v;
+        raw_item(rc, i, r, key[k], fr, v);
+      }
     }
-    atomicAdd(&h[(key >> pc.shift) & (RS_DIGITS - 1)], 1u);
+  } else {
+#pragma unroll
+    for (int k = 0; k < RS_IPT; k++) {
+      int64_t i = item_index(tile, w, k, lane);
+      key[k] = i < pc.n ? pc.key_in[i] : 0xffffffffu;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    if (key[k] == 0xffffffffu) continue;
+    if (FIRST && key[k] != pc.sentinel) atomicAdd(&cnt[key[k]], 1);
+    atomicAdd(&h[(key[k] >> pc.shift) & (RS_DIGITS - 1)], 1u);
   }
   __syncthreads();
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
@@ -148,11 +156,14 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
     r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
   }
   const unsigned lt = (1u << lane) - 1u;
+  // all loads first, so that they are in flight together
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
     int64_t i = item_index(tile, w, k, lane);
-    bool ok = i < pc.n;
-    if (ok) {
+    key[k] = 0xffffffffu;
+    fr[k] = 0;
+    v[k] = 0.f;
+    if (i < pc.n) {
       if (FIRST) {
         raw_item(rc, i, r, key[k], fr[k], v[k]);
       } else {
@@ -160,9 +171,11 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
         fr[k] = pc.fr_in[i];
         v[k] = pc.v_in[i];
       }
-    } else {
-      key[k] = 0xffffffffu;
     }
+  }
+#pragma unroll
+  for (int k = 0; k < RS_IPT; k++) {
+    const bool ok = key[k] != 0xffffffffu;
     uint32_t d = ok ? ((key[k] >> pc.shift) & (RS_DIGITS - 1)) : RS_DIGITS;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     int leader = __ffs(peers) - 1;
@@ -210,27 +223,16 @@ __device__ __forceinline__ void record_class(int32_t p, uint8_t c, int32_t n, ui
   atomicAdd(&stats->events, (unsigned long long)n);
 }
 
-__global__ void k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ cnt,
-                                 const int64_t *__restrict__ row_ptr, int32_t *__restrict__ fr,
-                                 float *__restrict__ val, int32_t *__restrict__ row_len,
-                                 uint8_t *__restrict__ pclass, int32_t *__restrict__ wlist,
-                                 int32_t *__restrict__ flist, float *__restrict__ pixels_sum,
-                                 DevStats *__restrict__ stats) {
-  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  const int32_t n = cnt[p];
-  if (n == 0) {
-    row_len[p] = 0;
-    pclass[p] = PCLASS_EMPTY;
-    pixels_sum[p] = 0.f;
-    return;
-  }
-  const int64_t b = row_ptr[p];
-  const float favg = (float)avg;
-  int32_t out = 0, i = 0;
-  float psum = 0.f;
-  bool integral = true;
-  long long total = 0;
+// Per-lane merge of one pixel's row: events of the same filter frame summed in
+// stream order as pixels_value_[pix] += v, then / avg (sparse_filter.cpp:
+// 146-172); pixelSum accumulated in frame order.
+__device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *fr, float *val,
+                          int32_t &out, bool &integral, long long &total, float &psum) {
+  int32_t i = 0;
+  out = 0;
+  integral = true;
+  total = 0;
+  psum = 0.f;
   while (i < n) {
     int32_t f = fr[b + i];
     float acc = 0.f;
@@ -249,6 +251,71 @@ __global__ void k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_
       else
         integral = false;
     }
+  }
+}
+
+// One warp per 32 consecutive pixels (their rows are contiguous): events are
+// read coalesced to detect duplicate frames and to collect, per pixel, whether
+// every value is an integer and sum |v|.  Without duplicates and with avg == 1
+// the rows are final as sorted; otherwise each lane merges its own row.
+__global__ void __launch_bounds__(256)
+k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ cnt,
+                 const int64_t *__restrict__ row_ptr, int32_t *__restrict__ fr,
+                 float *__restrict__ val, int32_t *__restrict__ row_len,
+                 uint8_t *__restrict__ pclass, int32_t *__restrict__ wlist,
+                 int32_t *__restrict__ flist, float *__restrict__ pixels_sum,
+                 DevStats *__restrict__ stats) {
+  __shared__ long long s_total[8][32];
+  __shared__ int32_t s_nonint[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int p0 = (blockIdx.x * 8 + w) * 32;
+  if (p0 >= P) return;
+  const int p = p0 + lane;
+  const int plast = min(p0 + 32, P);
+  const int64_t e0 = row_ptr[p0], e1 = row_ptr[plast];
+  const int64_t my_b = p < P ? row_ptr[p] : e1;
+  const int32_t my_n = p < P ? cnt[p] : 0;
+  s_total[w][lane] = 0;
+  s_nonint[w][lane] = 0;
+  __syncwarp();
+  bool dup = false;
+  for (int64_t base = e0; base < e1; base += 32) {
+    const int64_t e = base + lane;
+    int owner = 0;  // last lane whose row starts at or before e
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const int cand = owner + o;
+      const int64_t cb = __shfl_sync(0xffffffffu, my_b, cand & 31);
+      if (cand < 32 && cb <= e) owner = cand;
+    }
+    const int64_t ob = __shfl_sync(0xffffffffu, my_b, owner);
+    const bool in = e < e1;
+    int32_t f = in ? fr[e] : 0;
+    float x = in ? val[e] : 0.f;
+    int32_t fprev = __shfl_up_sync(0xffffffffu, f, 1);
+    if (lane == 0 && in && e > e0) fprev = fr[e - 1];
+    if (in && e > ob && f == fprev) dup = true;
+    const bool nonint = in && !(x == truncf(x) && fabsf(x) < 16777216.f);
+    const unsigned peers = __match_any_sync(0xffffffffu, in ? owner : 32);
+    const unsigned a = in ? (unsigned)fminf(fabsf(x), 16777216.f) : 0u;
+    const unsigned sum = __reduce_add_sync(peers, a);
+    const unsigned anynon = __reduce_or_sync(peers, nonint ? 1u : 0u);
+    if (in && lane == __ffs(peers) - 1) {
+      s_total[w][owner] += sum;
+      s_nonint[w][owner] |= (int)anynon;
+    }
+    __syncwarp();
+  }
+  dup = __any_sync(0xffffffffu, dup);
+  if (p >= P) return;
+  int32_t out = my_n;
+  bool integral = s_nonint[w][lane] == 0;
+  long long total = s_total[w][lane];
+  float psum = 0.f;
+  if (dup || avg != 1) {
+    merge_row(p, my_n, my_b, (float)avg, fr, val, out, integral, total, psum);
+  } else {
+    for (int32_t i = 0; i < my_n; i++) psum = __fadd_rn(psum, val[my_b + i]);
   }
   row_len[p] = out;
   pixels_sum[p] = psum;
@@ -349,8 +416,8 @@ void run_filter_transpose(Series &s) {
     s.scan_tmp.reserve(scan_workspace_bytes(P), st);
   }
   exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
-  int bs = 256;
-  k_merge_classify<<<(P + bs - 1) / bs, bs, 0, st>>>(
+  const int pix_per_block = 256;
+  k_merge_classify<<<(P + pix_per_block - 1) / pix_per_block, 256, 0, st>>>(
       P, s.F, s.desc.avg_frames, s.cnt.p, s.row_ptr.p, s.ev_frame.p, s.ev_val.p, s.row_len.p,
       s.pclass.p, s.wlist.p, s.flist.p, s.pixels_sum.p, s.stats.p);
   XG_CHECK_LAUNCH();
