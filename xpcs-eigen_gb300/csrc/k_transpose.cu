@@ -35,6 +35,7 @@ struct RawCfg {
   const int16_t *val;   // sparse series: raw values (flatfield applied here)
   const float *valf;    // dense series: values already filtered by K-b
   const int64_t *frame_off;  // [nframes+1]
+  const int32_t *frame_map;  // [nframes]: filter frame of a raw frame, -1 if unused
   int32_t nframes;
   int64_t n;
   int32_t P, F, R_in, stride;
@@ -70,8 +71,7 @@ __device__ __forceinline__ int32_t frame_of(const RawCfg &c, int64_t i) {
 __device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r, uint32_t &key,
                                          int32_t &frame, float &v) {
   while (c.frame_off[r + 1] <= i) r++;
-  const int32_t k = r / c.R_in;
-  const int32_t sub = r - k * c.R_in;
+  const int32_t k = c.frame_map[r];
   const int32_t p = c.idx[i];
   frame = k;
   if (p < 0 || p >= c.P) {
@@ -80,7 +80,7 @@ __device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r,
     v = 0.f;
     return;
   }
-  key = (k < c.F && (sub % c.stride) == 0 && c.mask[p]) ? (uint32_t)p : (uint32_t)c.P;
+  key = (k >= 0 && c.mask[p]) ? (uint32_t)p : (uint32_t)c.P;
   if (c.valf) {
     v = c.valf[i];
   } else {
@@ -346,6 +346,15 @@ void run_filter_transpose(Series &s) {
     s.d_frame_off.reserve(s.frame_off.size(), st);
     XG_CUDA(cudaMemcpyAsync(s.d_frame_off.p, s.frame_off.data(),
                             sizeof(int64_t) * s.frame_off.size(), cudaMemcpyHostToDevice, st));
+    s.frame_map.resize(s.raw_frames);
+    for (int32_t r = 0; r < s.raw_frames; r++) {  // stride*avg raw frames per filter frame
+      const int32_t k = r / s.R_in;
+      s.frame_map[r] = (k < s.F && ((r - k * s.R_in) % s.desc.stride_frames) == 0) ? k : -1;
+    }
+    s.d_frame_map.reserve(s.frame_map.size() ? s.frame_map.size() : 1, st);
+    if (!s.frame_map.empty())
+      XG_CUDA(cudaMemcpyAsync(s.d_frame_map.p, s.frame_map.data(),
+                              sizeof(int32_t) * s.frame_map.size(), cudaMemcpyHostToDevice, st));
     s.frame_off_dirty = false;
   }
 
@@ -370,8 +379,8 @@ void run_filter_transpose(Series &s) {
     }
     const bool dense = s.desc.dense != 0;
     RawCfg rc{s.raw_idx.p, dense ? nullptr : s.raw_val.p, dense ? s.raw_valf.p : nullptr,
-              s.d_frame_off.p, s.raw_frames, n, P, s.F, s.R_in, s.desc.stride_frames, s.d_mask.p,
-              s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
+              s.d_frame_off.p, s.d_frame_map.p, s.raw_frames, n, P, s.F, s.R_in,
+              s.desc.stride_frames, s.d_mask.p, s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
     uint32_t *kbuf[2] = {s.keyA.p, s.keyB.p};
     int32_t *fbuf[2] = {s.frA.p, s.frB.p};
     float *vbuf[2] = {s.vA.p, s.vB.p};
