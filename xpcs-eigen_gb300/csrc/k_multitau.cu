@@ -220,19 +220,34 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
     const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
     for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
     const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
+    // two pointers: jlo = first partner at distance >= tlo (monotone in i);
+    // the word at jlo and the next word of the scan are held in registers
     int jlo = 1;
+    uint32_t wlo = m > 1 ? row[32] : 0u;
+    uint32_t wi = m > 0 ? row[0] : 0u;
     for (int i = 0; i < m; i++) {
-      const uint32_t wi = row[i * 32];
       const int ti = pk_t(wi), vi = pk_v(wi);
-      if (jlo <= i) jlo = i + 1;
-      while (jlo < m && pk_t(row[jlo * 32]) - ti < tlo) jlo++;
-      for (int j = jlo; j < m; j++) {
-        const uint32_t wj = row[j * 32];
+      const uint32_t wi_next = i + 1 < m ? row[(i + 1) * 32] : 0u;
+      if (jlo <= i) {
+        jlo = i + 1;
+        wlo = wi_next;
+      }
+      while (jlo < m && pk_t(wlo) - ti < tlo) {
+        jlo++;
+        wlo = jlo < m ? row[jlo * 32] : 0u;
+      }
+      int j = jlo;
+      uint32_t wj = wlo;
+      while (j < m) {
         const int d = pk_t(wj) - ti;
         if (d > thi) break;
-        if (!sorted && lower_bound_packed(row, n0, pk_t(wj)) != j) continue;
-        acc[(d - tlo) * 32] += vi * pk_v(wj);
+        const uint32_t wn = j + 1 < m ? row[(j + 1) * 32] : 0u;
+        if (sorted || lower_bound_packed(row, n0, pk_t(wj)) == j)
+          acc[(d - tlo) * 32] += vi * pk_v(wj);
+        j++;
+        wj = wn;
       }
+      wi = wi_next;
     }
     if (p < P) {
       for (int k = 0; k < L.count; k++) {

@@ -69,20 +69,44 @@ __device__ __forceinline__ dw dw_mul(dw x, dw y) {
   float t = __fmaf_rn(x.l, y.h, __fmaf_rn(x.h, y.l, __fmul_rn(x.l, y.l)));
   return fast_two_sum(c.h, __fadd_rn(c.l, t));
 }
-// float / double-word: one correctly rounded quotient plus the quotient of
-// the (FMA-exact) remainder
+// float / double-word: a quotient from the reciprocal of the high word, then
+// the quotient of the FMA remainder a - q (bh + bl) as the low word
+// (relative error a few 2^-48)
 __device__ __forceinline__ dw f_div_dw(float a, dw b) {
-  float q = __fdiv_rn(a, b.h);
-  if (!isfinite(q) || q == 0.f) return {q, 0.f};
+  const float rb = __frcp_rn(b.h);
+  float q = __fmul_rn(a, rb);
+  if (!isfinite(q) || q == 0.f) return {__fdiv_rn(a, b.h), 0.f};
   float r = __fmaf_rn(-q, b.h, a);
   r = __fmaf_rn(-q, b.l, r);
-  return fast_two_sum(q, __fdiv_rn(r, b.h));
+  return fast_two_sum(q, __fmul_rn(r, rb));
 }
 __device__ __forceinline__ dw dw_from_double(double x) {
   float h = __double2float_rn(x);
   return {h, __double2float_rn(x - (double)h)};
 }
 __device__ __forceinline__ double to_double(dw x) { return (double)x.h + (double)x.l; }
+
+// Sums N doubles over the block at once (one pair of barriers).
+template <int N>
+__device__ __forceinline__ void block_sum_n(double (&x)[N], double *sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; k++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; k++) sh[k * (NB / 32) + w] = x[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    double r = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < NB / 32; ww++) r += sh[k * (NB / 32) + ww];
+    x[k] = r;
+  }
+  __syncthreads();
+}
 
 __device__ __forceinline__ double block_sum(double x, double *sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -108,7 +132,7 @@ __global__ void __launch_bounds__(NB)
 k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__restrict__ ch_k1,
              const int32_t *__restrict__ pix, const float *__restrict__ G2,
              const float *__restrict__ IP, const float *__restrict__ IF, double *__restrict__ part) {
-  __shared__ double sh[NB / 32 + 1];
+  __shared__ double sh[4 * (NB / 32) + 1];
   __shared__ float xh[NCH], xl[NCH];
   const int c = blockIdx.x, t = blockIdx.y;
   const int k0 = ch_k0[c], k1 = ch_k1[c];
@@ -131,10 +155,9 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
     }
   }
   const double n = (double)(k1 - k0);
-  const double Sg = block_sum(to_double(sg), sh);
-  const double Si = block_sum(to_double(si), sh);
-  const double Sf = block_sum(to_double(sf), sh);
-  const double Sx = block_sum(to_double(sx), sh);
+  double sums[4] = {to_double(sg), to_double(si), to_double(sf), to_double(sx)};
+  block_sum_n<4>(sums, sh);
+  const double Sg = sums[0], Si = sums[1], Sf = sums[2], Sx = sums[3];
   const dw mean = dw_from_double(Sx / n);
   const dw nmean{-mean.h, -mean.l};
   dw m2{0.f, 0.f};

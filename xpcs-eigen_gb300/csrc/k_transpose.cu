@@ -29,6 +29,7 @@ constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_IPT = 16;                      // items per lane
 constexpr int RS_TILE = RS_THREADS * RS_IPT;    // 4096
 constexpr int RS_DIGITS = 256;
+static_assert(RS_THREADS == RS_DIGITS, "one digit per thread in the downsweep scan");
 
 struct RawCfg {
   const int32_t *idx;
@@ -135,15 +136,27 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
     hist[(int64_t)d * pc.ntiles + tile] = h[d];
 }
 
+// Shared memory of the downsweep: per-warp digit counters, the tile's global
+// and local digit offsets, and the tile staged in digit order.
+struct DsSmem {
+  uint32_t wcnt[RS_WARPS][RS_DIGITS];
+  uint32_t toff[RS_DIGITS];
+  uint32_t tstart[RS_DIGITS];
+  uint32_t wtot[RS_THREADS / 32];
+  uint32_t key[RS_TILE];
+  int32_t fr[RS_TILE];
+  float v[RS_TILE];
+};
+
 template <bool FIRST, bool LAST>
 __global__ void __launch_bounds__(RS_THREADS)
 k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
-  __shared__ uint32_t wcnt[RS_WARPS][RS_DIGITS];
-  __shared__ uint32_t toff[RS_DIGITS];
+  extern __shared__ __align__(16) uint8_t ds_raw[];
+  DsSmem &sm = *reinterpret_cast<DsSmem *>(ds_raw);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
-  for (int d = lane; d < RS_DIGITS; d += 32) wcnt[w][d] = 0;
+  for (int d = lane; d < RS_DIGITS; d += 32) sm.wcnt[w][d] = 0;
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
-    toff[d] = offsets[(int64_t)d * pc.ntiles + tile];
+    sm.toff[d] = offsets[(int64_t)d * pc.ntiles + tile];
   __syncwarp();
 
   uint32_t key[RS_IPT];
@@ -173,6 +186,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
       }
     }
   }
+  // stable rank within the warp: equal digits keep (round, lane) order
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
     const bool ok = key[k] != 0xffffffffu;
@@ -181,32 +195,59 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
     int leader = __ffs(peers) - 1;
     uint32_t base = 0;
     if (ok && lane == leader) {
-      base = wcnt[w][d];
-      wcnt[w][d] = base + __popc(peers);
+      base = sm.wcnt[w][d];
+      sm.wcnt[w][d] = base + __popc(peers);
     }
     base = __shfl_sync(0xffffffffu, base, leader);
     rank[k] = base + __popc(peers & lt);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS) {
+  // per digit: exclusive over warps; tile total -> tile-local digit starts
+  {
+    const int d = threadIdx.x;  // RS_THREADS == RS_DIGITS
     uint32_t run = 0;
 #pragma unroll
     for (int ww = 0; ww < RS_WARPS; ww++) {
-      uint32_t c = wcnt[ww][d];
-      wcnt[ww][d] = run;
+      uint32_t c = sm.wcnt[ww][d];
+      sm.wcnt[ww][d] = run;
       run += c;
     }
+    uint32_t x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sm.wtot[w] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int ww = 0; ww < w; ww++) before += sm.wtot[ww];
+    sm.tstart[d] = before + x - run;
   }
   __syncthreads();
+  // stage the tile in digit order
 #pragma unroll
   for (int k = 0; k < RS_IPT; k++) {
     if (key[k] == 0xffffffffu) continue;
-    if (LAST && key[k] == pc.sentinel) continue;
-    uint32_t d = (key[k] >> pc.shift) & (RS_DIGITS - 1);
-    uint32_t pos = toff[d] + wcnt[w][d] + rank[k];
-    if (!LAST) pc.key_out[pos] = key[k];
-    pc.fr_out[pos] = fr[k];
-    pc.v_out[pos] = v[k];
+    const uint32_t d = (key[k] >> pc.shift) & (RS_DIGITS - 1);
+    const uint32_t q = sm.tstart[d] + sm.wcnt[w][d] + rank[k];
+    sm.key[q] = key[k];
+    sm.fr[q] = fr[k];
+    sm.v[q] = v[k];
+  }
+  __syncthreads();
+  // write out: consecutive staged elements of a digit go to consecutive addresses
+  uint32_t nvalid = 0;
+#pragma unroll
+  for (int ww = 0; ww < RS_THREADS / 32; ww++) nvalid += sm.wtot[ww];
+  for (uint32_t q = threadIdx.x; q < nvalid; q += RS_THREADS) {
+    const uint32_t kq = sm.key[q];
+    if (LAST && kq == pc.sentinel) continue;
+    const uint32_t d = (kq >> pc.shift) & (RS_DIGITS - 1);
+    const uint32_t pos = sm.toff[d] + (q - sm.tstart[d]);
+    if (!LAST) pc.key_out[pos] = kq;
+    pc.fr_out[pos] = sm.fr[q];
+    pc.v_out[pos] = sm.v[q];
   }
 }
 
@@ -322,6 +363,14 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ 
   record_class(p, pixel_class(out, integral, total, F), out, pclass, wlist, flist, stats);
 }
 
+template <bool FIRST, bool LAST>
+void launch_downsweep(int ntiles, size_t smem, cudaStream_t st, const RawCfg &rc,
+                      const PassCfg &pc, const uint32_t *offsets) {
+  XG_CUDA(cudaFuncSetAttribute(k_downsweep<FIRST, LAST>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_downsweep<FIRST, LAST><<<ntiles, RS_THREADS, smem, st>>>(rc, pc, offsets);
+}
+
 }  // namespace
 
 void run_filter_transpose(Series &s) {
@@ -411,14 +460,15 @@ void run_filter_transpose(Series &s) {
         k_upsweep<false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
       XG_CHECK_LAUNCH();
       exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
+      const size_t dsm = sizeof(DsSmem);
       if (first && last)
-        k_downsweep<true, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+        launch_downsweep<true, true>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
       else if (first)
-        k_downsweep<true, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+        launch_downsweep<true, false>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
       else if (last)
-        k_downsweep<false, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+        launch_downsweep<false, true>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
       else
-        k_downsweep<false, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist_scan.p);
+        launch_downsweep<false, false>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
       XG_CHECK_LAUNCH();
     }
   } else {
