@@ -29,7 +29,7 @@ namespace xg {
 namespace {
 
 constexpr int NB = 256;          // threads per chunk block
-constexpr int NIPT = 8;          // pixels per thread
+constexpr int NIPT = 16;         // pixels per thread
 constexpr int NCH = NB * NIPT;   // pixels per chunk
 
 // ------------------------------------------------ double-word arithmetic
@@ -73,6 +73,7 @@ __device__ __forceinline__ dw dw_mul(dw x, dw y) {
 // the quotient of the FMA remainder a - q (bh + bl) as the low word
 // (relative error a few 2^-48)
 __device__ __forceinline__ dw f_div_dw(float a, dw b) {
+  if (a == 0.f) return {0.f, 0.f};  // 0 / b is 0 or NaN, and NaN counts as 0
   const float rb = __frcp_rn(b.h);
   float q = __fmul_rn(a, rb);
   if (!isfinite(q) || q == 0.f) return {__fdiv_rn(a, b.h), 0.f};
@@ -104,6 +105,32 @@ __device__ __forceinline__ void block_sum_n(double (&x)[N], double *sh) {
 #pragma unroll
     for (int ww = 0; ww < NB / 32; ww++) r += sh[k * (NB / 32) + ww];
     x[k] = r;
+  }
+  __syncthreads();
+}
+
+// Block sum of N double-word values: warp reduction in double-word arithmetic
+// on the FP32 pipes, FP64 only for the per-warp partials.
+template <int N>
+__device__ __forceinline__ void block_sum_dw(dw (&x)[N], double (&out)[N], double *sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; k++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dw y{__shfl_down_sync(0xffffffffu, x[k].h, o), __shfl_down_sync(0xffffffffu, x[k].l, o)};
+      x[k] = dw_add(x[k], y);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; k++) sh[k * (NB / 32) + w] = to_double(x[k]);
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    double r = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < NB / 32; ww++) r += sh[k * (NB / 32) + ww];
+    out[k] = r;
   }
   __syncthreads();
 }
@@ -155,8 +182,9 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
     }
   }
   const double n = (double)(k1 - k0);
-  double sums[4] = {to_double(sg), to_double(si), to_double(sf), to_double(sx)};
-  block_sum_n<4>(sums, sh);
+  dw parts[4] = {sg, si, sf, sx};
+  double sums[4];
+  block_sum_dw<4>(parts, sums, sh);
   const double Sg = sums[0], Si = sums[1], Sf = sums[2], Sx = sums[3];
   const dw mean = dw_from_double(Sx / n);
   const dw nmean{-mean.h, -mean.l};
@@ -169,7 +197,10 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
       m2 = dw_add(m2, dw_mul(d, d));
     }
   }
-  const double M2 = block_sum(to_double(m2), sh);
+  dw mparts[1] = {m2};
+  double msum[1];
+  block_sum_dw<1>(mparts, msum, sh);
+  const double M2 = msum[0];
   if (threadIdx.x == 0) {
     double *q = part + ((size_t)c * D + t) * 5;
     q[0] = Sg;

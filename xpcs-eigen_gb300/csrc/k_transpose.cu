@@ -69,9 +69,14 @@ __device__ __forceinline__ int32_t frame_of(const RawCfg &c, int64_t i) {
   return lo;
 }
 
-__device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r, uint32_t &key,
-                                         int32_t &frame, float &v) {
-  while (c.frame_off[r + 1] <= i) r++;
+// r: raw frame of the previous item of this lane, nb = frame_off[r + 1] (kept
+// in a register so that the common case, no frame boundary crossed, loads nothing)
+__device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r, int64_t &nb,
+                                         uint32_t &key, int32_t &frame, float &v) {
+  while (nb <= i) {
+    r++;
+    nb = c.frame_off[r + 1];
+  }
   const int32_t k = c.frame_map[r];
   const int32_t p = c.idx[i];
   frame = k;
@@ -108,6 +113,7 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
   if (FIRST) {
     int64_t i0 = item_index(tile, w, 0, lane);
     int32_t r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
+    int64_t nb = rc.frame_off[r + 1];
 #pragma unroll
     for (int k = 0; k < RS_IPT; k++) {
       int64_t i = item_index(tile, w, k, lane);
@@ -115,7 +121,7 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
       if (i < pc.n) {
         int32_t fr;
         float v;
-        raw_item(rc, i, r, key[k], fr, v);
+        raw_item(rc, i, r, nb, key[k], fr, v);
       }
     }
   } else {
@@ -164,9 +170,11 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   float v[RS_IPT];
   uint32_t rank[RS_IPT];
   int32_t r = 0;
+  int64_t nb = 0;
   if (FIRST) {
     int64_t i0 = item_index(tile, w, 0, lane);
     r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
+    nb = rc.frame_off[r + 1];
   }
   const unsigned lt = (1u << lane) - 1u;
   // all loads first, so that they are in flight together
@@ -178,7 +186,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
     v[k] = 0.f;
     if (i < pc.n) {
       if (FIRST) {
-        raw_item(rc, i, r, key[k], fr[k], v[k]);
+        raw_item(rc, i, r, nb, key[k], fr[k], v[k]);
       } else {
         key[k] = pc.key_in[i];
         fr[k] = pc.fr_in[i];

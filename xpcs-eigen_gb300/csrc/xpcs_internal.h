@@ -140,7 +140,10 @@ __host__ __device__ inline McArrays mc_arrays(const void *plan, int D) {
 // need integer values with sum |v| < 4096 (every float partial sum of the
 // reference is then exact); the thread-per-pixel kernel also needs frames
 // below 65536 and at most MT_THREAD_CAP events.
-constexpr int MT_THREAD_CAP = 96;
+#ifndef XG_MT_THREAD_CAP
+#define XG_MT_THREAD_CAP 96
+#endif
+constexpr int MT_THREAD_CAP = XG_MT_THREAD_CAP;
 constexpr int MT_WARP_CAP = 256;
 enum : uint8_t { PCLASS_EMPTY = 0, PCLASS_THREAD = 1, PCLASS_WARP = 2, PCLASS_FLOAT = 3 };
 
