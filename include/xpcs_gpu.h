@@ -171,6 +171,18 @@ int xpcs_get_g2ipif(xpcs_series *s, float *G2, float *IP, float *IF);
 int xpcs_normalize(xpcs_series *s, double *g2, double *stderr_, float *g2_f32,
                    float *stderr_f32);
 
+/* The filters' side statistics after main.cpp's post-processing, bit-identical
+ * to the reference's datasets (sparse_filter.cpp:133-190, dense_filter.cpp:
+ * 176-208, main.cpp:321-411):
+ *   pixel_sum              pixelSum, float32 [height*width]
+ *   frame_sum              frameSum, float32 [2][frames]
+ *   partition_mean_total   partition-mean-total, float32 [total_static]
+ *   partition_mean_partial partition-mean-partial, float32
+ *                          [frames / static_window][total_static]
+ * Any pointer may be NULL.  Needs xpcs_multitau to have run. */
+int xpcs_side_stats(xpcs_series *s, float *pixel_sum, float *frame_sum,
+                    float *partition_mean_total, float *partition_mean_partial);
+
 /* Waits for the handle's stream; reports deferred device errors. */
 int xpcs_synchronize(xpcs_series *s);
 

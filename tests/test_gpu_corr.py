@@ -1,0 +1,93 @@
+"""The C++ `corr` driver end to end: for every golden case the IMM frames and
+the analysis file are rebuilt from the fixture's inputs, `corr --g2out
+--darkout` runs on them, and every dataset it writes must be bit-identical to
+what the reference's own `corr` wrote for the same inputs."""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import build
+import refio
+from fixtures import CASES, load, same_bits_nan
+
+DATASETS = ["G2", "IP", "IF", "norm-0-g2", "norm-0-stderr", "pixelSum", "frameSum",
+            "partition-mean-total", "partition-mean-partial", "timestamp_clock",
+            "timestamp_tick", "tau", "partition_norm_factor"]
+
+
+def _write_inputs(fx, wd: Path):
+    imm = wd / "frames.imm"
+    W, H = fx["W"], fx["H"]
+    flat = fx["flatfield"]
+    if fx["dense"]:
+        nd = fx["ndark"]
+        refio.write_imm_dense(imm, H, W, fx["raw"], clock=fx["clock"], ticks=fx["ticks"])
+        cfg = refio.config_entries(W, H, fx["dqmap"], fx["sqmap"], imm, first=nd + 1,
+                                   last=nd + fx["F"], dpl=fx["dpl"], compression=False,
+                                   flat=flat, dark=(1, nd), lld=float(fx["lld_sigma"][0]),
+                                   sigma=float(fx["lld_sigma"][1]), static_window=fx["swin"])
+    else:
+        refio.write_imm_sparse(imm, H, W, fx["nnz"], fx["idx"], fx["val"], clock=fx["clock"],
+                               ticks=fx["ticks"])
+        cfg = refio.config_entries(W, H, fx["dqmap"], fx["sqmap"], imm, first=1, last=fx["real"],
+                                   dpl=fx["dpl"], stride=fx["stride"], average=fx["avg"],
+                                   flat=flat, static_window=fx["swin"])
+    path = wd / "analysis.h5"
+    refio.write_xh5c(path, cfg)
+    return path
+
+
+@pytest.fixture(scope="module")
+def corr():
+    return build.build_corr()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_corr_matches_reference_outputs(corr, case, tmp_path):
+    fx = load(case)
+    cfg = _write_inputs(fx, tmp_path)
+    r = subprocess.run([str(corr), str(cfg), "--g2out", "--darkout"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = {k.split("/")[-1]: v for k, v in refio.read_xh5c(cfg).items() if k.startswith("/exchange/")}
+    for name in DATASETS:
+        ref = fx["ref_" + name.replace("-", "_")]
+        assert name in out, name
+        assert same_bits_nan(np.asarray(out[name]).reshape(ref.shape), ref), name
+    if fx["dense"]:
+        n = fx["W"] * fx["H"]
+        assert out["DarkAvg"].size == n and out["DarkStd"].size == n
+
+
+def test_corr_rejects_unsupported_reader_flags(corr, tmp_path):
+    r = subprocess.run([str(corr), str(tmp_path / "x.h5"), "--ufxc"], capture_output=True,
+                       text=True)
+    assert r.returncode != 0 and "outside the multi-tau IMM path" in r.stderr
+
+
+def test_corr_rejects_unsupported_analyses(corr, tmp_path):
+    fx = load("sparse_basic")
+    cfg = _write_inputs(fx, tmp_path)
+    ent = refio.read_xh5c(cfg)
+    ent["/xpcs/normalize_by_framesum"] = np.int32(1)
+    refio.write_xh5c(cfg, ent)
+    r = subprocess.run([str(corr), str(cfg)], capture_output=True, text=True)
+    assert r.returncode != 0 and "normalize_by_framesum" in r.stderr
+
+
+def test_corr_reads_config_and_frames_without_a_device(corr, tmp_path):
+    """On a machine without a GPU the driver parses the analysis file and the
+    IMM headers, then fails at series creation with the library's status."""
+    import shutil
+    if shutil.which("nvidia-smi"):
+        pytest.skip("a GPU is present")
+    for case in ("sparse_stride_avg", "dense_dark"):
+        fx = load(case)
+        cfg = _write_inputs(fx, tmp_path)
+        r = subprocess.run([str(corr), str(cfg)], capture_output=True, text=True)
+        assert r.returncode == 1
+        assert f"{fx['F']} frames (stride {fx['stride']}, average {fx['avg']})" in r.stdout
+        assert "(7): no CUDA device" in r.stderr

@@ -225,3 +225,33 @@ def test_dense_medium_vs_oracle():
     assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
     og, os_ = oracle.normalize_f32(qm, oG2, oIP, oIF)
     assert same_bits_nan(g32, og) and same_bits_nan(s32, os_)
+
+
+# ------------------------------------------------------------- side statistics
+
+def _side_gpu(fx):
+    if fx["dense"]:
+        nd = fx["ndark"]
+        s = xg.Series(fx["W"], fx["H"], fx["F"], fx["dpl"], fx["dqmap"], fx["sqmap"],
+                      flatfield=fx["flatfield"], stride=fx["stride"], average=fx["avg"],
+                      static_window=fx["swin"], dense=True, lld=float(fx["lld_sigma"][0]),
+                      sigma=float(fx["lld_sigma"][1]))
+        if nd:
+            s.set_dark(fx["raw"][:nd])
+        s.ingest_dense(fx["raw"][nd:])
+    else:
+        s = series_for(fx)
+        s.ingest_sparse(fx["nnz"], fx["idx"], fx["val"])
+    with s:
+        s.multitau()
+        return s.side_stats(fx["swin"])
+
+
+@pytest.mark.parametrize("case", [c for c in __import__("fixtures").CASES])
+def test_side_statistics_bit_exact_vs_reference(case):
+    fx = load(case)
+    ps, fs, tot, part = _side_gpu(fx)
+    assert same_bits_nan(ps, fx["ref_pixelSum"])
+    assert same_bits_nan(fs, fx["ref_frameSum"])
+    assert same_bits_nan(tot, fx["ref_partition_mean_total"])
+    assert same_bits_nan(part, fx["ref_partition_mean_partial"])

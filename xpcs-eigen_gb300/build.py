@@ -29,10 +29,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-I", str(INCLUDE), "-I", str(CSRC)]
 GPU_SOURCES = ["abi.cu", "scan.cu", "k_transpose.cu", "k_multitau.cu", "k_normalize.cu",
-               "qmap.cpp", "noalloc.cu", "k_dense.cu"]
+               "qmap.cpp", "noalloc.cu", "k_dense.cu", "k_side.cu"]
 
 LIB_GPU = BUILD / "libxpcs_gpu.so"
 LIB_SYNTH = BUILD / "libxpcs_synth.so"
+CORR = BUILD / "corr"
+HOST = PKG / "host"
 
 
 def _run(cmd):
@@ -83,13 +85,25 @@ def build_synth(force: bool = False) -> Path:
     return LIB_SYNTH
 
 
+def build_corr(force: bool = False) -> Path:
+    """The C++ `corr` driver, linked against libxpcs_gpu.so (rpath $ORIGIN)."""
+    srcs = [HOST / "corr_main.cpp", HOST / "xh5c.cpp", HOST / "imm.cpp"]
+    deps = srcs + [HOST / "xh5c.h", HOST / "imm.h", INCLUDE / "xpcs_gpu.h", LIB_GPU]
+    if force or _stale(CORR, deps):
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", str(INCLUDE), "-o", str(CORR)]
+             + [str(x) for x in srcs] + ["-L", str(BUILD), "-lxpcs_gpu",
+                                         "-Wl,-rpath,$ORIGIN"])
+    return CORR
+
+
 def build_all(force: bool = False) -> None:
     with ThreadPoolExecutor(max_workers=2) as ex:
         futs = [ex.submit(build_gpu, force), ex.submit(build_synth, force)]
         for f in futs:
             f.result()
+    build_corr(force)
 
 
 if __name__ == "__main__":
     build_all(force="--force" in sys.argv)
-    print("built", LIB_GPU, LIB_SYNTH)
+    print("built", LIB_GPU, LIB_SYNTH, CORR)

@@ -86,7 +86,8 @@ void free_series(Series *s) {
     DBuf<int32_t> *i32[] = {&s->raw_idx, &s->frA, &s->frB, &s->cnt, &s->row_len,
                             &s->flist, &s->wlist, &s->ev_frame, &s->sc_frame, &s->n_q_entry_ptr,
                             &s->n_entry_sbin, &s->n_entry_pix_ptr, &s->n_pix, &s->n_q_row,
-                            &s->n_ch_k0, &s->n_ch_k1, &s->n_e_chunk_ptr};
+                            &s->n_ch_k0, &s->n_ch_k1, &s->n_e_chunk_ptr, &s->d_sbin,
+                            &s->d_ppb};
     for (auto *b : i32) b->release(st);
     DBuf<float> *f32[] = {&s->vA, &s->vB, &s->ev_val, &s->pixels_sum, &s->sc_val, &s->G2,
                           &s->IP, &s->IF, &s->n_ratio32, &s->n_g2f, &s->n_sef};
@@ -107,6 +108,8 @@ void free_series(Series *s) {
     s->plan.release(st);
     s->d_flat.release(st);
     s->n_part.release(st);
+    s->side_pos.release(st);
+    s->side_out.release(st);
     s->n_g2.release(st);
     s->n_se.release(st);
     s->keyA.release(st);
@@ -190,6 +193,10 @@ int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out) {
     std::vector<int32_t> rows(q.q_ids.size());
     for (size_t k = 0; k < rows.size(); k++) rows[k] = q.q_ids[k] - 1;
     upload(s->n_q_row, rows, st);
+    std::vector<int32_t> sb(s->P);
+    for (int32_t i = 0; i < s->P; i++) sb[i] = q.valid[i] ? q.sbin[i] - 1 : -1;
+    upload(s->d_sbin, sb, st);
+    upload(s->d_ppb, q.pixels_per_bin, st);
     build_norm_chunks(*s);
     XG_CUDA(cudaStreamSynchronize(st));
     *out = (xpcs_series *)s;
@@ -389,6 +396,18 @@ int xpcs_normalize(xpcs_series *h, double *g2, double *se, float *g2f, float *se
     }
     XG_CUDA(cudaEventRecord(s.ev[11], st));
     sync_and_check(s);
+  });
+}
+
+int xpcs_side_stats(xpcs_series *h, float *pixel_sum, float *frame_sum,
+                    float *partition_mean_total, float *partition_mean_partial) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if (!s.have_multitau) throw Error(XPCS_ERR_STATE, "xpcs_multitau has not run");
+    DeviceGuard g(s.device);
+    sync_and_check(s);
+    run_side_stats(s, SideOut{pixel_sum, frame_sum, partition_mean_total, partition_mean_partial});
   });
 }
 

@@ -381,6 +381,43 @@ void launch_downsweep(int ntiles, size_t smem, cudaStream_t st, const RawCfg &rc
 
 }  // namespace
 
+// Stable LSD radix sort of (key, a, b) triples by the low `key_bits` bits of
+// key, with the passes above; (key2, a2, b2) is scratch of the same length.
+// Returns true when the sorted triples ended in the scratch arrays.
+bool radix_sort_triples(Series &s, uint32_t *key, int32_t *a, float *b, uint32_t *key2,
+                        int32_t *a2, float *b2, int64_t n, int key_bits) {
+  cudaStream_t st = s.stream;
+  if (n <= 0 || key_bits <= 0) return false;
+  const int passes = (key_bits + 7) / 8;
+  const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+  s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
+  s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);
+  s.scan_tmp.reserve(scan_workspace_bytes((int64_t)RS_DIGITS * ntiles), st);
+  RawCfg rc{};
+  uint32_t *kb[2] = {key, key2};
+  int32_t *ab[2] = {a, a2};
+  float *bb[2] = {b, b2};
+  for (int pass = 0; pass < passes; pass++) {
+    PassCfg pc{};
+    pc.n = n;
+    pc.shift = 8 * pass;
+    pc.ntiles = ntiles;
+    pc.sentinel = 0xfffffffeu;
+    pc.key_in = kb[pass & 1];
+    pc.fr_in = ab[pass & 1];
+    pc.v_in = bb[pass & 1];
+    pc.key_out = kb[(pass + 1) & 1];
+    pc.fr_out = ab[(pass + 1) & 1];
+    pc.v_out = bb[(pass + 1) & 1];
+    k_upsweep<false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, nullptr);
+    XG_CHECK_LAUNCH();
+    exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
+    launch_downsweep<false, false>(ntiles, sizeof(DsSmem), st, rc, pc, s.hist_scan.p);
+    XG_CHECK_LAUNCH();
+  }
+  return (passes & 1) != 0;
+}
+
 void run_filter_transpose(Series &s) {
   cudaStream_t st = s.stream;
   const int64_t n = s.raw_events;

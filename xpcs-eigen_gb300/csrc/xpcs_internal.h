@@ -141,7 +141,7 @@ __host__ __device__ inline McArrays mc_arrays(const void *plan, int D) {
 // reference is then exact); the thread-per-pixel kernel also needs frames
 // below 65536 and at most MT_THREAD_CAP events.
 #ifndef XG_MT_THREAD_CAP
-#define XG_MT_THREAD_CAP 96
+#define XG_MT_THREAD_CAP 80
 #endif
 constexpr int MT_THREAD_CAP = XG_MT_THREAD_CAP;
 constexpr int MT_WARP_CAP = 256;
@@ -212,6 +212,10 @@ struct Series {
   DBuf<int32_t> ev_frame;   // final pixel-major lists
   DBuf<float> ev_val;
   DBuf<float> pixels_sum;
+  DBuf<int32_t> d_sbin;     // per pixel: static bin - 1 (-1 none)
+  DBuf<int32_t> d_ppb;      // pixels per static bin
+  DBuf<int64_t> side_pos;
+  DBuf<float> side_out;
   DBuf<int32_t> sc_frame;   // float-path scratch rows
   DBuf<float> sc_val;
   DBuf<uint8_t> scan_tmp;
@@ -256,6 +260,20 @@ void run_filter_transpose(Series &s);                       // k_transpose.cu
 void run_multitau(Series &s, int mode);                      // k_multitau.cu
 void run_normalize(Series &s, bool want64, bool want32);     // k_normalize.cu
 void build_norm_chunks(Series &s);                           // k_normalize.cu
+
+// Stable radix sort of (key, a, b) by the low key_bits of key (k_transpose.cu);
+// returns true when the result is in the second set of arrays.
+bool radix_sort_triples(Series &s, uint32_t *key, int32_t *a, float *b, uint32_t *key2,
+                        int32_t *a2, float *b2, int64_t n, int key_bits);
+
+// Side statistics (k_side.cu)
+struct SideOut {
+  float *pixel_sum;       // [P]
+  float *frame_sum;       // [2][F]
+  float *part_total;      // [S]
+  float *part_partial;    // [floor(F / static_window)][S]
+};
+void run_side_stats(Series &s, const SideOut &out);
 
 // Dense frames (k_dense.cu)
 void dense_set_dark(Series &s, const int16_t *dark_host, int32_t ndark);

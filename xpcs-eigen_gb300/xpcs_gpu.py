@@ -33,7 +33,7 @@ EXPORTS = [
     "xpcs_ingest_sparse_device", "xpcs_multitau", "xpcs_get_g2ipif", "xpcs_normalize",
     "xpcs_synchronize", "xpcs_get_stage_times", "xpcs_multitau2", "xpcs_pin_host",
     "xpcs_unpin_host", "xpcs_multitau2_noalloc", "xpcs_set_dark", "xpcs_ingest_dense",
-    "xpcs_ingest_dense_device", "xpcs_get_dark",
+    "xpcs_ingest_dense_device", "xpcs_get_dark", "xpcs_side_stats",
 ]
 
 NOALLOC_MAX_EVENTS = 4194304
@@ -97,6 +97,7 @@ def lib() -> C.CDLL:
         L.xpcs_ingest_dense.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
         L.xpcs_ingest_dense_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
         L.xpcs_get_dark.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.xpcs_side_stats.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.xpcs_get_g2ipif.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_normalize.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
@@ -214,6 +215,19 @@ class Series:
             out = tuple(np.empty((self.D, self.P), np.float32) for _ in range(3))
         check(lib().xpcs_get_g2ipif(self._h, *[_ptr(a) for a in out]))
         return out
+
+    def side_stats(self, static_window):
+        """pixelSum [H][W], frameSum [2][F], partition-mean-total [1][S],
+        partition-mean-partial [F // static_window][S] (float32)."""
+        i = self.info()
+        S = i.total_static
+        nwin = self.frames // static_window
+        ps = np.empty((self.height, self.width), np.float32)
+        fs = np.empty((2, self.frames), np.float32)
+        tot = np.empty((1, S), np.float32)
+        part = np.empty((nwin, S), np.float32)
+        check(lib().xpcs_side_stats(self._h, _ptr(ps), _ptr(fs), _ptr(tot), _ptr(part)))
+        return ps, fs, tot, part
 
     def normalize(self, f64=True, f32=True, out=None):
         if out is None:
