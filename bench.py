@@ -3,6 +3,7 @@ sparse series (Poisson speckle, mean 0.005 photons/pixel/frame, tau_c
 log-uniform [5,500] per ring, 36/18 rings, 8 delays per level).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--width W --frames F]   (reduced series, for profiling)
 
 One JSON line on rank 0.  `value`: frames/s of one step with the raw frames
 resident in HBM (filter/transpose + multi-tau + normalisation, CUDA events on
@@ -40,6 +41,13 @@ WORKLOAD = "c1"
 WORKLOAD_DESC = ("1024x1024 detector, 10000 sparse IMM frames (uint16 counts), Poisson speckle "
                  "mean 0.005 photons/pixel/frame, tau_c log-uniform [5,500] per dynamic ring, "
                  "36 static / 18 dynamic rings, 5% masked pixels, 8 delays per level")
+
+
+def workload_desc(acq) -> str:
+    if (acq.width, acq.height, acq.frames) == (1024, 1024, 10000):
+        return WORKLOAD_DESC
+    return (f"{acq.width}x{acq.height} detector, {acq.frames} sparse IMM frames, otherwise as the "
+            "1024x1024 10000-frame series (a reduced case for profiling)")
 
 
 def rank_env():
@@ -96,6 +104,9 @@ class ClockSampler:
              "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         self.t = threading.Thread(target=self._read, daemon=True)
         self.t.start()
+        t0 = time.perf_counter()  # nvidia-smi takes a moment to print its first sample
+        while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+            time.sleep(0.02)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -127,8 +138,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_series_data(name=WORKLOAD):
-    acq = xs.preset(name)
+def make_series_data(name=WORKLOAD, width=None, frames=None):
+    over = {}
+    if width:
+        over.update(width=width, height=width)
+    if frames:
+        over["frames"] = frames
+    acq = xs.preset(name, **over)
     dq, sq, _, _ = xs.maps(acq)
     nnz, idx, val = xs.sparse_frames(acq)
     return acq, dq, sq, nnz, idx, val
@@ -207,7 +223,7 @@ def run_gpu_arm(args, dist):
     import xpcs_gpu as xg
 
     dev = dist.local
-    acq, dq, sq, nnz, idx, val = make_series_data()
+    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames)
     F, P = acq.frames, acq.width * acq.height
     xg.pin(idx)
     xg.pin(val)
@@ -286,7 +302,8 @@ def run_gpu_arm(args, dist):
         "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32/f32 (bit-exact multi-tau), f64 normalisation",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_DESC, "detector": "1024x1024", "frames": F, "delays": D,
+        "config": {"workload": workload_desc(acq), "detector": f"{acq.width}x{acq.height}",
+                   "frames": F, "delays": D,
                    "qbins": Q, "raw_events": int(info.raw_events), "events": int(info.events),
                    "float_path_pixels": int(info.float_path_pixels), "mode": "reference",
                    "l2": "no flush: every step reads and writes > 1 GB (inputs 313 MB, "
@@ -310,8 +327,8 @@ def run_gpu_arm(args, dist):
         t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
         result["cpu_baseline"] = {
             "value": frames / t_cpu, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
-            "sample": f"first {frames} of {F} frames, full 1024x1024 detector (oracle restatement "
-                      "of SparseFilter + multiTau2 + normalizeG2s)"}
+            "sample": f"first {frames} of {F} frames, full {acq.width}x{acq.height} detector "
+                      "(oracle restatement of SparseFilter + multiTau2 + normalizeG2s)"}
     s.close()
     xg.unpin(idx)
     xg.unpin(val)
@@ -322,11 +339,15 @@ def run_gpu_arm(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-frames", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--width", type=int, default=None,
+                    help="square detector side (reduced case for profiling; default 1024)")
+    ap.add_argument("--frames", type=int, default=None,
+                    help="frames in the series (reduced case for profiling; default 10000)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     dist = Dist()

@@ -101,6 +101,7 @@ void free_series(Series *s) {
     s->dn_offsets.release(st);
     s->d_frame_off.release(st);
     s->d_frame_map.release(st);
+    s->d_chunk_frame.release(st);
     s->row_ptr.release(st);
     s->d_mask.release(st);
     s->pclass.release(st);

@@ -7,18 +7,20 @@
 // pixel's events come out contiguous and in stream order (frame order).
 //
 //   pass 0   reads the raw events directly: per event it derives the filter
-//            frame (raw frame / (stride*avg)), drops masked pixels, unused
-//            stride sub-frames and frames past the end (key = P, sorts last),
-//            and forms v = (float)(value * flatfield) as the reference does
-//            (sparse_filter.cpp:149-153).
+//            frame (raw frame / (stride*avg), from a per-512-event table of
+//            raw frames and a per-raw-frame table of filter frames), drops
+//            unused stride sub-frames and frames past the end (key = P, sorts
+//            last), and forms v = (float)(value * flatfield) as the reference
+//            does (sparse_filter.cpp:149-153).
 //   pass k   8-bit digit k of the pixel index: tile histograms -> digit-major
 //            exclusive scan -> stable scatter.  Ranking inside a tile uses
 //            warp match_any + per-warp digit counters, so equal digits keep
 //            stream order (tile, warp, round, lane).
-//   merge    one thread per pixel sums events of the same filter frame in
-//            stream order, divides by avg (sparse_filter.cpp:160-172),
-//            accumulates pixelSum in frame order and classifies the pixel for
-//            the multi-tau kernels.
+//   merge    one warp per 32 pixels: events of the same filter frame are
+//            summed in stream order and divided by avg (sparse_filter.cpp:
+//            160-172), pixelSum is accumulated in frame order, pixels outside
+//            the mask (sparse_filter.cpp:147) get empty rows, and every pixel
+//            is classified for the multi-tau kernels.
 #include "xpcs_internal.h"
 
 namespace xg {
@@ -37,10 +39,10 @@ struct RawCfg {
   const float *valf;    // dense series: values already filtered by K-b
   const int64_t *frame_off;  // [nframes+1]
   const int32_t *frame_map;  // [nframes]: filter frame of a raw frame, -1 if unused
+  const int32_t *chunk_frame;  // [ceil(n / 512)]: raw frame of item 512 c
   int32_t nframes;
   int64_t n;
   int32_t P, F, R_in, stride;
-  const uint8_t *mask;
   const double *flat;  // may be null
   DevStats *stats;
 };
@@ -58,27 +60,39 @@ struct PassCfg {
   uint32_t sentinel;
 };
 
-// first raw frame r with frame_off[r+1] > i
-__device__ __forceinline__ int32_t frame_of(const RawCfg &c, int64_t i) {
-  int32_t lo = 0, hi = c.nframes - 1;
-  while (lo < hi) {
-    int32_t mid = (lo + hi + 1) >> 1;
-    if (c.frame_off[mid] <= i) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
+// Raw frame of the first item of every 512-item chunk (one warp's share of a
+// tile): chunk c starts in frame r when off[r] <= 512 c < off[r + 1].
+constexpr int RS_CHUNK = 512;
+
+__global__ void k_chunk_frames(int32_t nframes, const int64_t *__restrict__ off, int64_t nchunks,
+                               int32_t *__restrict__ chunk_frame) {
+  const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nframes) return;
+  const int64_t c0 = (off[r] + RS_CHUNK - 1) / RS_CHUNK;
+  const int64_t c1 = min((off[r + 1] + RS_CHUNK - 1) / RS_CHUNK, nchunks);
+  for (int64_t c = c0; c < c1; c++) chunk_frame[c] = r;
 }
 
-// r: raw frame of the previous item of this lane, nb = frame_off[r + 1] (kept
-// in a register so that the common case, no frame boundary crossed, loads nothing)
-__device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r, int64_t &nb,
-                                         uint32_t &key, int32_t &frame, float &v) {
+// The raw loads of item i (pixel index and value), issued before any of the
+// per-item work so that a lane's loads are in flight together.
+__device__ __forceinline__ void raw_load(const RawCfg &c, int64_t i, int32_t &p, float &v) {
+  p = c.idx[i];
+  v = c.valf ? c.valf[i] : (float)c.val[i];
+}
+
+// Filter frame, sort key and filtered value of item i.  r is the raw frame of
+// this lane's previous item, nb = frame_off[r + 1] and k = frame_map[r], kept
+// in registers so that the common case (no frame boundary crossed) loads
+// nothing.  Masked pixels keep their own key here; their rows are emptied by
+// the merge, which reads the mask once per pixel instead of once per event.
+__device__ __forceinline__ void raw_key(const RawCfg &c, int64_t i, int32_t &r, int64_t &nb,
+                                        int32_t &k, int32_t p, float &v, uint32_t &key,
+                                        int32_t &frame) {
   while (nb <= i) {
     r++;
     nb = c.frame_off[r + 1];
+    k = c.frame_map[r];
   }
-  const int32_t k = c.frame_map[r];
-  const int32_t p = c.idx[i];
   frame = k;
   if (p < 0 || p >= c.P) {
     c.stats->error |= DEVERR_PIXEL_INDEX;
@@ -86,13 +100,8 @@ __device__ __forceinline__ void raw_item(const RawCfg &c, int64_t i, int32_t &r,
     v = 0.f;
     return;
   }
-  key = (k >= 0 && c.mask[p]) ? (uint32_t)p : (uint32_t)c.P;
-  if (c.valf) {
-    v = c.valf[i];
-  } else {
-    const float raw = (float)c.val[i];
-    v = c.flat ? __double2float_rn(__dmul_rn((double)raw, c.flat[p])) : raw;
-  }
+  key = k >= 0 ? (uint32_t)p : (uint32_t)c.P;
+  if (!c.valf && c.flat) v = __double2float_rn(__dmul_rn((double)v, c.flat[p]));
 }
 
 // Item i of a tile in warp-striped order: warp w owns [w*32*IPT, (w+1)*32*IPT),
@@ -111,17 +120,28 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
   uint32_t key[RS_IPT];
   // all loads first, so that they are in flight together
   if (FIRST) {
-    int64_t i0 = item_index(tile, w, 0, lane);
-    int32_t r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
+    const int64_t nch = (rc.n + RS_CHUNK - 1) / RS_CHUNK;
+    int32_t r = rc.chunk_frame[min((int64_t)tile * RS_WARPS + w, nch - 1)];
     int64_t nb = rc.frame_off[r + 1];
+    int32_t kf = rc.frame_map[r];
+    int32_t pix[RS_IPT];
+#pragma unroll
+    for (int k = 0; k < RS_IPT; k++) {
+      const int64_t i = item_index(tile, w, k, lane);
+      pix[k] = i < pc.n ? rc.idx[i] : 0;
+    }
 #pragma unroll
     for (int k = 0; k < RS_IPT; k++) {
       int64_t i = item_index(tile, w, k, lane);
       key[k] = 0xffffffffu;
       if (i < pc.n) {
-        int32_t fr;
-        float v;
-        raw_item(rc, i, r, nb, key[k], fr, v);
+        while (nb <= i) {
+          r++;
+          nb = rc.frame_off[r + 1];
+          kf = rc.frame_map[r];
+        }
+        const int32_t p = pix[k];
+        key[k] = (p < 0 || p >= rc.P || kf < 0) ? (uint32_t)rc.P : (uint32_t)p;
       }
     }
   } else {
@@ -169,25 +189,36 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   int32_t fr[RS_IPT];
   float v[RS_IPT];
   uint32_t rank[RS_IPT];
-  int32_t r = 0;
-  int64_t nb = 0;
-  if (FIRST) {
-    int64_t i0 = item_index(tile, w, 0, lane);
-    r = frame_of(rc, i0 < rc.n ? i0 : rc.n - 1);
-    nb = rc.frame_off[r + 1];
-  }
   const unsigned lt = (1u << lane) - 1u;
   // all loads first, so that they are in flight together
+  if (FIRST) {
+    const int64_t nch = (rc.n + RS_CHUNK - 1) / RS_CHUNK;
+    int32_t r = rc.chunk_frame[min((int64_t)tile * RS_WARPS + w, nch - 1)];
+    int64_t nb = rc.frame_off[r + 1];
+    int32_t kf = rc.frame_map[r];
+    int32_t pix[RS_IPT];
 #pragma unroll
-  for (int k = 0; k < RS_IPT; k++) {
-    int64_t i = item_index(tile, w, k, lane);
-    key[k] = 0xffffffffu;
-    fr[k] = 0;
-    v[k] = 0.f;
-    if (i < pc.n) {
-      if (FIRST) {
-        raw_item(rc, i, r, nb, key[k], fr[k], v[k]);
-      } else {
+    for (int k = 0; k < RS_IPT; k++) {
+      const int64_t i = item_index(tile, w, k, lane);
+      pix[k] = 0;
+      v[k] = 0.f;
+      if (i < pc.n) raw_load(rc, i, pix[k], v[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < RS_IPT; k++) {
+      const int64_t i = item_index(tile, w, k, lane);
+      key[k] = 0xffffffffu;
+      fr[k] = 0;
+      if (i < pc.n) raw_key(rc, i, r, nb, kf, pix[k], v[k], key[k], fr[k]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < RS_IPT; k++) {
+      int64_t i = item_index(tile, w, k, lane);
+      key[k] = 0xffffffffu;
+      fr[k] = 0;
+      v[k] = 0.f;
+      if (i < pc.n) {
         key[k] = pc.key_in[i];
         fr[k] = pc.fr_in[i];
         v[k] = pc.v_in[i];
@@ -259,17 +290,34 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   }
 }
 
-// One thread per pixel: merge events of the same filter frame (stream order,
-// float sums exactly as pixels_value_[pix] += v, then / avg), accumulate
-// pixelSum in frame order, classify for the multi-tau kernels.
-__device__ __forceinline__ void record_class(int32_t p, uint8_t c, int32_t n, uint8_t *pclass,
-                                             int32_t *wlist, int32_t *flist, DevStats *stats) {
-  pclass[p] = c;
-  if (c == PCLASS_EMPTY) return;
-  if (c == PCLASS_WARP) wlist[atomicAdd(&stats->nwarp, 1)] = p;
-  if (c == PCLASS_FLOAT) flist[atomicAdd(&stats->nfloat, 1)] = p;
-  atomicAdd(&stats->nvalid, 1);
-  atomicAdd(&stats->events, (unsigned long long)n);
+// Classification of the pixels of one warp (all 32 lanes call it; lanes
+// without a pixel pass has = false): pclass, the float/warp work lists and the
+// counters, one atomic per warp and counter.
+__device__ __forceinline__ void record_class_warp(bool has, int32_t p, uint8_t c, int32_t n,
+                                                  uint8_t *pclass, int32_t *wlist, int32_t *flist,
+                                                  DevStats *stats) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  if (has) pclass[p] = c;
+  const bool live = has && c != PCLASS_EMPTY;
+  const unsigned mv = __ballot_sync(FULL, live);
+  const unsigned mw = __ballot_sync(FULL, live && c == PCLASS_WARP);
+  const unsigned mf = __ballot_sync(FULL, live && c == PCLASS_FLOAT);
+  const unsigned ev = __reduce_add_sync(FULL, live ? (unsigned)n : 0u);
+  int bw = 0, bf = 0;
+  if (lane == 0) {
+    if (mv) {
+      atomicAdd(&stats->nvalid, __popc(mv));
+      atomicAdd(&stats->events, (unsigned long long)ev);
+    }
+    if (mw) bw = atomicAdd(&stats->nwarp, __popc(mw));
+    if (mf) bf = atomicAdd(&stats->nfloat, __popc(mf));
+  }
+  bw = __shfl_sync(FULL, bw, 0);
+  bf = __shfl_sync(FULL, bf, 0);
+  if (live && c == PCLASS_WARP) wlist[bw + __popc(mw & lt)] = p;
+  if (live && c == PCLASS_FLOAT) flist[bf + __popc(mf & lt)] = p;
 }
 
 // Per-lane merge of one pixel's row: events of the same filter frame summed in
@@ -305,26 +353,33 @@ __device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *
 
 // One warp per 32 consecutive pixels (their rows are contiguous): events are
 // read coalesced to detect duplicate frames and to collect, per pixel, whether
-// every value is an integer and sum |v|.  Without duplicates and with avg == 1
-// the rows are final as sorted; otherwise each lane merges its own row.
+// every value is an integer, sum |v| and sum v.  Without duplicates and with
+// avg == 1 the rows are final as sorted, and for integer rows with sum |v| <
+// 2^24 every float partial sum of pixelSum is exact, so pixelSum = (float)sum v;
+// otherwise each lane merges its own row / sums it in frame order.  Pixels
+// outside the mask get empty rows.
 __global__ void __launch_bounds__(256)
 k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ cnt,
-                 const int64_t *__restrict__ row_ptr, int32_t *__restrict__ fr,
-                 float *__restrict__ val, int32_t *__restrict__ row_len,
+                 const int64_t *__restrict__ row_ptr, const uint8_t *__restrict__ mask,
+                 int32_t *__restrict__ fr, float *__restrict__ val, int32_t *__restrict__ row_len,
                  uint8_t *__restrict__ pclass, int32_t *__restrict__ wlist,
                  int32_t *__restrict__ flist, float *__restrict__ pixels_sum,
                  DevStats *__restrict__ stats) {
   __shared__ long long s_total[8][32];
+  __shared__ long long s_sum[8][32];
   __shared__ int32_t s_nonint[8][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int p0 = (blockIdx.x * 8 + w) * 32;
   if (p0 >= P) return;
   const int p = p0 + lane;
+  const bool has = p < P;
   const int plast = min(p0 + 32, P);
   const int64_t e0 = row_ptr[p0], e1 = row_ptr[plast];
-  const int64_t my_b = p < P ? row_ptr[p] : e1;
-  const int32_t my_n = p < P ? cnt[p] : 0;
+  const int64_t my_b = has ? row_ptr[p] : e1;
+  const int32_t my_n = has ? cnt[p] : 0;
+  const bool keep = has && mask[p] != 0;
   s_total[w][lane] = 0;
+  s_sum[w][lane] = 0;
   s_nonint[w][lane] = 0;
   __syncwarp();
   bool dup = false;
@@ -347,28 +402,37 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ 
     const bool nonint = in && !(x == truncf(x) && fabsf(x) < 16777216.f);
     const unsigned peers = __match_any_sync(0xffffffffu, in ? owner : 32);
     const unsigned a = in ? (unsigned)fminf(fabsf(x), 16777216.f) : 0u;
+    const int xi = (in && !nonint) ? (int)x : 0;
     const unsigned sum = __reduce_add_sync(peers, a);
+    const int ssum = __reduce_add_sync(peers, xi);
     const unsigned anynon = __reduce_or_sync(peers, nonint ? 1u : 0u);
     if (in && lane == __ffs(peers) - 1) {
       s_total[w][owner] += sum;
+      s_sum[w][owner] += ssum;
       s_nonint[w][owner] |= (int)anynon;
     }
     __syncwarp();
   }
   dup = __any_sync(0xffffffffu, dup);
-  if (p >= P) return;
-  int32_t out = my_n;
+  int32_t out = keep ? my_n : 0;
   bool integral = s_nonint[w][lane] == 0;
   long long total = s_total[w][lane];
   float psum = 0.f;
-  if (dup || avg != 1) {
-    merge_row(p, my_n, my_b, (float)avg, fr, val, out, integral, total, psum);
-  } else {
-    for (int32_t i = 0; i < my_n; i++) psum = __fadd_rn(psum, val[my_b + i]);
+  if (keep) {
+    if (dup || avg != 1) {
+      merge_row(p, my_n, my_b, (float)avg, fr, val, out, integral, total, psum);
+    } else if (integral && total < 16777216) {
+      psum = (float)s_sum[w][lane];
+    } else {
+      for (int32_t i = 0; i < my_n; i++) psum = __fadd_rn(psum, val[my_b + i]);
+    }
   }
-  row_len[p] = out;
-  pixels_sum[p] = psum;
-  record_class(p, pixel_class(out, integral, total, F), out, pclass, wlist, flist, stats);
+  if (has) {
+    row_len[p] = out;
+    pixels_sum[p] = psum;
+  }
+  const uint8_t c = keep ? pixel_class(out, integral, total, F) : (uint8_t)PCLASS_EMPTY;
+  record_class_warp(has, p, c, out, pclass, wlist, flist, stats);
 }
 
 template <bool FIRST, bool LAST>
@@ -472,9 +536,14 @@ void run_filter_transpose(Series &s) {
       s.vB.reserve(n, st);
     }
     const bool dense = s.desc.dense != 0;
+    const int64_t nch = (n + RS_CHUNK - 1) / RS_CHUNK;
+    s.d_chunk_frame.reserve((size_t)nch, st);
+    k_chunk_frames<<<(s.raw_frames + 255) / 256, 256, 0, st>>>(s.raw_frames, s.d_frame_off.p, nch,
+                                                              s.d_chunk_frame.p);
+    XG_CHECK_LAUNCH();
     RawCfg rc{s.raw_idx.p, dense ? nullptr : s.raw_val.p, dense ? s.raw_valf.p : nullptr,
-              s.d_frame_off.p, s.d_frame_map.p, s.raw_frames, n, P, s.F, s.R_in,
-              s.desc.stride_frames, s.d_mask.p, s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
+              s.d_frame_off.p, s.d_frame_map.p, s.d_chunk_frame.p, s.raw_frames, n, P, s.F,
+              s.R_in, s.desc.stride_frames, s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
     uint32_t *kbuf[2] = {s.keyA.p, s.keyB.p};
     int32_t *fbuf[2] = {s.frA.p, s.frB.p};
     float *vbuf[2] = {s.vA.p, s.vB.p};
@@ -522,8 +591,8 @@ void run_filter_transpose(Series &s) {
   exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
   const int pix_per_block = 256;
   k_merge_classify<<<(P + pix_per_block - 1) / pix_per_block, 256, 0, st>>>(
-      P, s.F, s.desc.avg_frames, s.cnt.p, s.row_ptr.p, s.ev_frame.p, s.ev_val.p, s.row_len.p,
-      s.pclass.p, s.wlist.p, s.flist.p, s.pixels_sum.p, s.stats.p);
+      P, s.F, s.desc.avg_frames, s.cnt.p, s.row_ptr.p, s.d_mask.p, s.ev_frame.p, s.ev_val.p,
+      s.row_len.p, s.pclass.p, s.wlist.p, s.flist.p, s.pixels_sum.p, s.stats.p);
   XG_CHECK_LAUNCH();
 }
 
@@ -540,15 +609,12 @@ __global__ void k_classify_rows(int32_t P, int32_t F, const int64_t *__restrict_
                                 int32_t *__restrict__ row_len, uint8_t *__restrict__ pclass,
                                 int32_t *__restrict__ wlist, int32_t *__restrict__ flist,
                                 DevStats *__restrict__ stats) {
-  int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  const int64_t b = row_ptr[p];
-  const int32_t n = (int32_t)(row_ptr[p + 1] - b);
-  row_len[p] = n;
-  if (n == 0) {
-    pclass[p] = PCLASS_EMPTY;
-    return;
-  }
+  const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p - (int32_t)(threadIdx.x & 31) >= P) return;  // whole warp past the end
+  const bool has = p < P;
+  const int64_t b = has ? row_ptr[p] : 0;
+  const int32_t n = has ? (int32_t)(row_ptr[p + 1] - b) : 0;
+  if (has) row_len[p] = n;
   bool ok = n <= MT_WARP_CAP;
   long long total = 0;
   int32_t prev = -1;
@@ -559,7 +625,8 @@ __global__ void k_classify_rows(int32_t P, int32_t F, const int64_t *__restrict_
     if (ok) total += llabs((long long)x);
     prev = f;
   }
-  record_class(p, pixel_class(n, ok, total, F), n, pclass, wlist, flist, stats);
+  const uint8_t c = n == 0 ? (uint8_t)PCLASS_EMPTY : pixel_class(n, ok, total, F);
+  record_class_warp(has, p, c, n, pclass, wlist, flist, stats);
 }
 
 }  // namespace

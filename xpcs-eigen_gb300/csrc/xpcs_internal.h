@@ -178,6 +178,7 @@ struct Series {
   std::vector<int64_t> frame_off{0};  // host copy, [raw_frames+1]
   std::vector<int32_t> frame_map;     // per raw frame: its filter frame, -1 if not used
   DBuf<int32_t> d_frame_map;
+  DBuf<int32_t> d_chunk_frame;  // raw frame of every 512th raw event
   DBuf<int32_t> raw_idx;
   DBuf<int16_t> raw_val;    // sparse series: raw int16 values
   DBuf<float> raw_valf;     // dense series: filtered float values
