@@ -23,7 +23,9 @@
 //   * G2 needs the compacted rows: per level the row is compacted in place
 //     (the same buffer the reference keeps, stale tail included) and the
 //     pairs whose bin distance lies in the level's delay window are scanned
-//     with a second pointer.  In REFERENCE mode a pair counts only when
+//     with a second pointer, in one flat loop per level (one visit per
+//     iteration) so that the lanes of a warp do not wait on each other's
+//     inner loops.  In REFERENCE mode a pair counts only when
 //     lower_bound over the whole buffer lands on the partner; that always
 //     holds while the buffer is globally sorted, which is tracked per level
 //     from the junction between the new prefix and the stale tail.
@@ -220,34 +222,45 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
     const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
     for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
     const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
-    // two pointers: jlo = first partner at distance >= tlo (monotone in i);
-    // the word at jlo and the next word of the scan are held in registers
-    int jlo = 1;
-    uint32_t wlo = m > 1 ? row[32] : 0u;
-    uint32_t wi = m > 0 ? row[0] : 0u;
-    for (int i = 0; i < m; i++) {
-      const int ti = pk_t(wi), vi = pk_v(wi);
-      const uint32_t wi_next = i + 1 < m ? row[(i + 1) * 32] : 0u;
-      if (jlo <= i) {
-        jlo = i + 1;
-        wlo = wi_next;
-      }
-      while (jlo < m && pk_t(wlo) - ti < tlo) {
-        jlo++;
-        wlo = jlo < m ? row[jlo * 32] : 0u;
-      }
-      int j = jlo;
-      uint32_t wj = wlo;
-      while (j < m) {
+    if (sorted) {
+      // one flat loop, one visit per iteration, so that the lanes of a warp
+      // stay together however their pairs are spread: either the partner
+      // pointer j takes the next word (a pair when its distance is in
+      // [tlo, thi]; closer words can pair with no later source, so jlo moves
+      // past them) or the source i moves on and j restarts at jlo.
+      int i = 0, j = 1, jlo = 1;
+      uint32_t wi = m > 0 ? row[0] : 0u;
+      uint32_t wj = m > 1 ? row[32] : 0u;
+      while (i < m - 1) {
+        const int ti = pk_t(wi);
         const int d = pk_t(wj) - ti;
-        if (d > thi) break;
-        const uint32_t wn = j + 1 < m ? row[(j + 1) * 32] : 0u;
-        if (sorted || lower_bound_packed(row, n0, pk_t(wj)) == j)
-          acc[(d - tlo) * 32] += vi * pk_v(wj);
-        j++;
-        wj = wn;
+        if (j < m && d <= thi) {
+          if (d >= tlo)
+            acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
+          else
+            jlo = j + 1;
+          j++;
+        } else {
+          i++;
+          wi = row[i * 32];
+          j = max(jlo, i + 1);
+        }
+        wj = j < m ? row[j * 32] : 0u;
       }
-      wi = wi_next;
+    } else {
+      // the buffer is not globally sorted: a pair counts only when the
+      // reference's lower_bound over the whole buffer lands on the partner
+      for (int i = 0; i < m; i++) {
+        const uint32_t wi = row[i * 32];
+        const int ti = pk_t(wi);
+        for (int j = i + 1; j < m; j++) {
+          const uint32_t wj = row[j * 32];
+          const int d = pk_t(wj) - ti;
+          if (d > thi) break;
+          if (d >= tlo && lower_bound_packed(row, n0, pk_t(wj)) == j)
+            acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
+        }
+      }
     }
     if (p < P) {
       for (int k = 0; k < L.count; k++) {
