@@ -287,9 +287,12 @@ def run_gpu_arm(args, dist):
     gbs = {k: b / (ms * 1e-3) / 1e9 if ms > 0 else None for k, (b, ms) in cand.items()}
     achieved = gbs[top]
     traffic = None
-    tp = ROOT / "profiles" / "traffic.json"
-    if tp.exists():
-        traffic = json.loads(tp.read_text()).get(top)
+    tp = ROOT / "profiles" / "traffic.txt"  # ncu DRAM bytes per launch at the 1024x1024 series
+    if tp.exists() and (acq.width, acq.height, F) == (1024, 1024, 10000):
+        for ln in tp.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) == 2 and not ln.startswith("#") and parts[0] == top:
+                traffic = int(parts[1])
 
     h2d = int(idx.nbytes + val.nbytes + 8 * (F + 1))
     d2h = int(sum(a.nbytes for a in out if a is not None))
@@ -306,8 +309,8 @@ def run_gpu_arm(args, dist):
                    "frames": F, "delays": D,
                    "qbins": Q, "raw_events": int(info.raw_events), "events": int(info.events),
                    "float_path_pixels": int(info.float_path_pixels), "mode": "reference",
-                   "l2": "no flush: every step reads and writes > 1 GB (inputs 313 MB, "
-                         "outputs 1.1 GB), far above the 126 MB L2",
+                   "l2": f"no flush: every step reads {idx.nbytes + val.nbytes >> 20} MB of raw "
+                         f"events and writes {12 * D * P >> 20} MB of G2/IP/IF, above the 126 MB L2",
                    "parallelism": f"replicas x{world}"},
         "pixel_frames_per_s": value * P,
         "stages_ms": med,
