@@ -219,6 +219,86 @@ def algorithmic_bytes(P, D, Q, npix, raw_events, events):
     return ka, kc, kd
 
 
+BATCH_DESC = ("64 independent sparse series: square detector side log-uniform [256, 1024], "
+              "frames log-uniform [500, 20000], mean photons/pixel/frame log-uniform "
+              "[0.1 %, 5 %], tau_c log-uniform [2, 2000] per ring, 4 or 8 delays per level, "
+              "9-36 dynamic rings (2 static per dynamic), seed 2026")
+
+
+def batch_mix(n=64, seed=2026):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        side = int(np.exp(rng.uniform(np.log(256), np.log(1024))))
+        frames = int(np.exp(rng.uniform(np.log(500), np.log(20000))))
+        mean = float(np.exp(rng.uniform(np.log(0.001), np.log(0.05))))
+        dpl = int(rng.choice([4, 8]))
+        q = int(rng.integers(9, 37))
+        out.append(xs.Acquisition(width=side, height=side, frames=frames, n_static=2 * q,
+                                  n_dynamic=q, mean=mean, tau_min=2.0, tau_max=2000.0,
+                                  seed=seed + 1 + i, dpl=dpl))
+    return out
+
+
+def run_batch(args, dev):
+    """Batched vs plain per-series throughput on the 64-series mix: the same
+    series, resident in HBM, run one after another through the per-series
+    calls (xpcs_multitau + xpcs_normalize, each waited for) and as one batch
+    graph (xpcs_batch_run).  Every series is autotuned first (xpcs_autotune),
+    and both forms run once untimed to size their buffers."""
+    import xpcs_gpu as xg
+
+    mix = batch_mix(args.batch_series)
+    series, events = [], 0
+    for acq in mix:
+        dq, sq, _, _ = xs.maps(acq)
+        d = xs.DeviceFrames(acq)
+        s = xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, device=dev)
+        s.ingest_sparse_device(d.nnz, d.idx, d.val)
+        s.synchronize()
+        d.close()
+        events += d.events
+        series.append(s)
+    outs = [(np.empty((s.D, s.nq)), np.empty((s.D, s.nq)), None, None) for s in series]
+    caps = [s.autotune(xg.MODE_REFERENCE) for s in series]  # both forms use the tuned kernels
+
+    def plain():
+        for s, o in zip(series, outs):
+            s.multitau(xg.MODE_REFERENCE)
+            s.normalize(out=o)
+
+    plain()
+    t0 = time.perf_counter()
+    for _ in range(args.batch_reps):
+        plain()
+    t_plain = (time.perf_counter() - t0) / args.batch_reps
+    b = xg.Batch(series)
+    b.run(xg.MODE_REFERENCE, f64=True, autotune=True)  # tunes the chain count, captures
+    t0 = time.perf_counter()
+    dev_ms = []
+    for _ in range(args.batch_reps):
+        b.run(xg.MODE_REFERENCE, f64=True, autotune=True)
+        dev_ms.append(b.stats()[0])
+    t_batch = (time.perf_counter() - t0) / args.batch_reps
+    _, kernels, lanes = b.stats()
+    # the batch's results are those of the plain run
+    same = all(np.array_equal(s.normalized(f64=True)[0], o[0], equal_nan=True)
+               for s, o in zip(series, outs))
+    b.close()
+    for s in series:
+        s.close()
+    n = len(mix)
+    return {"workload": BATCH_DESC, "series": n, "raw_events": int(events),
+            "pixel_frames": int(sum(a.width * a.height * a.frames for a in mix)),
+            "plain_ms": t_plain * 1e3, "batched_ms": t_batch * 1e3,
+            "batched_device_ms": statistics.median(dev_ms),
+            "plain_series_per_s": n / t_plain, "batched_series_per_s": n / t_batch,
+            "batched_over_plain": t_plain / t_batch, "kernels_in_graph": int(kernels),
+            "concurrent_chains": int(lanes),
+            "thread_caps": {str(c): caps.count(c) for c in sorted(set(caps))},
+            "identical_results": bool(same), "reps": args.batch_reps}
+
+
 def run_gpu_arm(args, dist):
     import xpcs_gpu as xg
 
@@ -325,6 +405,8 @@ def run_gpu_arm(args, dist):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    if not args.no_batch:
+        result["batch"] = run_batch(args, dev)
     if dist.rank == 0 and world == 1 and not args.no_cpu_baseline:
         frames = args.cpu_sample_frames
         t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
@@ -347,6 +429,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-frames", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-series batch measure")
+    ap.add_argument("--batch-series", type=int, default=64)
+    ap.add_argument("--batch-reps", type=int, default=3)
     ap.add_argument("--width", type=int, default=None,
                     help="square detector side (reduced case for profiling; default 1024)")
     ap.add_argument("--frames", type=int, default=None,

@@ -183,6 +183,21 @@ int xpcs_normalize(xpcs_series *s, double *g2, double *stderr_, float *g2_f32,
 int xpcs_side_stats(xpcs_series *s, float *pixel_sum, float *frame_sum,
                     float *partition_mean_total, float *partition_mean_partial);
 
+/* The results of the handle's last normalisation (xpcs_normalize or a batch
+ * run), without computing again: [D][Q] each, any pointer may be NULL.  A
+ * float64 / float32 output that the last normalisation did not compute is
+ * an XPCS_ERR_STATE. */
+int xpcs_get_normalized(xpcs_series *s, double *g2, double *stderr_, float *g2_f32,
+                        float *stderr_f32);
+
+/* Autotuner (no reference counterpart).  Times the filter and multi-tau
+ * passes of the ingested frames with each row capacity of the
+ * thread-per-pixel kernel (32, 48, 64, 80, 112 events; longer rows go to the
+ * warp-per-pixel kernel) and keeps the fastest for this series.  Results do
+ * not depend on the choice; only the time does.  The default without tuning
+ * is 80.  *thread_cap (may be NULL) receives the choice. */
+int xpcs_autotune(xpcs_series *s, int32_t mode, int32_t *thread_cap);
+
 /* Waits for the handle's stream; reports deferred device errors. */
 int xpcs_synchronize(xpcs_series *s);
 
@@ -230,6 +245,36 @@ int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *frame, const f
                            int32_t pixels, int64_t events, int32_t frames,
                            int32_t delays_per_level, int32_t mode, float *G2, float *IP,
                            float *IF, void *stream);
+
+/* Batches: no counterpart in the reference, which runs one series per
+ * process.  A batch holds several series handles of one device (uneven frame
+ * counts, detector sizes and occupancies) and runs the whole path for all of
+ * them -- filter/transpose, multi-tau and normalisation -- as one CUDA graph in
+ * which the series' kernels are independent branches, so that small series
+ * fill the GPU together instead of one after another (the series are dealt,
+ * largest first, onto a number of concurrent chains; XPCS_BATCH_AUTOTUNE
+ * times the candidate chain counts on the first run).  The graph is captured
+ * on the first run and replayed until a member's frames, the mode or the flags
+ * change (then it is captured again).  The work of each series is the same as
+ * xpcs_multitau + xpcs_normalize on its own, so results are bit-identical to
+ * running the series alone.  Member handles must outlive the batch and must
+ * not be used by other threads while xpcs_batch_run runs.
+ *  flags: XPCS_BATCH_F64 (float64 normalisation), XPCS_BATCH_F32 (float32
+ *  normalisation in the reference's operation order), XPCS_BATCH_AUTOTUNE
+ *  (tune each member's kernel choice first); read the results with
+ *  xpcs_get_g2ipif / xpcs_get_normalized on each member. */
+typedef struct xpcs_batch xpcs_batch;
+#define XPCS_BATCH_F64 1u
+#define XPCS_BATCH_F32 2u
+#define XPCS_BATCH_AUTOTUNE 4u /* run xpcs_autotune on members not yet tuned before capture */
+int xpcs_batch_create(xpcs_series *const *series, int32_t count, xpcs_batch **out);
+/* Runs the batch and waits for it. */
+int xpcs_batch_run(xpcs_batch *b, int32_t mode, uint32_t flags);
+/* Device time of the last run (graph launch to completion, CUDA events), the
+ * number of kernels in the graph and the number of concurrent chains of
+ * series in it (any pointer may be NULL). */
+int xpcs_batch_stats(xpcs_batch *b, float *ms, int64_t *kernels, int32_t *lanes);
+void xpcs_batch_destroy(xpcs_batch *b);
 
 #ifdef __cplusplus
 }

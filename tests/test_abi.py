@@ -100,3 +100,12 @@ def test_no_device_reported_cleanly():
         xg.Series(W, H, 64, 4, dq, sq)
     assert e.value.code == 7
     assert "CUDA" in xg.lib().xpcs_last_error().decode()
+
+
+def test_batch_rejects_bad_arguments():
+    import ctypes as C
+    h = C.c_void_p()
+    rc = xg.lib().xpcs_batch_create(None, 0, C.byref(h))
+    assert rc == 1 and h.value is None
+    assert xg.lib().xpcs_batch_run(None, 0, 1) == 1
+    xg.lib().xpcs_batch_destroy(None)

@@ -255,3 +255,24 @@ def test_side_statistics_bit_exact_vs_reference(case):
     assert same_bits_nan(fs, fx["ref_frameSum"])
     assert same_bits_nan(tot, fx["ref_partition_mean_total"])
     assert same_bits_nan(part, fx["ref_partition_mean_partial"])
+
+
+@pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
+def test_long_rows_take_the_integer_path_and_match_the_oracle(mode):
+    """Rows of 300-2000 events (beyond the 256-event warp rows) are integer
+    rows with sum |v| < 4096: the long-row warp kernel, not the float replay."""
+    acq = xs.Acquisition(width=40, height=36, frames=20000, n_static=12, n_dynamic=6, mean=0.06,
+                         tau_min=3, tau_max=3000, seed=77, dpl=8)
+    dq, sq, _, _ = xs.maps(acq)
+    nnz, idx, val = xs.sparse_frames(acq)
+    with xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+        info = s.info()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, acq.frames)
+    lens = np.diff(rows.row_ptr)
+    assert lens.max() > 256 and info.float_path_pixels == 0
+    oG2, oIP, oIF = oracle.multitau2(rows, acq.frames, acq.dpl, mode)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)

@@ -2,6 +2,7 @@
 
   libxpcs_gpu.so    CUDA kernels + C ABI (include/xpcs_gpu.h), sm_103a only
   libxpcs_synth.so  seeded synthetic acquisitions (benchmark/test inputs)
+  libxpcs_synth_gpu.so  the same sparse frames drawn on the GPU (large benchmark inputs)
   corr              C++ command-line driver with the reference's flags
 
 Everything is compiled in-tree into xpcs-eigen_gb300/_build/.  Translation
@@ -29,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-I", str(INCLUDE), "-I", str(CSRC)]
 GPU_SOURCES = ["abi.cu", "scan.cu", "k_transpose.cu", "k_multitau.cu", "k_normalize.cu",
-               "qmap.cpp", "noalloc.cu", "k_dense.cu", "k_side.cu"]
+               "qmap.cpp", "noalloc.cu", "k_dense.cu", "k_side.cu", "batch.cu"]
 
 LIB_GPU = BUILD / "libxpcs_gpu.so"
 LIB_SYNTH = BUILD / "libxpcs_synth.so"
@@ -85,6 +86,20 @@ def build_synth(force: bool = False) -> Path:
     return LIB_SYNTH
 
 
+LIB_SYNTH_GPU = BUILD / "libxpcs_synth_gpu.so"
+
+
+def build_synth_gpu(force: bool = False) -> Path:
+    """The GPU draw of the synthetic sparse frames (benchmark inputs)."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    src = PKG / "synth" / "xpcs_synth_gpu.cu"
+    if force or _stale(LIB_SYNTH_GPU, [src, PKG / "synth" / "xpcs_synth.h"]):
+        _run([NVCC] + ARCH + ["-O3", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+                              "-shared", "-I", str(PKG / "synth"), "-o", str(LIB_SYNTH_GPU),
+                              str(src)])
+    return LIB_SYNTH_GPU
+
+
 def build_corr(force: bool = False) -> Path:
     """The C++ `corr` driver, linked against libxpcs_gpu.so (rpath $ORIGIN)."""
     srcs = [HOST / "corr_main.cpp", HOST / "xh5c.cpp", HOST / "imm.cpp"]
@@ -97,8 +112,9 @@ def build_corr(force: bool = False) -> Path:
 
 
 def build_all(force: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        futs = [ex.submit(build_gpu, force), ex.submit(build_synth, force)]
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_gpu, force), ex.submit(build_synth, force),
+                ex.submit(build_synth_gpu, force)]
         for f in futs:
             f.result()
     build_corr(force)

@@ -84,7 +84,8 @@ void free_series(Series *s) {
     cudaStream_t st = s->stream;
     cudaStreamSynchronize(st);
     DBuf<int32_t> *i32[] = {&s->raw_idx, &s->frA, &s->frB, &s->cnt, &s->row_len,
-                            &s->flist, &s->wlist, &s->ev_frame, &s->sc_frame, &s->n_q_entry_ptr,
+                            &s->flist, &s->wlist, &s->llist, &s->ev_frame, &s->sc_frame,
+                            &s->n_q_entry_ptr,
                             &s->n_entry_sbin, &s->n_entry_pix_ptr, &s->n_pix, &s->n_q_row,
                             &s->n_ch_k0, &s->n_ch_k1, &s->n_e_chunk_ptr, &s->d_sbin,
                             &s->d_ppb};
@@ -220,8 +221,10 @@ int xpcs_series_reset(xpcs_series *h) {
     s.raw_frames = 0;
     s.frame_off_dirty = true;
     s.have_multitau = false;
+    s.have_norm64 = s.have_norm32 = false;
     s.timed_h2d = false;
     s.h2d_ms_acc = 0.f;
+    s.generation++;
   });
 }
 
@@ -277,6 +280,7 @@ static void ingest_common(Series &s, const int32_t *idx, const int16_t *val, con
   s.raw_frames += nframes;
   s.frame_off_dirty = true;
   s.have_multitau = false;
+  s.generation++;
 }
 
 int xpcs_ingest_sparse(xpcs_series *h, const int32_t *idx, const int16_t *val,
@@ -306,6 +310,7 @@ int xpcs_set_dark(xpcs_series *h, const int16_t *dark, int32_t ndark) {
     need(ndark >= 0 && (ndark == 0 || dark), "bad dark frames");
     DeviceGuard g(s.device);
     dense_set_dark(s, dark, ndark);
+    s.generation++;
   });
 }
 
@@ -321,6 +326,8 @@ static int ingest_dense_common(xpcs_series *h, const int16_t *frames, int32_t nf
       s.timed_h2d = true;
     }
     dense_ingest(s, frames, nframes, dev);
+    s.generation++;
+    s.have_multitau = false;
     XG_CUDA(cudaEventRecord(s.ev[1], s.stream));
   });
 }
@@ -355,6 +362,7 @@ int xpcs_multitau(xpcs_series *h, int32_t mode) {
     run_multitau(s, mode);
     s.launches = (int32_t)(tl_launches - l0);
     s.have_multitau = true;
+    s.have_norm64 = s.have_norm32 = false;
     s.timed_h2d = false;
   });
 }
@@ -386,6 +394,8 @@ int xpcs_normalize(xpcs_series *h, double *g2, double *se, float *g2f, float *se
     const int64_t l0 = tl_launches;
     XG_CUDA(cudaEventRecord(s.ev[7], st));
     run_normalize(s, w64, w32);
+    s.have_norm64 = w64;
+    s.have_norm32 = w32;
     s.launches += (int32_t)(tl_launches - l0);
     XG_CUDA(cudaEventRecord(s.ev[8], st));
     const size_t n = (size_t)s.D * s.qmap.nq();
@@ -400,6 +410,27 @@ int xpcs_normalize(xpcs_series *h, double *g2, double *se, float *g2f, float *se
   });
 }
 
+int xpcs_get_normalized(xpcs_series *h, double *g2, double *se, float *g2f, float *sef) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if ((g2 || se) && !s.have_norm64)
+      throw Error(XPCS_ERR_STATE, "no float64 normalisation has run since the last change");
+    if ((g2f || sef) && !s.have_norm32)
+      throw Error(XPCS_ERR_STATE, "no float32 normalisation has run since the last change");
+    DeviceGuard g(s.device);
+    cudaStream_t st = s.stream;
+    const size_t n = (size_t)s.D * s.qmap.nq();
+    if (n) {
+      if (g2) XG_CUDA(cudaMemcpyAsync(g2, s.n_g2.p, 8 * n, cudaMemcpyDeviceToHost, st));
+      if (se) XG_CUDA(cudaMemcpyAsync(se, s.n_se.p, 8 * n, cudaMemcpyDeviceToHost, st));
+      if (g2f) XG_CUDA(cudaMemcpyAsync(g2f, s.n_g2f.p, 4 * n, cudaMemcpyDeviceToHost, st));
+      if (sef) XG_CUDA(cudaMemcpyAsync(sef, s.n_sef.p, 4 * n, cudaMemcpyDeviceToHost, st));
+    }
+    sync_and_check(s);
+  });
+}
+
 int xpcs_side_stats(xpcs_series *h, float *pixel_sum, float *frame_sum,
                     float *partition_mean_total, float *partition_mean_partial) {
   return guarded([&] {
@@ -410,6 +441,56 @@ int xpcs_side_stats(xpcs_series *h, float *pixel_sum, float *frame_sum,
     sync_and_check(s);
     run_side_stats(s, SideOut{pixel_sum, frame_sum, partition_mean_total, partition_mean_partial});
   });
+}
+
+int xpcs_autotune(xpcs_series *h, int32_t mode, int32_t *thread_cap) {
+  return guarded([&] {
+    need(h, "null handle");
+    need(mode == XPCS_MODE_REFERENCE || mode == XPCS_MODE_EXACT, "unknown mode");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    const int32_t c = autotune(s, mode);
+    if (thread_cap) *thread_cap = c;
+  });
+}
+
+int xpcs_batch_create(xpcs_series *const *series, int32_t count, xpcs_batch **out) {
+  return guarded([&] {
+    need(series && out && count > 0, "bad batch arguments");
+    *out = nullptr;
+    DeviceGuard g(((Series *)series[0])->device);
+    *out = (xpcs_batch *)batch_create((Series *const *)series, count);
+  });
+}
+
+int xpcs_batch_run(xpcs_batch *h, int32_t mode, uint32_t flags) {
+  return guarded([&] {
+    need(h, "null batch");
+    need(mode == XPCS_MODE_REFERENCE || mode == XPCS_MODE_EXACT, "unknown mode");
+    need((flags & ~(XPCS_BATCH_F64 | XPCS_BATCH_F32 | XPCS_BATCH_AUTOTUNE)) == 0,
+         "unknown batch flags");
+    Batch &b = *(Batch *)h;
+    DeviceGuard g(b.device);
+    batch_run(b, mode, flags);
+  });
+}
+
+int xpcs_batch_stats(xpcs_batch *h, float *ms, int64_t *kernels, int32_t *lanes) {
+  return guarded([&] {
+    need(h, "null batch");
+    Batch &b = *(Batch *)h;
+    if (ms) *ms = b.last_ms;
+    if (kernels) *kernels = b.kernels;
+    if (lanes) *lanes = b.lanes;
+  });
+}
+
+void xpcs_batch_destroy(xpcs_batch *h) {
+  if (!h) return;
+  Batch *b = (Batch *)h;
+  DeviceGuard g(b->device);
+  cudaStreamSynchronize(b->origin);
+  delete b;
 }
 
 int xpcs_synchronize(xpcs_series *h) {

@@ -1,0 +1,230 @@
+// Batches of series run as one CUDA graph.
+//
+// The reference processes one series per `corr` process (main.cpp:86-479).
+// A batch runs the path of several series -- filter/transpose (K-a),
+// multi-tau (K-c) and normalisation (K-d) -- as one graph in which every
+// series is an independent branch: the kernels of small series run side by
+// side instead of one after another, and the whole batch costs one launch
+// from the host.  The graph is captured from the series' own streams (fork
+// from the batch's origin stream, join back), after one eager pass that
+// sizes every buffer and uploads every per-series table, so that the
+// captured work is kernels and device-side copies only.  It is replayed
+// until a member's frames (its generation counter), the mode or the flags
+// change.
+//
+// Schedule: the series are dealt, largest first, onto `lanes` chains (each
+// chain runs its series one after another; the chains run side by side), so
+// that a few large series do not all compete for the GPU at once while the
+// small ones fill the gaps.  With XPCS_BATCH_AUTOTUNE the lane count is chosen
+// by timing the candidates on the first run.
+#include <algorithm>
+#include <numeric>
+
+#include "xpcs_internal.h"
+
+namespace xg {
+
+Batch::~Batch() {
+  if (exec) cudaGraphExecDestroy(exec);
+  for (cudaEvent_t e : join)
+    if (e) cudaEventDestroy(e);
+  if (fork) cudaEventDestroy(fork);
+  if (t0) cudaEventDestroy(t0);
+  if (t1) cudaEventDestroy(t1);
+  if (origin) cudaStreamDestroy(origin);
+}
+
+Batch *batch_create(Series *const *ss, int32_t n) {
+  if (n <= 0) throw Error(XPCS_ERR_INVALID_ARGUMENT, "empty batch");
+  for (int32_t i = 0; i < n; i++) {
+    if (!ss[i]) throw Error(XPCS_ERR_INVALID_ARGUMENT, "null series in batch");
+    if (ss[i]->device != ss[0]->device)
+      throw Error(XPCS_ERR_INVALID_ARGUMENT, "batch members must use one device");
+    for (int32_t j = 0; j < i; j++)
+      if (ss[j] == ss[i]) throw Error(XPCS_ERR_INVALID_ARGUMENT, "series twice in one batch");
+  }
+  Batch *b = new Batch();
+  try {
+    b->ss.assign(ss, ss + n);
+    b->device = ss[0]->device;
+    XG_CUDA(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+    XG_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    XG_CUDA(cudaEventCreate(&b->t0));
+    XG_CUDA(cudaEventCreate(&b->t1));
+    b->join.assign(n, nullptr);
+    for (auto &e : b->join) XG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  } catch (...) {
+    delete b;
+    throw;
+  }
+  return b;
+}
+
+// Times filter + multi-tau of the series' frames with every thread-kernel row
+// capacity (after one untimed pass that sizes the buffers) and keeps the
+// fastest.  A change of capacity changes the pixel classification, so it
+// counts as a change of the series for captured batch graphs.
+int32_t autotune(Series &s, int mode) {
+  cudaStream_t st = s.stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  XG_CUDA(cudaEventCreate(&e0));
+  XG_CUDA(cudaEventCreate(&e1));
+  const int32_t before = s.thread_cap;
+  int32_t best = before;
+  float best_ms = 0.f;
+  try {
+    run_filter_transpose(s);
+    run_multitau(s, mode);
+    for (int k = 0; k < MT_THREAD_NCAPS; k++) {
+      s.thread_cap = MT_THREAD_CAPS[k];
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; rep++) {  // the second pass is timed
+        XG_CUDA(cudaEventRecord(e0, st));
+        run_filter_transpose(s);
+        run_multitau(s, mode);
+        XG_CUDA(cudaEventRecord(e1, st));
+        XG_CUDA(cudaEventSynchronize(e1));
+        XG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      }
+      if (k == 0 || ms < best_ms) {
+        best_ms = ms;
+        best = s.thread_cap;
+      }
+    }
+  } catch (...) {
+    s.thread_cap = before;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s.thread_cap = best;
+  s.tuned = true;
+  s.have_multitau = false;
+  s.have_norm64 = s.have_norm32 = false;
+  s.generation++;
+  return best;
+}
+
+namespace {
+
+void series_pass(Series &s, int mode, uint32_t flags) {
+  run_filter_transpose(s);
+  run_multitau(s, mode);
+  run_normalize(s, (flags & XPCS_BATCH_F64) != 0, (flags & XPCS_BATCH_F32) != 0);
+}
+
+bool stale(const Batch &b, int mode, uint32_t flags) {
+  if (!b.exec || b.mode != mode || b.flags != flags || b.gens.size() != b.ss.size()) return true;
+  for (size_t i = 0; i < b.ss.size(); i++) {
+    if (b.ss[i]->generation != b.gens[i]) return true;
+    if ((flags & XPCS_BATCH_AUTOTUNE) && !b.ss[i]->tuned) return true;
+  }
+  return false;
+}
+
+void build_graph(Batch &b, int mode, uint32_t flags, int lanes) {
+  if (b.exec) {
+    cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+  }
+  const int n = (int)b.ss.size();
+  if (lanes <= 0 || lanes > n) lanes = n;
+  // largest first, each onto the least loaded chain
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return b.ss[x]->raw_events > b.ss[y]->raw_events;
+  });
+  std::vector<int64_t> load(lanes, 0);
+  std::vector<int> last(lanes, -1);  // last series of each chain
+  XG_CUDA(cudaStreamBeginCapture(b.origin, cudaStreamCaptureModeRelaxed));
+  cudaGraph_t g = nullptr;
+  const int64_t l0 = tl_launches;
+  try {
+    XG_CUDA(cudaEventRecord(b.fork, b.origin));
+    for (int i : order) {
+      const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      Series &s = *b.ss[i];
+      XG_CUDA(cudaStreamWaitEvent(s.stream, last[c] < 0 ? b.fork : b.join[last[c]], 0));
+      series_pass(s, mode, flags);
+      XG_CUDA(cudaEventRecord(b.join[i], s.stream));
+      load[c] += s.raw_events + s.P;
+      last[c] = i;
+    }
+    for (int c = 0; c < lanes; c++)
+      if (last[c] >= 0) XG_CUDA(cudaStreamWaitEvent(b.origin, b.join[last[c]], 0));
+  } catch (...) {
+    cudaStreamEndCapture(b.origin, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    throw;
+  }
+  XG_CUDA(cudaStreamEndCapture(b.origin, &g));
+  b.kernels = tl_launches - l0;
+  const cudaError_t e = cudaGraphInstantiate(&b.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b.exec = nullptr;
+    throw Error(XPCS_ERR_CUDA, cudaGetErrorString(e));
+  }
+  b.lanes = lanes;
+}
+
+float launch(Batch &b) {
+  XG_CUDA(cudaEventRecord(b.t0, b.origin));
+  XG_CUDA(cudaGraphLaunch(b.exec, b.origin));
+  XG_CUDA(cudaEventRecord(b.t1, b.origin));
+  XG_CUDA(cudaStreamSynchronize(b.origin));
+  float ms = 0.f;
+  XG_CUDA(cudaEventElapsedTime(&ms, b.t0, b.t1));
+  return ms;
+}
+
+void capture(Batch &b, int mode, uint32_t flags) {
+  if (flags & XPCS_BATCH_AUTOTUNE)
+    for (Series *s : b.ss)
+      if (!s->tuned) autotune(*s, mode);
+  // eager pass: buffers reach their sizes, frame tables and plans are uploaded
+  for (Series *s : b.ss) series_pass(*s, mode, flags);
+  for (Series *s : b.ss) XG_CUDA(cudaStreamSynchronize(s->stream));
+  const int n = (int)b.ss.size();
+  if ((flags & XPCS_BATCH_AUTOTUNE) && !b.lanes_tuned) {
+    int best = n;
+    float best_ms = 0.f;
+    bool first = true;
+    for (int lanes : {1, 2, 4, 8, 16, n}) {
+      if (lanes > n) continue;
+      build_graph(b, mode, flags, lanes);
+      launch(b);
+      const float ms = launch(b);
+      if (first || ms < best_ms) {
+        best_ms = ms;
+        best = lanes;
+        first = false;
+      }
+    }
+    b.lanes = best;
+    b.lanes_tuned = true;
+  }
+  build_graph(b, mode, flags, b.lanes);
+  b.mode = mode;
+  b.flags = flags;
+  b.gens.resize(b.ss.size());
+  for (size_t i = 0; i < b.ss.size(); i++) b.gens[i] = b.ss[i]->generation;
+}
+
+}  // namespace
+
+void batch_run(Batch &b, int mode, uint32_t flags) {
+  if (stale(b, mode, flags)) capture(b, mode, flags);
+  b.last_ms = launch(b);
+  for (Series *s : b.ss) {
+    s->have_multitau = true;
+    s->have_norm64 = (flags & XPCS_BATCH_F64) != 0;
+    s->have_norm32 = (flags & XPCS_BATCH_F32) != 0;
+  }
+}
+
+}  // namespace xg

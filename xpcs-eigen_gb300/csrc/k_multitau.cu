@@ -34,7 +34,9 @@
 //   written straight to [D][P] (32 consecutive pixels per warp = coalesced).
 //   Pixels of other classes get zeros here and are rewritten by the kernels
 //   below.
-// k_mt_warp:   one warp per pixel for rows of up to 256 events.
+// k_mt_warp:   one warp per pixel, rows packed in shared memory: rows of up
+//   to 256 events (8 warps per block), up to 1024 (4 warps per block) and up
+//   to 4096 (2 warps per block).
 // k_mt_float:  one thread per pixel replaying the reference's float
 //   operations in its order (no fused multiply-add) on a scratch copy.
 #include <algorithm>
@@ -48,6 +50,9 @@ namespace {
 
 constexpr int MT_WARPS = 2;  // warps per block of the thread-per-pixel kernel
 constexpr int WP_WARPS = 8;  // warps per block of the warp-per-pixel kernel
+constexpr int MT_MID_CAP = 1024;  // long rows up to this length: 4 warps per block
+constexpr int MID_WARPS = 4;
+constexpr int LONG_WARPS = 2;  // warps per block for rows of up to MT_LONG_CAP events
 
 // std::lower_bound as libstdc++ implements it (halving the remaining length).
 __device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t x) {
@@ -101,6 +106,7 @@ __device__ __forceinline__ void copy_plan(uint8_t *dst, const uint8_t *src, size
 
 // ------------------------------------------------------ thread per pixel
 
+template <int CAP>
 __global__ void __launch_bounds__(MT_WARPS * 32)
 k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
             const int32_t *__restrict__ row_len, const uint8_t *__restrict__ pclass,
@@ -116,9 +122,9 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
   const int P = pl->P, nlev = pl->nlev, mode = pl->mode;
   const int scr = max(pl->acc, nlev);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *wbase = (uint32_t *)(smem + pb) + (size_t)warp * (MT_THREAD_CAP + scr) * 32;
+  uint32_t *wbase = (uint32_t *)(smem + pb) + (size_t)warp * (CAP + scr) * 32;
   uint32_t *row = wbase + lane;
-  int32_t *acc = (int32_t *)(row + MT_THREAD_CAP * 32);  // scratch, also S(t_end) per level
+  int32_t *acc = (int32_t *)(row + CAP * 32);  // scratch, also S(t_end) per level
 
   const int p0 = (blockIdx.x * MT_WARPS + warp) * 32;
   if (p0 >= P) return;
@@ -273,30 +279,46 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
 
 // ------------------------------------------------------- warp per pixel
 
-// In-place compaction of the live prefix t[0..m), v[0..m) (warp-cooperative).
-// Returns the new live length; entries at and beyond it are left untouched.
-__device__ int compact_warp(int32_t *t, int32_t *v, int m, int lastframe, int lane) {
+// lower_bound over a contiguous packed row (frame in the high half)
+__device__ __forceinline__ int lower_bound_row(const uint32_t *row, int n, int32_t x) {
+  int first = 0, len = n;
+  while (len > 0) {
+    int half = len >> 1;
+    if ((int32_t)(row[first + half] >> 16) < x) {
+      first += half + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  return first;
+}
+
+// In-place compaction of the live prefix row[0, m) for the next level
+// (warp-cooperative): frame/2, equal neighbours merged, frames >= lastframe
+// dropped.  Entries at and beyond the returned length are left untouched
+// (the reference's stale tail).
+__device__ int compact_row(uint32_t *row, int m, int lastframe, int lane) {
   const unsigned FULL = 0xffffffffu, lt = (1u << lane) - 1u;
   int gbase = 0;
-  int prev = INT_MIN;  // halved index of the element before the current chunk
+  int prev = INT_MIN;  // halved frame of the entry before the current chunk
   for (int c0 = 0; c0 < m; c0 += 32) {
-    int i = c0 + lane;
-    bool in = i < m;
-    int ti = in ? (t[i] >> 1) : INT_MAX;
-    int vi = in ? v[i] : 0;
-    bool pair = (i + 1 < m) && ((t[i + 1] >> 1) == ti);
-    int vn = pair ? v[i + 1] : 0;
+    const int i = c0 + lane;
+    const bool in = i < m;
+    const uint32_t w = in ? row[i] : 0u;
+    const int ti = in ? (pk_t(w) >> 1) : INT_MAX;
+    int vi = in ? pk_v(w) : 0;
+    if (i + 1 < m) {
+      const uint32_t w2 = row[i + 1];
+      if ((pk_t(w2) >> 1) == ti) vi += pk_v(w2);  // rows hold distinct frames: pairs at most
+    }
     int tp = __shfl_up_sync(FULL, ti, 1);
     if (lane == 0) tp = prev;
-    bool head = in && ti != tp && ti < lastframe;
-    unsigned hm = __ballot_sync(FULL, head);
+    const bool head = in && ti != tp && ti < lastframe;
+    const unsigned hm = __ballot_sync(FULL, head);
     prev = __shfl_sync(FULL, ti, 31);
     __syncwarp();
-    if (head) {
-      int g = gbase + __popc(hm & lt);
-      t[g] = ti;
-      v[g] = vi + vn;
-    }
+    if (head) row[gbase + __popc(hm & lt)] = pk(ti, vi);
     gbase += __popc(hm);
     __syncwarp();
     if (prev >= lastframe) break;
@@ -304,12 +326,21 @@ __device__ int compact_warp(int32_t *t, int32_t *v, int m, int lastframe, int la
   return gbase;
 }
 
-__global__ void __launch_bounds__(WP_WARPS * 32)
-k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ wlist,
-          const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
-          const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
-          const float *__restrict__ ev_val, float *__restrict__ G2, float *__restrict__ IP,
-          float *__restrict__ IF) {
+// One warp per pixel of `list` (count at *count_p) whose row holds more than
+// min_n and at most `cap` events, packed (frame << 16 | int16 value) in the warp's shared memory, with
+// the row's inclusive prefix sums and per-lane accumulators beside it.
+//   IP / IF: from the original row, as in the thread kernel: lanes take the
+//     delays and look the thresholds up in the prefix sums.
+//   G2: per level, warp-cooperative compaction, then every lane takes the
+//     sources lane, lane+32, ... in one flat loop over (source, partner)
+//     visits into its own accumulators, summed over the warp at the end of
+//     the level.
+__global__ void __launch_bounds__(256)
+k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
+          const int32_t *__restrict__ count_p, int32_t min_n, int32_t cap,
+          const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ row_len,
+          const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
+          float *__restrict__ G2, float *__restrict__ IP, float *__restrict__ IF) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int D = ((const McPlan *)plan_g)->D;
   const size_t pb = mc_plan_bytes(D);
@@ -317,74 +348,86 @@ k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ wlist,
   __syncthreads();
   const McPlan *pl = (const McPlan *)smem;
   const McArrays ar = mc_arrays(smem, D);
-  const int P = pl->P, mode = pl->mode, ACC = pl->acc;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int32_t *t = (int32_t *)(smem + pb) + (size_t)warp * (3 * MT_WARP_CAP + ACC);
-  int32_t *v = t + MT_WARP_CAP;
-  int32_t *S = v + MT_WARP_CAP;
-  int32_t *acc = S + MT_WARP_CAP;
+  const int P = pl->P, mode = pl->mode, ACC = max(pl->acc, pl->nlev);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  uint32_t *row = (uint32_t *)(smem + pb) + (size_t)warp * (2 * cap + 32 * ACC);
+  int32_t *S = (int32_t *)(row + cap);
+  int32_t *acc = S + cap + lane;  // acc[k * 32]: this lane's accumulator k
   const unsigned FULL = 0xffffffffu;
-  const int nw = stats->nwarp;
-  for (int q = blockIdx.x * WP_WARPS + warp; q < nw; q += gridDim.x * WP_WARPS) {
-    const int p = wlist[q];
-    const int64_t b = row_ptr[p];
+  const int nw = *count_p;
+  for (int q = blockIdx.x * nwb + warp; q < nw; q += gridDim.x * nwb) {
+    const int p = list[q];
     const int n0 = row_len[p];
-    for (int i = lane; i < n0; i += 32) {
-      t[i] = ev_frame[b + i];
-      v[i] = __float2int_rn(ev_val[b + i]);
+    if (n0 <= min_n || n0 > cap) continue;  // another launch's share of the list
+    const int64_t b = row_ptr[p];
+    int carry = 0;
+    for (int c0 = 0; c0 < n0; c0 += 32) {
+      const int i = c0 + lane;
+      int x = 0;
+      if (i < n0) {
+        x = __float2int_rn(ev_val[b + i]);
+        row[i] = pk(ev_frame[b + i], x);
+      }
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+      }
+      if (i < n0) S[i] = x + carry;
+      carry += __shfl_sync(FULL, x, 31);
     }
     __syncwarp();
+    // IP(d) = S(t_ip[d]); IF(d) = S(t_end of its level) - S(tau_abs[d]); S(T) = sum of
+    // v over frames < T
+    for (int d = lane; d < D; d += 32) {
+      const int g = ar.gi[d];
+      const int lvl = pl->lv[g].level;
+      const int c_ip = lower_bound_row(row, n0, ar.t_ip[d]);
+      const int c_end = lower_bound_row(row, n0, pl->lv[g].t_end);
+      const int c_tau = lower_bound_row(row, n0, ar.tau_abs[d]);
+      const int ip = c_ip ? S[c_ip - 1] : 0;
+      const int iff = (c_end ? S[c_end - 1] : 0) - (c_tau ? S[c_tau - 1] : 0);
+      IP[(size_t)d * P + p] = scaled_quotient(ip, lvl, ar.denom[d]);
+      IF[(size_t)d * P + p] = scaled_quotient(iff, lvl, ar.denom[d]);
+    }
     int m = n0;
+    bool J = true, U = true;  // junction at m sorted; stale suffix [m, n0) sorted
     for (int gi = 0; gi < pl->nlev; gi++) {
       const McLevel L = pl->lv[gi];
-      const int lastframe = L.lastframe;
-      if (L.compact && m > 0) m = compact_warp(t, v, m, lastframe, lane);
-      bool sorted = true;
-      if (mode == XPCS_MODE_REFERENCE && m > 0) {
-        bool ok = true;
-        for (int i = lane; i + 1 < n0; i += 32) ok &= t[i] <= t[i + 1];
-        sorted = __all_sync(FULL, ok);
+      if (L.compact && m > 0) {
+        const int m2 = compact_row(row, m, L.lastframe, lane);
+        U = (m2 < m) ? (J && U) : U;
+        J = (m2 == 0 || m2 >= n0) ? true : (pk_t(row[m2 - 1]) <= pk_t(row[m2]));
+        m = m2;
       }
-      int carry = 0;
-      for (int c0 = 0; c0 < m; c0 += 32) {
-        int i = c0 + lane;
-        int x = i < m ? v[i] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          int y = __shfl_up_sync(FULL, x, o);
-          if (lane >= o) x += y;
-        }
-        if (i < m) S[i] = x + carry;
-        carry += __shfl_sync(FULL, x, 31);
-      }
-      for (int k = lane; k < L.count; k += 32) acc[k] = 0;
-      __syncwarp();
+      const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
       const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
-      for (int i = lane; i < m; i += 32) {
-        const int ti = t[i], vi = v[i];
-        for (int j = i + 1; j < m; j++) {
-          const int tj = t[j];
-          const int d = tj - ti;
-          if (d > thi) break;
-          if (d >= tlo) {
-            if (!sorted && lower_bound_i32(t, n0, tj) != j) continue;
-            atomicAdd(&acc[d - tlo], vi * v[j]);
-          }
+      for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
+      int i = lane, j = lane + 1;
+      uint32_t wi = i < m ? row[i] : 0u;
+      uint32_t wj = j < m ? row[j] : 0u;
+      while (i < m) {
+        const int d = pk_t(wj) - pk_t(wi);
+        if (j < m && d <= thi) {
+          if (d >= tlo && (sorted || lower_bound_row(row, n0, pk_t(wj)) == j))
+            acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
+          j++;
+        } else {
+          i += 32;
+          if (i >= m) break;
+          wi = row[i];
+          j = i + 1;
         }
+        wj = j < m ? row[j] : 0u;
       }
-      __syncwarp();
-      const int total = m > 0 ? S[m - 1] : 0;
-      for (int k = lane; k < L.count; k += 32) {
-        const int tau = tlo + k;
-        const int cip = m > 0 ? lower_bound_i32(t, m, lastframe - tau) : 0;
-        const int cif = m > 0 ? lower_bound_i32(t, m, tau) : 0;
-        const int ip = cip ? S[cip - 1] : 0;
-        const int iff = total - (cif ? S[cif - 1] : 0);
-        const int d = L.first + k;
-        const float den = ar.denom[d];
-        G2[(size_t)d * P + p] = scaled_quotient(acc[k], 2 * L.level, den);
-        IP[(size_t)d * P + p] = scaled_quotient(ip, L.level, den);
-        IF[(size_t)d * P + p] = scaled_quotient(iff, L.level, den);
+      int mine = 0;
+      for (int k = 0; k < L.count; k++) {
+        const int tot = __reduce_add_sync(FULL, acc[k * 32]);
+        if (lane == k) mine = tot;
+      }
+      if (lane < L.count) {
+        const int d = L.first + lane;
+        G2[(size_t)d * P + p] = scaled_quotient(mine, 2 * L.level, ar.denom[d]);
       }
       __syncwarp();
     }
@@ -529,11 +572,25 @@ std::vector<uint8_t> make_plan(const Series &s, int mode) {
   return buf;
 }
 
-size_t thread_smem(int D, int scr) {
-  return mc_plan_bytes(D) + (size_t)MT_WARPS * (MT_THREAD_CAP + scr) * 32 * sizeof(uint32_t);
+size_t thread_smem(int D, int scr, int cap) {
+  return mc_plan_bytes(D) + (size_t)MT_WARPS * (cap + scr) * 32 * sizeof(uint32_t);
 }
-size_t warp_smem(int D, int acc) {
-  return mc_plan_bytes(D) + (size_t)WP_WARPS * (3 * MT_WARP_CAP + acc) * sizeof(int32_t);
+
+using ThreadKernel = void (*)(const uint8_t *, const int64_t *, const int32_t *, const uint8_t *,
+                              const int32_t *, const float *, float *, float *, float *);
+
+ThreadKernel thread_kernel(int cap) {
+  switch (cap) {
+    case 32: return k_mt_thread<32>;
+    case 48: return k_mt_thread<48>;
+    case 64: return k_mt_thread<64>;
+    case 80: return k_mt_thread<80>;
+    case 112: return k_mt_thread<112>;
+  }
+  throw Error(XPCS_ERR_INVALID_ARGUMENT, "unsupported thread-kernel row capacity");
+}
+size_t warp_smem(int D, int acc, int cap, int warps) {
+  return mc_plan_bytes(D) + (size_t)warps * (2 * cap + 32 * acc) * sizeof(int32_t);
 }
 
 }  // namespace
@@ -541,32 +598,53 @@ size_t warp_smem(int D, int acc) {
 void run_multitau(Series &s, int mode) {
   cudaStream_t st = s.stream;
   const int D = s.D, P = s.P;
+  // the plan depends on the series' shape and the mode only; it is uploaded
+  // once per mode (a captured batch graph must not copy from host memory)
   std::vector<uint8_t> plan = make_plan(s, mode);
   const McPlan *hp = (const McPlan *)plan.data();
-  s.plan.reserve(plan.size(), st);
-  XG_CUDA(cudaMemcpyAsync(s.plan.p, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
+  if (s.plan_mode != mode) {
+    s.plan.reserve(plan.size(), st);
+    XG_CUDA(cudaMemcpyAsync(s.plan.p, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
+    XG_CUDA(cudaStreamSynchronize(st));
+    s.plan_mode = mode;
+  }
   const size_t nD = (size_t)D * P;
   s.G2.reserve(nD ? nD : 1, st);
   s.IP.reserve(nD ? nD : 1, st);
   s.IF.reserve(nD ? nD : 1, st);
   if (D == 0 || P == 0) return;
   const int scr = std::max(hp->acc, hp->nlev);
-  const size_t smt = thread_smem(D, scr), smw = warp_smem(D, hp->acc);
-  if (smt > 227 * 1024 || smw > 227 * 1024)
+  const ThreadKernel ktt = thread_kernel(s.thread_cap);
+  const size_t smt = thread_smem(D, scr, s.thread_cap), smw = warp_smem(D, scr, MT_WARP_CAP, WP_WARPS);
+  const size_t smm = warp_smem(D, scr, MT_MID_CAP, MID_WARPS);
+  const size_t sml = warp_smem(D, scr, MT_LONG_CAP, LONG_WARPS);
+  if (smt > 227 * 1024 || smw > 227 * 1024 || smm > 227 * 1024 || sml > 227 * 1024)
     throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay schedule too large for the multi-tau kernels");
-  XG_CUDA(cudaFuncSetAttribute(k_mt_thread, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
-  XG_CUDA(cudaFuncSetAttribute(k_mt_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw));
+  XG_CUDA(cudaFuncSetAttribute(ktt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
+  XG_CUDA(cudaFuncSetAttribute(k_mt_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)std::max(std::max(smw, smm), sml)));
   int sms = 0;
   XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
   XG_CUDA(cudaEventRecord(s.ev[4], st));
   const int per_block = MT_WARPS * 32;
-  k_mt_thread<<<(P + per_block - 1) / per_block, per_block, smt, st>>>(
+  ktt<<<(P + per_block - 1) / per_block, per_block, smt, st>>>(
       s.plan.p, s.row_ptr.p, s.row_len.p, s.pclass.p, s.ev_frame.p, s.ev_val.p, s.G2.p, s.IP.p,
       s.IF.p);
   XG_CHECK_LAUNCH();
-  k_mt_warp<<<sms * 2, WP_WARPS * 32, smw, st>>>(s.plan.p, s.wlist.p, s.stats.p, s.row_ptr.p,
-                                                 s.row_len.p, s.ev_frame.p, s.ev_val.p, s.G2.p,
-                                                 s.IP.p, s.IF.p);
+  const DevStats *ds = s.stats.p;
+  // rows of 81-256 events; long rows in two launches over one list: up to 1024
+  // events with 4 warps per block, longer ones with 2 warps per block
+  k_mt_warp<<<sms * (int)((227 * 1024) / smw), WP_WARPS * 32, smw, st>>>(
+      s.plan.p, s.wlist.p, &ds->nwarp, 0, MT_WARP_CAP, s.row_ptr.p, s.row_len.p, s.ev_frame.p,
+      s.ev_val.p, s.G2.p, s.IP.p, s.IF.p);
+  XG_CHECK_LAUNCH();
+  k_mt_warp<<<sms * (int)((227 * 1024) / smm), MID_WARPS * 32, smm, st>>>(
+      s.plan.p, s.llist.p, &ds->nlong, MT_WARP_CAP, MT_MID_CAP, s.row_ptr.p, s.row_len.p,
+      s.ev_frame.p, s.ev_val.p, s.G2.p, s.IP.p, s.IF.p);
+  XG_CHECK_LAUNCH();
+  k_mt_warp<<<sms * (int)((227 * 1024) / sml), LONG_WARPS * 32, sml, st>>>(
+      s.plan.p, s.llist.p, &ds->nlong, MT_MID_CAP, MT_LONG_CAP, s.row_ptr.p, s.row_len.p,
+      s.ev_frame.p, s.ev_val.p, s.G2.p, s.IP.p, s.IF.p);
   XG_CHECK_LAUNCH();
   XG_CUDA(cudaEventRecord(s.ev[5], st));
   size_t ne = s.raw_events > 0 ? (size_t)s.raw_events : 1;

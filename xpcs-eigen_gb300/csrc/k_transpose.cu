@@ -290,11 +290,16 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   }
 }
 
+// Work lists of the multi-tau kernels (pixel indices per class).
+struct ClassLists {
+  int32_t *wlist, *llist, *flist;
+};
+
 // Classification of the pixels of one warp (all 32 lanes call it; lanes
 // without a pixel pass has = false): pclass, the float/warp work lists and the
 // counters, one atomic per warp and counter.
 __device__ __forceinline__ void record_class_warp(bool has, int32_t p, uint8_t c, int32_t n,
-                                                  uint8_t *pclass, int32_t *wlist, int32_t *flist,
+                                                  uint8_t *pclass, const ClassLists &cl,
                                                   DevStats *stats) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -303,21 +308,25 @@ __device__ __forceinline__ void record_class_warp(bool has, int32_t p, uint8_t c
   const bool live = has && c != PCLASS_EMPTY;
   const unsigned mv = __ballot_sync(FULL, live);
   const unsigned mw = __ballot_sync(FULL, live && c == PCLASS_WARP);
+  const unsigned ml = __ballot_sync(FULL, live && c == PCLASS_LONG);
   const unsigned mf = __ballot_sync(FULL, live && c == PCLASS_FLOAT);
   const unsigned ev = __reduce_add_sync(FULL, live ? (unsigned)n : 0u);
-  int bw = 0, bf = 0;
+  int bw = 0, bl = 0, bf = 0;
   if (lane == 0) {
     if (mv) {
       atomicAdd(&stats->nvalid, __popc(mv));
       atomicAdd(&stats->events, (unsigned long long)ev);
     }
     if (mw) bw = atomicAdd(&stats->nwarp, __popc(mw));
+    if (ml) bl = atomicAdd(&stats->nlong, __popc(ml));
     if (mf) bf = atomicAdd(&stats->nfloat, __popc(mf));
   }
   bw = __shfl_sync(FULL, bw, 0);
+  bl = __shfl_sync(FULL, bl, 0);
   bf = __shfl_sync(FULL, bf, 0);
-  if (live && c == PCLASS_WARP) wlist[bw + __popc(mw & lt)] = p;
-  if (live && c == PCLASS_FLOAT) flist[bf + __popc(mf & lt)] = p;
+  if (live && c == PCLASS_WARP) cl.wlist[bw + __popc(mw & lt)] = p;
+  if (live && c == PCLASS_LONG) cl.llist[bl + __popc(ml & lt)] = p;
+  if (live && c == PCLASS_FLOAT) cl.flist[bf + __popc(mf & lt)] = p;
 }
 
 // Per-lane merge of one pixel's row: events of the same filter frame summed in
@@ -359,11 +368,10 @@ __device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *
 // otherwise each lane merges its own row / sums it in frame order.  Pixels
 // outside the mask get empty rows.
 __global__ void __launch_bounds__(256)
-k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ cnt,
+k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, const int32_t *__restrict__ cnt,
                  const int64_t *__restrict__ row_ptr, const uint8_t *__restrict__ mask,
                  int32_t *__restrict__ fr, float *__restrict__ val, int32_t *__restrict__ row_len,
-                 uint8_t *__restrict__ pclass, int32_t *__restrict__ wlist,
-                 int32_t *__restrict__ flist, float *__restrict__ pixels_sum,
+                 uint8_t *__restrict__ pclass, ClassLists cl, float *__restrict__ pixels_sum,
                  DevStats *__restrict__ stats) {
   __shared__ long long s_total[8][32];
   __shared__ long long s_sum[8][32];
@@ -431,8 +439,8 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, const int32_t *__restrict__ 
     row_len[p] = out;
     pixels_sum[p] = psum;
   }
-  const uint8_t c = keep ? pixel_class(out, integral, total, F) : (uint8_t)PCLASS_EMPTY;
-  record_class_warp(has, p, c, out, pclass, wlist, flist, stats);
+  const uint8_t c = keep ? pixel_class(out, integral, total, F, tcap) : (uint8_t)PCLASS_EMPTY;
+  record_class_warp(has, p, c, out, pclass, cl, stats);
 }
 
 template <bool FIRST, bool LAST>
@@ -492,6 +500,7 @@ void run_filter_transpose(Series &s) {
   s.pclass.reserve(P, st);
   s.flist.reserve(P, st);
   s.wlist.reserve(P, st);
+  s.llist.reserve(P, st);
   s.pixels_sum.reserve(P, st);
   s.stats.reserve(1, st);
   XG_CUDA(cudaMemsetAsync(s.cnt.p, 0, sizeof(int32_t) * P, st));
@@ -591,8 +600,10 @@ void run_filter_transpose(Series &s) {
   exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
   const int pix_per_block = 256;
   k_merge_classify<<<(P + pix_per_block - 1) / pix_per_block, 256, 0, st>>>(
-      P, s.F, s.desc.avg_frames, s.cnt.p, s.row_ptr.p, s.d_mask.p, s.ev_frame.p, s.ev_val.p,
-      s.row_len.p, s.pclass.p, s.wlist.p, s.flist.p, s.pixels_sum.p, s.stats.p);
+      P, s.F, s.desc.avg_frames, s.thread_cap, s.cnt.p, s.row_ptr.p, s.d_mask.p, s.ev_frame.p,
+      s.ev_val.p,
+      s.row_len.p, s.pclass.p, ClassLists{s.wlist.p, s.llist.p, s.flist.p}, s.pixels_sum.p,
+      s.stats.p);
   XG_CHECK_LAUNCH();
 }
 
@@ -604,18 +615,17 @@ namespace {
 // Caller-held rows (xpcs_multitau2): rows stay as given; a pixel takes the
 // integer path only if its frames are strictly increasing within [0, F), its
 // values are integers and sum |v| < 4096.
-__global__ void k_classify_rows(int32_t P, int32_t F, const int64_t *__restrict__ row_ptr,
+__global__ void k_classify_rows(int32_t P, int32_t F, int32_t tcap, const int64_t *__restrict__ row_ptr,
                                 const int32_t *__restrict__ fr, const float *__restrict__ val,
                                 int32_t *__restrict__ row_len, uint8_t *__restrict__ pclass,
-                                int32_t *__restrict__ wlist, int32_t *__restrict__ flist,
-                                DevStats *__restrict__ stats) {
+                                ClassLists cl, DevStats *__restrict__ stats) {
   const int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p - (int32_t)(threadIdx.x & 31) >= P) return;  // whole warp past the end
   const bool has = p < P;
   const int64_t b = has ? row_ptr[p] : 0;
   const int32_t n = has ? (int32_t)(row_ptr[p + 1] - b) : 0;
   if (has) row_len[p] = n;
-  bool ok = n <= MT_WARP_CAP;
+  bool ok = n <= MT_LONG_CAP;
   long long total = 0;
   int32_t prev = -1;
   for (int32_t i = 0; i < n && ok; i++) {
@@ -625,8 +635,8 @@ __global__ void k_classify_rows(int32_t P, int32_t F, const int64_t *__restrict_
     if (ok) total += llabs((long long)x);
     prev = f;
   }
-  const uint8_t c = n == 0 ? (uint8_t)PCLASS_EMPTY : pixel_class(n, ok, total, F);
-  record_class_warp(has, p, c, n, pclass, wlist, flist, stats);
+  const uint8_t c = n == 0 ? (uint8_t)PCLASS_EMPTY : pixel_class(n, ok, total, F, tcap);
+  record_class_warp(has, p, c, n, pclass, cl, stats);
 }
 
 }  // namespace
@@ -641,6 +651,7 @@ void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *fram
   s.pclass.reserve(P, st);
   s.flist.reserve(P, st);
   s.wlist.reserve(P, st);
+  s.llist.reserve(P, st);
   s.stats.reserve(1, st);
   s.ev_frame.reserve(ne, st);
   s.ev_val.reserve(ne, st);
@@ -653,9 +664,10 @@ void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *fram
     XG_CUDA(cudaMemcpyAsync(s.ev_val.p, value, sizeof(float) * events, cudaMemcpyHostToDevice, st));
   }
   const int bs = 256;
-  k_classify_rows<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.F, s.row_ptr.p, s.ev_frame.p,
+  k_classify_rows<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.F, s.thread_cap, s.row_ptr.p, s.ev_frame.p,
                                                      s.ev_val.p, s.row_len.p, s.pclass.p,
-                                                     s.wlist.p, s.flist.p, s.stats.p);
+                                                     ClassLists{s.wlist.p, s.llist.p, s.flist.p},
+                                                     s.stats.p);
   XG_CHECK_LAUNCH();
 }
 

@@ -138,20 +138,29 @@ __host__ __device__ inline McArrays mc_arrays(const void *plan, int D) {
 
 // Pixel classes assigned by the filter's merge pass.  The integer kernels
 // need integer values with sum |v| < 4096 (every float partial sum of the
-// reference is then exact); the thread-per-pixel kernel also needs frames
-// below 65536 and at most MT_THREAD_CAP events.
-#ifndef XG_MT_THREAD_CAP
-#define XG_MT_THREAD_CAP 80
-#endif
-constexpr int MT_THREAD_CAP = XG_MT_THREAD_CAP;
+// reference is then exact) and frames below 65536 (packed with the value in
+// one 32-bit word); by row length they go to the thread-per-pixel kernel, the
+// warp-per-pixel kernel or its long-row launch.
+// Row capacities of the thread-per-pixel kernel (one instantiation each); a
+// series uses one of them (Series::thread_cap, default MT_THREAD_CAP_DEFAULT,
+// chosen per series by xpcs_autotune).  Rows longer than the series' capacity
+// go to the warp-per-pixel kernel.
+constexpr int MT_THREAD_CAPS[] = {32, 48, 64, 80, 112};
+constexpr int MT_THREAD_NCAPS = 5;
+constexpr int MT_THREAD_CAP_DEFAULT = 80;
 constexpr int MT_WARP_CAP = 256;
-enum : uint8_t { PCLASS_EMPTY = 0, PCLASS_THREAD = 1, PCLASS_WARP = 2, PCLASS_FLOAT = 3 };
+constexpr int MT_LONG_CAP = 4096;  // an integer row with sum |v| < 4096 has fewer non-zero events
+enum : uint8_t { PCLASS_EMPTY = 0, PCLASS_THREAD = 1, PCLASS_WARP = 2, PCLASS_FLOAT = 3,
+                 PCLASS_LONG = 4 };
 
-__host__ __device__ inline uint8_t pixel_class(int n, bool integral, long long total, int F) {
+__host__ __device__ inline uint8_t pixel_class(int n, bool integral, long long total, int F,
+                                               int thread_cap) {
   if (n == 0) return PCLASS_EMPTY;
   if (!integral || total >= 4096) return PCLASS_FLOAT;
-  if (n <= MT_THREAD_CAP && F <= 65536) return PCLASS_THREAD;
+  if (F > 65536) return PCLASS_FLOAT;  // the integer kernels pack frames in 16 bits
+  if (n <= thread_cap) return PCLASS_THREAD;
   if (n <= MT_WARP_CAP) return PCLASS_WARP;
+  if (n <= MT_LONG_CAP) return PCLASS_LONG;
   return PCLASS_FLOAT;
 }
 
@@ -161,6 +170,7 @@ struct DevStats {
   int32_t nfloat;
   int32_t nvalid;
   int32_t nwarp;
+  int32_t nlong;
   unsigned long long events;
 };
 
@@ -210,6 +220,7 @@ struct Series {
   DBuf<uint8_t> pclass;
   DBuf<int32_t> flist;      // pixels of the float path
   DBuf<int32_t> wlist;      // pixels of the warp-per-pixel integer path
+  DBuf<int32_t> llist;      // pixels of the long-row warp-per-pixel integer path
   DBuf<int32_t> ev_frame;   // final pixel-major lists
   DBuf<float> ev_val;
   DBuf<float> pixels_sum;
@@ -224,8 +235,13 @@ struct Series {
 
   // multi-tau
   DBuf<uint8_t> plan;       // McPlan + tau_lvl[D] + denom[D]
+  int32_t plan_mode = -1;   // mode of the plan in `plan` (-1: none uploaded)
+  int32_t thread_cap = MT_THREAD_CAP_DEFAULT;  // rows up to this length: thread per pixel
+  bool tuned = false;       // thread_cap chosen by xpcs_autotune
   DBuf<float> G2, IP, IF;
   bool have_multitau = false;
+  bool have_norm64 = false, have_norm32 = false;
+  int64_t generation = 0;   // bumped by every change of the ingested frames
 
   // normalisation
   DBuf<int32_t> n_q_entry_ptr, n_entry_sbin, n_entry_pix_ptr, n_pix, n_q_row;
@@ -246,6 +262,28 @@ struct Series {
   void *pinned = nullptr;
   size_t pinned_cap = 0;
 };
+
+// --------------------------------------------------------------- a batch
+
+struct Batch {
+  std::vector<Series *> ss;
+  int device = 0;
+  cudaStream_t origin = nullptr;   // the graph is captured from and launched on it
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+  std::vector<cudaEvent_t> join;
+  std::vector<int64_t> gens;       // member generations at capture
+  int mode = -1;
+  uint32_t flags = 0;
+  int64_t kernels = 0;             // kernel nodes in the graph
+  float last_ms = 0.f;
+  int32_t lanes = 0;               // concurrent chains of series in the graph (0: one per series)
+  bool lanes_tuned = false;
+  ~Batch();
+};
+Batch *batch_create(Series *const *ss, int32_t n);   // batch.cu
+int32_t autotune(Series &s, int mode);               // batch.cu
+void batch_run(Batch &b, int mode, uint32_t flags);
 
 // Sets the message xpcs_last_error() returns on this thread (abi.cu).
 void xpcs_set_last_error(const char *msg);

@@ -144,6 +144,18 @@ extern "C" int xs_make_maps(const xs_params *p, int32_t *dqmap, int32_t *sqmap, 
   return 0;
 }
 
+extern "C" int xs_pixel_fields(const xs_params *p, float *a, float *s) {
+  if (!p || p->width <= 0 || p->height <= 0 || p->n_static <= 0 || p->n_dynamic <= 0) return 1;
+  Geometry g = geometry(p, nullptr, nullptr);
+  const int P = p->width * p->height;
+  for (int i = 0; i < P; i++) {
+    const double tau = g.tau[g.ring[i]];
+    a[i] = (float)std::exp(-1.0 / tau);
+    s[i] = (float)std::sqrt(1.0 - (double)a[i] * a[i]);
+  }
+  return 0;
+}
+
 extern "C" int64_t xs_sparse(const xs_params *p, uint32_t *nnz, int32_t **idx_out,
                              int16_t **val_out) {
   const int P = p->width * p->height, F = p->frames;

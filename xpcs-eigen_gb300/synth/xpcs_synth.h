@@ -58,6 +58,11 @@ void xs_dense_destroy(xs_dense_state *s);
 
 void xs_free(void *ptr);
 
+/* The speckle field's AR(1) coefficients of every pixel (a = exp(-1/tau_c) of
+ * its ring, s = sqrt(1-a^2)), masked pixels included: [height*width] each.
+ * The GPU generator (xpcs_synth_gpu.cu) takes them to draw the same frames. */
+int xs_pixel_fields(const xs_params *p, float *a, float *s);
+
 #ifdef __cplusplus
 }
 #endif

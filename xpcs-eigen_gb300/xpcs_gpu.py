@@ -33,8 +33,14 @@ EXPORTS = [
     "xpcs_ingest_sparse_device", "xpcs_multitau", "xpcs_get_g2ipif", "xpcs_normalize",
     "xpcs_synchronize", "xpcs_get_stage_times", "xpcs_multitau2", "xpcs_pin_host",
     "xpcs_unpin_host", "xpcs_multitau2_noalloc", "xpcs_set_dark", "xpcs_ingest_dense",
-    "xpcs_ingest_dense_device", "xpcs_get_dark", "xpcs_side_stats",
+    "xpcs_ingest_dense_device", "xpcs_get_dark", "xpcs_side_stats", "xpcs_get_normalized",
+    "xpcs_batch_create", "xpcs_batch_run", "xpcs_batch_stats", "xpcs_batch_destroy",
+    "xpcs_autotune",
 ]
+
+BATCH_F64 = 1
+BATCH_F32 = 2
+BATCH_AUTOTUNE = 4
 
 NOALLOC_MAX_EVENTS = 4194304
 
@@ -100,6 +106,13 @@ def lib() -> C.CDLL:
         L.xpcs_side_stats.argtypes = [C.c_void_p] + [C.c_void_p] * 4
         L.xpcs_get_g2ipif.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_normalize.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.xpcs_get_normalized.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        L.xpcs_batch_create.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
+        L.xpcs_batch_run.argtypes = [C.c_void_p, C.c_int32, C.c_uint32]
+        L.xpcs_batch_stats.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int32)]
+        L.xpcs_batch_destroy.argtypes = [C.c_void_p]
+        L.xpcs_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
         L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                              C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -239,10 +252,66 @@ class Series:
         check(lib().xpcs_normalize(self._h, *[_ptr(a) for a in out]))
         return out
 
+    def autotune(self, mode=MODE_REFERENCE) -> int:
+        """xpcs_autotune: pick this series' thread-kernel row capacity; returns it."""
+        c = C.c_int32(0)
+        check(lib().xpcs_autotune(self._h, mode, C.byref(c)))
+        return c.value
+
+    def normalized(self, f64=True, f32=False, out=None):
+        """Results of the last normalisation (xpcs_normalize or a batch run)."""
+        if out is None:
+            shp = (self.D, self.nq)
+            out = (np.empty(shp, np.float64) if f64 else None,
+                   np.empty(shp, np.float64) if f64 else None,
+                   np.empty(shp, np.float32) if f32 else None,
+                   np.empty(shp, np.float32) if f32 else None)
+        check(lib().xpcs_get_normalized(self._h, *[_ptr(a) for a in out]))
+        return out
+
     def stage_times(self) -> dict:
         t = StageTimes()
         check(lib().xpcs_get_stage_times(self._h, C.byref(t)))
         return {n: getattr(t, n) for n, _ in StageTimes._fields_}
+
+
+class Batch:
+    """Several series of one device run as one CUDA graph (an xpcs_batch handle).
+    The member Series objects must stay open while the batch exists."""
+
+    def __init__(self, series):
+        self.series = list(series)
+        arr = (C.c_void_p * len(self.series))(*[s._h for s in self.series])
+        self._arr = arr
+        self._h = C.c_void_p()
+        check(lib().xpcs_batch_create(arr, len(self.series), C.byref(self._h)))
+
+    def run(self, mode=MODE_REFERENCE, f64=True, f32=False, autotune=False):
+        flags = ((BATCH_F64 if f64 else 0) | (BATCH_F32 if f32 else 0)
+                 | (BATCH_AUTOTUNE if autotune else 0))
+        check(lib().xpcs_batch_run(self._h, mode, flags))
+
+    def stats(self):
+        """(device ms of the last run, kernels in the graph, concurrent chains)."""
+        ms = C.c_float(0)
+        k = C.c_int64(0)
+        lanes = C.c_int32(0)
+        check(lib().xpcs_batch_stats(self._h, C.byref(ms), C.byref(k), C.byref(lanes)))
+        return ms.value, k.value, lanes.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().xpcs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def pin(a: np.ndarray) -> np.ndarray:

@@ -16,6 +16,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libxpcs_synth.so"
+LIB_GPU = HERE / "_build" / "libxpcs_synth_gpu.so"
 
 
 class _Params(C.Structure):
@@ -107,6 +108,7 @@ def lib():
         L.xs_dense_next.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int16)]
         L.xs_dense_destroy.argtypes = [C.c_void_p]
         L.xs_free.argtypes = [C.c_void_p]
+        L.xs_pixel_fields.argtypes = [C.POINTER(_Params), C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -142,6 +144,73 @@ def sparse_frames(acq: Acquisition):
     lib().xs_free(C.cast(pi, C.c_void_p))
     lib().xs_free(C.cast(pv, C.c_void_p))
     return nnz, idx, val
+
+
+_glib = None
+
+
+def glib():
+    """libxpcs_synth_gpu: the same sparse frames drawn on the current CUDA device."""
+    global _glib
+    if _glib is None:
+        if not LIB_GPU.exists():
+            from build import build_synth_gpu  # noqa: E402
+            build_synth_gpu()
+        L = C.CDLL(str(LIB_GPU))
+        L.xsg_sparse.restype = C.c_int64
+        L.xsg_sparse.argtypes = [C.POINTER(_Params), C.c_void_p, C.c_void_p,
+                                 C.POINTER(C.c_uint32), C.POINTER(C.c_void_p),
+                                 C.POINTER(C.c_void_p)]
+        L.xsg_free.argtypes = [C.c_void_p]
+        L.xsg_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+        _glib = L
+    return _glib
+
+
+def pixel_fields(acq: Acquisition):
+    """Per-pixel AR(1) coefficients (a, s) of the speckle field, float32 [P] each."""
+    p = acq._struct()
+    P = acq.width * acq.height
+    a = np.zeros(P, np.float32)
+    s = np.zeros(P, np.float32)
+    lib().xs_pixel_fields(C.byref(p), a.ctypes.data_as(C.c_void_p), s.ctypes.data_as(C.c_void_p))
+    return a, s
+
+
+class DeviceFrames:
+    """Sparse frames of ``sparse_frames(acq)`` drawn on the current CUDA device:
+    ``nnz`` (host uint32 [frames]), ``idx`` / ``val`` device pointers of
+    ``events`` int32 / int16 entries.  Free with close()."""
+
+    def __init__(self, acq: Acquisition):
+        p = acq._struct()
+        a, s = pixel_fields(acq)
+        self.nnz = np.zeros(acq.frames, np.uint32)
+        pi, pv = C.c_void_p(), C.c_void_p()
+        n = glib().xsg_sparse(C.byref(p), a.ctypes.data_as(C.c_void_p),
+                              s.ctypes.data_as(C.c_void_p),
+                              self.nnz.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(pi),
+                              C.byref(pv))
+        if n < 0:
+            raise MemoryError("xsg_sparse failed")
+        self.events, self.idx, self.val = int(n), pi.value, pv.value
+
+    def to_host(self):
+        idx = np.empty(self.events, np.int32)
+        val = np.empty(self.events, np.int16)
+        if self.events:
+            glib().xsg_to_host(idx.ctypes.data_as(C.c_void_p), self.idx, idx.nbytes)
+            glib().xsg_to_host(val.ctypes.data_as(C.c_void_p), self.val, val.nbytes)
+        return self.nnz, idx, val
+
+    def close(self):
+        if getattr(self, "idx", None):
+            glib().xsg_free(self.idx)
+            glib().xsg_free(self.val)
+            self.idx = self.val = None
+
+    def __del__(self):
+        self.close()
 
 
 class DenseStream:
