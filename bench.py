@@ -299,6 +299,68 @@ def run_batch(args, dev):
             "identical_results": bool(same), "reps": args.batch_reps}
 
 
+def run_serving(args, dev):
+    """Streaming: 16 concurrent 1024x1024 sparse acquisitions at 200 Hz each
+    with staggered starts, pushed frame by frame into one xpcs_server as the
+    frames fall due (one feeder thread replays the merged arrival schedule);
+    each acquisition is finished after its last frame and its g2 read back.
+    Reports frames/s, the per-frame ingest latency and the time to final g2."""
+    import xpcs_gpu as xg
+
+    rng = np.random.default_rng(4242)
+    n = args.serve_streams
+    lengths = [int(round(L * args.serve_length_scale))
+               for L in rng.choice([2000, 5000, 20000], size=n)]
+    acqs, data = [], []
+    for i, F in enumerate(lengths):
+        acq = xs.Acquisition(width=1024, height=1024, frames=F, n_static=36, n_dynamic=18,
+                             mean=0.01, tau_min=5.0, tau_max=1000.0, seed=5000 + i, dpl=8)
+        dq, sq, _, _ = xs.maps(acq)
+        d = xs.DeviceFrames(acq)
+        nnz, idx, val = d.to_host()
+        d.close()
+        off = np.concatenate([[0], np.cumsum(nnz.astype(np.int64))])
+        acqs.append((acq, dq, sq))
+        data.append((nnz, idx, val, off))
+    starts = [i * args.serve_stagger for i in range(n)]
+    sched = sorted((starts[i] + k / args.serve_hz, i, k)
+                   for i in range(n) for k in range(lengths[i]))
+    budget = int(args.serve_budget_gb * (1 << 30))
+    with xg.Server(memory_budget=budget, device=dev) as srv:
+        ids = []
+        for (acq, dq, sq), (nnz, idx, _, _) in zip(acqs, data):
+            ids.append(srv.submit(acq.width, acq.height, acq.frames, acq.dpl, dq, sq,
+                                  expected_events=idx.size))
+        t0 = time.perf_counter()
+        for t, i, k in sched:
+            dt = t0 + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            nnz, idx, val, off = data[i]
+            srv.push(ids[i], nnz[k:k + 1], idx[off[k]:off[k + 1]], val[off[k]:off[k + 1]])
+            if k == lengths[i] - 1:
+                srv.finish(ids[i])
+        for i in ids:
+            srv.result(i)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        for i in ids:
+            srv.release(i)
+    frames = int(sum(lengths))
+    return {"workload": (f"{n} concurrent 1024x1024 sparse acquisitions at {args.serve_hz:g} Hz "
+                         f"each, mean 0.01 photons/pixel/frame, tau_c log-uniform [5, 1000], "
+                         f"lengths drawn from 2000/5000/20000 frames x {args.serve_length_scale:g}, "
+                         f"starts {args.serve_stagger:g} s apart, seed 4242"),
+            "streams": n, "frames": frames, "events": int(sum(d[1].size for d in data)),
+            "wall_s": wall, "frames_per_s": frames / wall,
+            "ingest_p50_ms": st["ingest_p50_ms"], "ingest_p99_ms": st["ingest_p99_ms"],
+            "ingest_max_ms": st["ingest_max_ms"],
+            "time_to_final_g2_p50_ms": st["final_p50_ms"],
+            "time_to_final_g2_p99_ms": st["final_p99_ms"],
+            "peak_active": st["peak_active"], "memory_budget_gb": args.serve_budget_gb,
+            "peak_footprint_gb": st["peak_used_bytes"] / (1 << 30)}
+
+
 def run_gpu_arm(args, dist):
     import xpcs_gpu as xg
 
@@ -407,6 +469,8 @@ def run_gpu_arm(args, dist):
     }
     if not args.no_batch:
         result["batch"] = run_batch(args, dev)
+    if not args.no_serving:
+        result["serving"] = run_serving(args, dev)
     if dist.rank == 0 and world == 1 and not args.no_cpu_baseline:
         frames = args.cpu_sample_frames
         t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
@@ -430,6 +494,13 @@ def main():
     ap.add_argument("--cpu-sample-frames", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-series batch measure")
+    ap.add_argument("--no-serving", action="store_true", help="skip the streaming measure")
+    ap.add_argument("--serve-streams", type=int, default=16)
+    ap.add_argument("--serve-hz", type=float, default=200.0)
+    ap.add_argument("--serve-stagger", type=float, default=0.2, help="seconds between starts")
+    ap.add_argument("--serve-length-scale", type=float, default=0.1,
+                    help="scale of the 2000/5000/20000-frame lengths (1.0 = full, ~100 s)")
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--batch-series", type=int, default=64)
     ap.add_argument("--batch-reps", type=int, default=3)
     ap.add_argument("--width", type=int, default=None,

@@ -276,6 +276,51 @@ int xpcs_batch_run(xpcs_batch *b, int32_t mode, uint32_t flags);
 int xpcs_batch_stats(xpcs_batch *b, float *ms, int64_t *kernels, int32_t *lanes);
 void xpcs_batch_destroy(xpcs_batch *b);
 
+/* Serving (no reference counterpart): several acquisitions streamed at once.
+ * An acquisition is submitted with its series description and expected event
+ * count; it is admitted -- its series created on the GPU -- as soon as its
+ * estimated device footprint (raw events and work buffers, ~46 B per event,
+ * plus 12 B per pixel and delay for G2/IP/IF) fits `memory_budget`, in
+ * submission order (an acquisition larger than the budget is admitted when
+ * nothing else is active).  Frames pushed before admission wait in host
+ * memory.  push copies frames into the acquisition's resident buffers on its
+ * own stream and returns; finish enqueues filter/transpose, multi-tau and the
+ * float64 normalisation and returns; result waits and reads g2/stderr [D][Q]
+ * (and G2/IP/IF [D][P]; any pointer may be NULL); release frees the series and
+ * admits waiting acquisitions.  Results equal those of the series run alone.
+ * Different acquisitions may be driven from different threads; calls for one
+ * acquisition must be ordered by the caller.
+ * Statistics: ingest latency per frame = arrival in push to the end of its
+ * device copy; time to final g2 per acquisition = arrival of its last frame
+ * (or the finish call) to the end of its normalisation. */
+typedef struct xpcs_server xpcs_server;
+typedef struct {
+  int64_t frames_ingested;
+  int64_t series_finished;
+  double ingest_p50_ms, ingest_p99_ms, ingest_max_ms;
+  double final_p50_ms, final_p99_ms;
+  int32_t active, pending, peak_active, reserved;
+  uint64_t used_bytes, peak_used_bytes;
+} xpcs_server_stats;
+/* xpcs_server_state values */
+#define XPCS_ACQ_PENDING 0
+#define XPCS_ACQ_ACTIVE 1
+#define XPCS_ACQ_FINISHING 2
+#define XPCS_ACQ_DONE 3
+#define XPCS_ACQ_FAILED 4
+int xpcs_server_create(int32_t device, uint64_t memory_budget, xpcs_server **out);
+void xpcs_server_destroy(xpcs_server *srv);
+int xpcs_server_submit(xpcs_server *srv, const xpcs_series_desc *desc, int64_t expected_events,
+                       int64_t *id);
+int xpcs_server_push_sparse(xpcs_server *srv, int64_t id, const int32_t *idx, const int16_t *val,
+                            const uint32_t *nnz, int32_t nframes);
+int xpcs_server_finish(xpcs_server *srv, int64_t id, int32_t mode);
+int xpcs_server_state(xpcs_server *srv, int64_t id, int32_t *state);
+int xpcs_server_result(xpcs_server *srv, int64_t id, double *g2, double *stderr_, float *G2,
+                       float *IP, float *IF);
+int xpcs_server_release(xpcs_server *srv, int64_t id);
+int xpcs_server_get_stats(xpcs_server *srv, xpcs_server_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -109,3 +109,14 @@ def test_batch_rejects_bad_arguments():
     assert rc == 1 and h.value is None
     assert xg.lib().xpcs_batch_run(None, 0, 1) == 1
     xg.lib().xpcs_batch_destroy(None)
+
+
+def test_server_needs_a_device():
+    import ctypes as C
+    import shutil
+    if shutil.which("nvidia-smi"):
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    rc = xg.lib().xpcs_server_create(0, 1 << 30, C.byref(h))
+    assert rc == 7 and h.value is None
+    xg.lib().xpcs_server_destroy(None)

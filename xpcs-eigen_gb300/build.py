@@ -30,7 +30,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-I", str(INCLUDE), "-I", str(CSRC)]
 GPU_SOURCES = ["abi.cu", "scan.cu", "k_transpose.cu", "k_multitau.cu", "k_normalize.cu",
-               "qmap.cpp", "noalloc.cu", "k_dense.cu", "k_side.cu", "batch.cu"]
+               "qmap.cpp", "noalloc.cu", "k_dense.cu", "k_side.cu", "batch.cu",
+               "server.cpp"]
 
 LIB_GPU = BUILD / "libxpcs_gpu.so"
 LIB_SYNTH = BUILD / "libxpcs_synth.so"

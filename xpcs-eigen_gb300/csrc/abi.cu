@@ -493,6 +493,72 @@ void xpcs_batch_destroy(xpcs_batch *h) {
   delete b;
 }
 
+int xpcs_server_create(int32_t device, uint64_t memory_budget, xpcs_server **out) {
+  return guarded([&] {
+    need(out, "null argument");
+    *out = nullptr;
+    *out = (xpcs_server *)server_create(device, memory_budget);
+  });
+}
+
+void xpcs_server_destroy(xpcs_server *h) {
+  if (h) server_destroy(h);
+}
+
+int xpcs_server_submit(xpcs_server *h, const xpcs_series_desc *desc, int64_t expected_events,
+                       int64_t *id) {
+  return guarded([&] {
+    need(h && desc && id, "null argument");
+    *id = server_submit(h, *desc, expected_events);
+  });
+}
+
+int xpcs_server_push_sparse(xpcs_server *h, int64_t id, const int32_t *idx, const int16_t *val,
+                            const uint32_t *nnz, int32_t nframes) {
+  return guarded([&] {
+    need(h && (nframes == 0 || nnz), "null argument");
+    need(nframes >= 0, "negative frame count");
+    server_push(h, id, idx, val, nnz, nframes);
+  });
+}
+
+int xpcs_server_finish(xpcs_server *h, int64_t id, int32_t mode) {
+  return guarded([&] {
+    need(h, "null server");
+    need(mode == XPCS_MODE_REFERENCE || mode == XPCS_MODE_EXACT, "unknown mode");
+    server_finish(h, id, mode);
+  });
+}
+
+int xpcs_server_state(xpcs_server *h, int64_t id, int32_t *state) {
+  return guarded([&] {
+    need(h && state, "null argument");
+    *state = server_state(h, id);
+  });
+}
+
+int xpcs_server_result(xpcs_server *h, int64_t id, double *g2, double *se, float *G2, float *IP,
+                       float *IF) {
+  return guarded([&] {
+    need(h, "null server");
+    server_result(h, id, g2, se, G2, IP, IF);
+  });
+}
+
+int xpcs_server_release(xpcs_server *h, int64_t id) {
+  return guarded([&] {
+    need(h, "null server");
+    server_release(h, id);
+  });
+}
+
+int xpcs_server_get_stats(xpcs_server *h, xpcs_server_stats *st) {
+  return guarded([&] {
+    need(h && st, "null argument");
+    server_stats(h, st);
+  });
+}
+
 int xpcs_synchronize(xpcs_series *h) {
   return guarded([&] {
     need(h, "null handle");

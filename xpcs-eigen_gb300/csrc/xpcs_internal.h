@@ -285,6 +285,18 @@ Batch *batch_create(Series *const *ss, int32_t n);   // batch.cu
 int32_t autotune(Series &s, int mode);               // batch.cu
 void batch_run(Batch &b, int mode, uint32_t flags);
 
+// Serving front end (server.cpp); the handle is an opaque Server.
+void *server_create(int device, uint64_t budget);
+void server_destroy(void *srv);
+int64_t server_submit(void *srv, const xpcs_series_desc &desc, int64_t expected_events);
+void server_push(void *srv, int64_t id, const int32_t *idx, const int16_t *val,
+                 const uint32_t *nnz, int32_t nframes);
+void server_finish(void *srv, int64_t id, int mode);
+int server_state(void *srv, int64_t id);
+void server_result(void *srv, int64_t id, double *g2, double *se, float *G2, float *IP, float *IF);
+void server_release(void *srv, int64_t id);
+void server_stats(void *srv, xpcs_server_stats *out);
+
 // Sets the message xpcs_last_error() returns on this thread (abi.cu).
 void xpcs_set_last_error(const char *msg);
 

@@ -35,7 +35,9 @@ EXPORTS = [
     "xpcs_unpin_host", "xpcs_multitau2_noalloc", "xpcs_set_dark", "xpcs_ingest_dense",
     "xpcs_ingest_dense_device", "xpcs_get_dark", "xpcs_side_stats", "xpcs_get_normalized",
     "xpcs_batch_create", "xpcs_batch_run", "xpcs_batch_stats", "xpcs_batch_destroy",
-    "xpcs_autotune",
+    "xpcs_autotune", "xpcs_server_create", "xpcs_server_destroy", "xpcs_server_submit",
+    "xpcs_server_push_sparse", "xpcs_server_finish", "xpcs_server_state", "xpcs_server_result",
+    "xpcs_server_release", "xpcs_server_get_stats",
 ]
 
 BATCH_F64 = 1
@@ -43,6 +45,20 @@ BATCH_F32 = 2
 BATCH_AUTOTUNE = 4
 
 NOALLOC_MAX_EVENTS = 4194304
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("frames_ingested", C.c_int64), ("series_finished", C.c_int64),
+        ("ingest_p50_ms", C.c_double), ("ingest_p99_ms", C.c_double),
+        ("ingest_max_ms", C.c_double), ("final_p50_ms", C.c_double),
+        ("final_p99_ms", C.c_double), ("active", C.c_int32), ("pending", C.c_int32),
+        ("peak_active", C.c_int32), ("reserved", C.c_int32), ("used_bytes", C.c_uint64),
+        ("peak_used_bytes", C.c_uint64),
+    ]
+
+
+ACQ_STATES = {0: "pending", 1: "active", 2: "finishing", 3: "done", 4: "failed"}
 
 
 class XpcsError(RuntimeError):
@@ -113,6 +129,17 @@ def lib() -> C.CDLL:
                                        C.POINTER(C.c_int32)]
         L.xpcs_batch_destroy.argtypes = [C.c_void_p]
         L.xpcs_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+        L.xpcs_server_create.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]
+        L.xpcs_server_destroy.argtypes = [C.c_void_p]
+        L.xpcs_server_submit.argtypes = [C.c_void_p, C.POINTER(SeriesDesc), C.c_int64,
+                                         C.POINTER(C.c_int64)]
+        L.xpcs_server_push_sparse.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_int32]
+        L.xpcs_server_finish.argtypes = [C.c_void_p, C.c_int64, C.c_int32]
+        L.xpcs_server_state.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]
+        L.xpcs_server_result.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 5
+        L.xpcs_server_release.argtypes = [C.c_void_p, C.c_int64]
+        L.xpcs_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
         L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                              C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -302,6 +329,91 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None):
             lib().xpcs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def _desc(width, height, frames, dpl, dq, sq, flat=None, stride=1, average=1,
+          static_window=None, device=0):
+    d = SeriesDesc()
+    d.width, d.height, d.frames, d.delays_per_level = width, height, frames, dpl
+    d.stride_frames, d.avg_frames = stride, average
+    d.static_window = static_window or max(frames // 10, 1)
+    d.dqmap = dq.ctypes.data_as(C.POINTER(C.c_int32))
+    d.sqmap = sq.ctypes.data_as(C.POINTER(C.c_int32))
+    d.flatfield = flat.ctypes.data_as(C.POINTER(C.c_double)) if flat is not None else None
+    d.device = device
+    return d
+
+
+class Server:
+    """Streaming front end (an xpcs_server handle): acquisitions admitted by
+    device-memory budget, frames pushed as they arrive."""
+
+    def __init__(self, memory_budget: int, device=0):
+        self._h = C.c_void_p()
+        check(lib().xpcs_server_create(device, int(memory_budget), C.byref(self._h)))
+        self.device = device
+        self._shape = {}
+
+    def submit(self, width, height, frames, dpl, dqmap, sqmap, expected_events, flatfield=None,
+               stride=1, average=1, static_window=None) -> int:
+        dq = np.ascontiguousarray(dqmap, np.int32).ravel()
+        sq = np.ascontiguousarray(sqmap, np.int32).ravel()
+        flat = None if flatfield is None else np.ascontiguousarray(flatfield, np.float64).ravel()
+        d = _desc(width, height, frames, dpl, dq, sq, flat, stride, average, static_window,
+                  self.device)
+        i = C.c_int64(0)
+        check(lib().xpcs_server_submit(self._h, C.byref(d), int(expected_events), C.byref(i)))
+        lv, _ = delay_schedule(frames, dpl)
+        nq = int(np.unique(dq[(dq > 0) & (sq > 0)]).size)
+        self._shape[i.value] = (lv.size, nq, width * height)
+        return i.value
+
+    def push(self, acq_id, nnz, idx, val):
+        nnz = np.ascontiguousarray(nnz, np.uint32)
+        idx = np.ascontiguousarray(idx, np.int32)
+        val = np.ascontiguousarray(val, np.int16)
+        check(lib().xpcs_server_push_sparse(self._h, acq_id, _ptr(idx), _ptr(val), _ptr(nnz),
+                                            nnz.size))
+
+    def finish(self, acq_id, mode=MODE_REFERENCE):
+        check(lib().xpcs_server_finish(self._h, acq_id, mode))
+
+    def state(self, acq_id) -> str:
+        st = C.c_int32(0)
+        check(lib().xpcs_server_state(self._h, acq_id, C.byref(st)))
+        return ACQ_STATES[st.value]
+
+    def result(self, acq_id, g2ipif=False):
+        D, Q, P = self._shape[acq_id]
+        g2 = np.empty((D, Q))
+        se = np.empty((D, Q))
+        arrs = [np.empty((D, P), np.float32) for _ in range(3)] if g2ipif else [None] * 3
+        check(lib().xpcs_server_result(self._h, acq_id, _ptr(g2), _ptr(se),
+                                       *[_ptr(a) for a in arrs]))
+        return (g2, se, *arrs) if g2ipif else (g2, se)
+
+    def release(self, acq_id):
+        check(lib().xpcs_server_release(self._h, acq_id))
+        self._shape.pop(acq_id, None)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().xpcs_server_get_stats(self._h, C.byref(st)))
+        return {n: getattr(st, n) for n, _ in ServerStats._fields_ if n != "reserved"}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().xpcs_server_destroy(self._h)
             self._h = None
 
     def __del__(self):
