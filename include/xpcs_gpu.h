@@ -71,6 +71,10 @@ typedef struct {
   float lld;                /* dense with darks: /xpcs/lld */
   float sigma;              /* dense with darks: /xpcs/sigma */
   int32_t device;           /* CUDA device ordinal */
+  int32_t normalize_by_framesum; /* /xpcs/normalize_by_framesum: 1 divides every value by
+                                    (frame sum / mean frame sum) before multi-tau
+                                    (main.cpp:314-337); such series take the float path
+                                    and cannot join a batch */
 } xpcs_series_desc;
 
 typedef struct {

@@ -263,6 +263,20 @@ def dense_filter(qm: QMap, raw, frames, dark_avg=None, dark_std=None, lld=0.0, s
     return _collect(rows_s, side_s, fp, qm, finish)
 
 
+def framesum_normalize(rows: Rows, frames_sum, frames: int) -> Rows:
+    """The normalize_by_framesum pre-pass (src/xpcs/main.cpp:314-337): every
+    value divided by (frameSum[F+f] / mean), mean = the float sum of
+    frameSum[F..2F) in frame order divided by the frame count; all float32."""
+    fs = np.ascontiguousarray(frames_sum, np.float32).ravel()[frames:2 * frames]
+    acc = np.float32(0.0)
+    for x in fs:
+        acc = np.float32(acc + x)
+    mean = np.float32(acc / np.float32(frames))
+    q = (fs / mean).astype(np.float32)
+    value = (rows.value / q[rows.frame]).astype(np.float32)
+    return Rows(rows.row_ptr, rows.frame, value)
+
+
 def multitau2(rows: Rows, frames: int, dpl: int, mode: int = 0, threads: int = 0):
     """Corr::multiTau2 (src/xpcs/corr.cpp:315). mode 0 = reference, 1 = exact."""
     lv, _ = delays(frames, dpl)

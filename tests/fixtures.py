@@ -23,6 +23,7 @@ def load(name: str) -> dict:
     fx.update(W=W, H=H, F=F, real=real, dpl=dpl, stride=stride, avg=avg, swin=swin,
               ndark=ndark, dense=bool(dense))
     fx["flatfield"] = fx["flat"] if fx["flat"].size else None
+    fx["framesum"] = int(fx["framesum"]) if "framesum" in fx else 0
     return fx
 
 
@@ -45,6 +46,8 @@ def oracle_filter(fx):
             stride=fx["stride"], average=fx["avg"], static_window=fx["swin"],
             flat=flat.ravel() if flat is not None else None, clock=fx["clock"],
             ticks=fx["ticks"])
+    if fx["framesum"]:
+        rows = oracle.framesum_normalize(rows, side["frames_sum"], fx["F"])
     return qm, rows, side
 
 

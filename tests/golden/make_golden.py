@@ -140,9 +140,18 @@ def case_dense_dark():
     return acq, dict(raw=raw), dict(flat=True, dense=True, lld=2.0, sigma=3.0)
 
 
+def case_sparse_framesum():
+    # values divided by (frame sum / mean frame sum) before multi-tau (main.cpp:314-337)
+    acq = xs.Acquisition(width=36, height=36, frames=400, n_static=10, n_dynamic=5, mean=0.05,
+                         tau_min=4, tau_max=60, seed=19, dpl=4)
+    nnz, idx, val = _sparse(acq)
+    return acq, dict(nnz=nnz, idx=idx, val=val), dict(framesum=True)
+
+
 CASES = {f.__name__[5:]: f for f in [case_sparse_basic, case_sparse_quirk, case_sparse_stride_avg,
                                       case_sparse_flat, case_sparse_hot, case_sparse_dups,
-                                      case_qmap_shared_sbin, case_dense_dark]}
+                                      case_qmap_shared_sbin, case_dense_dark,
+                                      case_sparse_framesum]}
 
 
 def make(name, corr: Path):
@@ -174,7 +183,8 @@ def make(name, corr: Path):
                                    ticks=ticks)
             cfg = refio.config_entries(W, H, dq, sq, imm, first=1, last=real, dpl=acq.dpl,
                                        stride=stride, average=average,
-                                       flat=flat if use_flat else None)
+                                       flat=flat if use_flat else None,
+                                       normalize_by_framesum=1 if opt.get("framesum") else 0)
         cpath = wd / "config.h5"
         refio.write_xh5c(cpath, cfg)
         out = refio.run_reference(corr, cpath, wd)
@@ -185,7 +195,8 @@ def make(name, corr: Path):
                   params=np.array([W, H, frames, real, acq.dpl, stride, average,
                                    int(cfg["/xpcs/static_mean_window_size"]), acq.dark_frames,
                                    1 if opt.get("dense") else 0], np.int64),
-                  lld_sigma=np.array([opt.get("lld", 0.0), opt.get("sigma", 0.0)], np.float32))
+                  lld_sigma=np.array([opt.get("lld", 0.0), opt.get("sigma", 0.0)], np.float32),
+                  framesum=np.int32(1 if opt.get("framesum") else 0))
     for k, v in out.items():
         if k != "_stdout":
             arrays["ref_" + k.replace("-", "_")] = v

@@ -144,3 +144,15 @@ def test_autotune_changes_time_not_results():
     finally:
         for s in series:
             s.close()
+
+
+def test_framesum_series_cannot_join_a_batch():
+    fx, s = golden_member("sparse_quirk")
+    fs = xg.Series(fx["W"], fx["H"], fx["F"], fx["dpl"], fx["dqmap"], fx["sqmap"],
+                   normalize_by_framesum=True)
+    try:
+        with pytest.raises(xg.XpcsError):
+            xg.Batch([s, fs])
+    finally:
+        s.close()
+        fs.close()

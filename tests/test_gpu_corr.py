@@ -33,7 +33,8 @@ def _write_inputs(fx, wd: Path):
                                ticks=fx["ticks"])
         cfg = refio.config_entries(W, H, fx["dqmap"], fx["sqmap"], imm, first=1, last=fx["real"],
                                    dpl=fx["dpl"], stride=fx["stride"], average=fx["avg"],
-                                   flat=flat, static_window=fx["swin"])
+                                   flat=flat, static_window=fx["swin"],
+                                   normalize_by_framesum=fx["framesum"])
     path = wd / "analysis.h5"
     refio.write_xh5c(path, cfg)
     return path
@@ -72,10 +73,10 @@ def test_corr_rejects_unsupported_analyses(corr, tmp_path):
     fx = load("sparse_basic")
     cfg = _write_inputs(fx, tmp_path)
     ent = refio.read_xh5c(cfg)
-    ent["/xpcs/normalize_by_framesum"] = np.int32(1)
+    ent["/xpcs/analysis_type"] = "Twotime"
     refio.write_xh5c(cfg, ent)
     r = subprocess.run([str(corr), str(cfg)], capture_output=True, text=True)
-    assert r.returncode != 0 and "normalize_by_framesum" in r.stderr
+    assert r.returncode != 0 and "two-time" in r.stderr
 
 
 def test_corr_reads_config_and_frames_without_a_device(corr, tmp_path):

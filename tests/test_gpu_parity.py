@@ -21,7 +21,7 @@ F64_TOL = 1e-12
 def series_for(fx):
     return xg.Series(fx["W"], fx["H"], fx["F"], fx["dpl"], fx["dqmap"], fx["sqmap"],
                      flatfield=fx["flatfield"], stride=fx["stride"], average=fx["avg"],
-                     static_window=fx["swin"])
+                     static_window=fx["swin"], normalize_by_framesum=fx["framesum"])
 
 
 def run_gpu(fx, mode=xg.MODE_REFERENCE, chunks=1):

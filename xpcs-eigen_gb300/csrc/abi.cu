@@ -161,6 +161,8 @@ int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out) {
     need(desc->static_window >= 1, "static_window must be >= 1");
     need(desc->dqmap && desc->sqmap, "dqmap and sqmap are required");
     need(desc->dense == 0 || desc->dense == 1, "dense must be 0 or 1");
+    need(desc->normalize_by_framesum == 0 || desc->normalize_by_framesum == 1,
+         "normalize_by_framesum must be 0 or 1");
     s = new Series();
     s->desc = *desc;
     s->desc.dqmap = nullptr;

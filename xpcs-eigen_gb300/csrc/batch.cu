@@ -42,6 +42,9 @@ Batch *batch_create(Series *const *ss, int32_t n) {
       throw Error(XPCS_ERR_INVALID_ARGUMENT, "batch members must use one device");
     for (int32_t j = 0; j < i; j++)
       if (ss[j] == ss[i]) throw Error(XPCS_ERR_INVALID_ARGUMENT, "series twice in one batch");
+    if (ss[i]->desc.normalize_by_framesum)
+      throw Error(XPCS_ERR_INVALID_ARGUMENT,
+                  "normalize_by_framesum reads frame sums back to the host: not in a batch");
   }
   Batch *b = new Batch();
   try {

@@ -440,9 +440,9 @@ __global__ void __launch_bounds__(128)
 k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
            const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
            const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
-           const float *__restrict__ ev_val, int32_t *__restrict__ sc_frame,
-           float *__restrict__ sc_val, float *__restrict__ G2, float *__restrict__ IP,
-           float *__restrict__ IF) {
+           const float *__restrict__ ev_val, const float *__restrict__ fscale,
+           int32_t *__restrict__ sc_frame, float *__restrict__ sc_val, float *__restrict__ G2,
+           float *__restrict__ IP, float *__restrict__ IF) {
   const McPlan *pl = (const McPlan *)plan_g;
   const int D = pl->D, P = pl->P, mode = pl->mode;
   const McArrays ar = mc_arrays(plan_g, D);
@@ -455,7 +455,8 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
     float *val = sc_val + b;
     for (int i = 0; i < n0; i++) {
       idx[i] = ev_frame[b + i];
-      val[i] = ev_val[b + i];
+      // normalize_by_framesum: v / (frameSum[f] / mean) (main.cpp:330-333)
+      val[i] = fscale ? __fdiv_rn(ev_val[b + i], fscale[idx[i]]) : ev_val[b + i];
     }
     int lastIndex = n0;
     for (int gi = 0; gi < pl->nlev; gi++) {
@@ -651,9 +652,14 @@ void run_multitau(Series &s, int mode) {
   s.sc_frame.reserve(ne, st);
   s.sc_val.reserve(ne, st);
   int grid = std::max(1, std::min((P + 127) / 128, sms * 8));
+  const float *fscale = nullptr;
+  if (s.desc.normalize_by_framesum) {
+    prepare_framesum_scale(s);
+    fscale = s.d_fscale.p;
+  }
   k_mt_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p,
-                                   s.ev_frame.p, s.ev_val.p, s.sc_frame.p, s.sc_val.p, s.G2.p,
-                                   s.IP.p, s.IF.p);
+                                   s.ev_frame.p, s.ev_val.p, fscale, s.sc_frame.p, s.sc_val.p,
+                                   s.G2.p, s.IP.p, s.IF.p);
   XG_CHECK_LAUNCH();
   XG_CUDA(cudaEventRecord(s.ev[6], st));
 }

@@ -198,4 +198,23 @@ void run_side_stats(Series &s, const SideOut &out) {
   XG_CUDA(cudaStreamSynchronize(st));
 }
 
+// normalize_by_framesum (main.cpp:314-337): divisor frameSum[F+f] / mean per
+// frame, mean = the float sum of frameSum[F..2F) in frame order / F, computed
+// in float on the host exactly as the reference does; the float multi-tau
+// kernel divides every value by it when it loads the rows.
+void prepare_framesum_scale(Series &s) {
+  const int32_t F = s.F;
+  std::vector<float> fs(2 * (size_t)F + 1);
+  run_side_stats(s, SideOut{nullptr, fs.data(), nullptr, nullptr});
+  float acc = 0.f;
+  for (int32_t f = 0; f < F; f++) acc += fs[(size_t)F + f];
+  const float mean = acc / (float)F;
+  std::vector<float> q((size_t)F + 1, 1.f);
+  for (int32_t f = 0; f < F; f++) q[f] = fs[(size_t)F + f] / mean;
+  s.d_fscale.reserve(q.size(), s.stream);
+  XG_CUDA(cudaMemcpyAsync(s.d_fscale.p, q.data(), sizeof(float) * q.size(),
+                          cudaMemcpyHostToDevice, s.stream));
+  XG_CUDA(cudaStreamSynchronize(s.stream));
+}
+
 }  // namespace xg

@@ -368,7 +368,8 @@ __device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *
 // otherwise each lane merges its own row / sums it in frame order.  Pixels
 // outside the mask get empty rows.
 __global__ void __launch_bounds__(256)
-k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, const int32_t *__restrict__ cnt,
+k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_float,
+                 const int32_t *__restrict__ cnt,
                  const int64_t *__restrict__ row_ptr, const uint8_t *__restrict__ mask,
                  int32_t *__restrict__ fr, float *__restrict__ val, int32_t *__restrict__ row_len,
                  uint8_t *__restrict__ pclass, ClassLists cl, float *__restrict__ pixels_sum,
@@ -439,7 +440,8 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, const int32_t 
     row_len[p] = out;
     pixels_sum[p] = psum;
   }
-  const uint8_t c = keep ? pixel_class(out, integral, total, F, tcap) : (uint8_t)PCLASS_EMPTY;
+  uint8_t c = keep ? pixel_class(out, integral, total, F, tcap) : (uint8_t)PCLASS_EMPTY;
+  if (force_float && c != PCLASS_EMPTY) c = PCLASS_FLOAT;  // values rescaled after the filter
   record_class_warp(has, p, c, out, pclass, cl, stats);
 }
 
@@ -600,7 +602,8 @@ void run_filter_transpose(Series &s) {
   exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
   const int pix_per_block = 256;
   k_merge_classify<<<(P + pix_per_block - 1) / pix_per_block, 256, 0, st>>>(
-      P, s.F, s.desc.avg_frames, s.thread_cap, s.cnt.p, s.row_ptr.p, s.d_mask.p, s.ev_frame.p,
+      P, s.F, s.desc.avg_frames, s.thread_cap, s.desc.normalize_by_framesum, s.cnt.p,
+      s.row_ptr.p, s.d_mask.p, s.ev_frame.p,
       s.ev_val.p,
       s.row_len.p, s.pclass.p, ClassLists{s.wlist.p, s.llist.p, s.flist.p}, s.pixels_sum.p,
       s.stats.p);

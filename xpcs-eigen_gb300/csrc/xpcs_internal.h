@@ -228,6 +228,7 @@ struct Series {
   DBuf<int32_t> d_ppb;      // pixels per static bin
   DBuf<int64_t> side_pos;
   DBuf<float> side_out;
+  DBuf<float> d_fscale;     // normalize_by_framesum: per-frame divisor frameSum/mean
   DBuf<int32_t> sc_frame;   // float-path scratch rows
   DBuf<float> sc_val;
   DBuf<uint8_t> scan_tmp;
@@ -325,6 +326,7 @@ struct SideOut {
   float *part_partial;    // [floor(F / static_window)][S]
 };
 void run_side_stats(Series &s, const SideOut &out);
+void prepare_framesum_scale(Series &s);  // k_side.cu
 
 // Dense frames (k_dense.cu)
 void dense_set_dark(Series &s, const int16_t *dark_host, int32_t ndark);

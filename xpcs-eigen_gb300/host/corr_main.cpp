@@ -140,11 +140,8 @@ int main(int argc, char **argv) {
     const int stride = (int)cfg.get_scalar(entry + "/stride_frames");
     const int avg = (int)cfg.get_scalar(entry + "/avg_frames");
     const int swin = (int)cfg.get_scalar(entry + "/static_mean_window_size");
-    if (cfg.has(entry + "/normalize_by_framesum") &&
-        cfg.get_scalar(entry + "/normalize_by_framesum") != 0) {
-      fprintf(stderr, "corr: normalize_by_framesum is not supported by this build\n");
-      return 1;
-    }
+    const bool by_framesum = cfg.has(entry + "/normalize_by_framesum") &&
+                             cfg.get_scalar(entry + "/normalize_by_framesum") != 0;
     if (cfg.has(entry + "/analysis_type") && cfg.get_string(entry + "/analysis_type") == "Twotime") {
       fprintf(stderr, "corr: the two-time analysis is not supported by this build\n");
       return 1;
@@ -209,6 +206,7 @@ int main(int argc, char **argv) {
     d.lld = lld;
     d.sigma = sigma;
     d.device = fl.device;
+    d.normalize_by_framesum = by_framesum ? 1 : 0;
     xpcs_series *s = nullptr;
     CHECK(xpcs_series_create(&d, &s));
     xpcs_series_info info{};

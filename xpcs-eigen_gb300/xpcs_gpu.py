@@ -74,6 +74,7 @@ class SeriesDesc(C.Structure):
         ("static_window", C.c_int32), ("dqmap", C.POINTER(C.c_int32)),
         ("sqmap", C.POINTER(C.c_int32)), ("flatfield", C.POINTER(C.c_double)),
         ("dense", C.c_int32), ("lld", C.c_float), ("sigma", C.c_float), ("device", C.c_int32),
+        ("normalize_by_framesum", C.c_int32),
     ]
 
 
@@ -174,7 +175,8 @@ class Series:
     """One XPCS series on one GPU (an xpcs_series handle)."""
 
     def __init__(self, width, height, frames, dpl, dqmap, sqmap, flatfield=None, stride=1,
-                 average=1, static_window=None, device=0, dense=False, lld=0.0, sigma=0.0):
+                 average=1, static_window=None, device=0, dense=False, lld=0.0, sigma=0.0,
+                 normalize_by_framesum=False):
         self._dq = np.ascontiguousarray(dqmap, np.int32).ravel()
         self._sq = np.ascontiguousarray(sqmap, np.int32).ravel()
         self._flat = (None if flatfield is None
@@ -189,6 +191,7 @@ class Series:
                        if self._flat is not None else None)
         d.device = device
         d.dense, d.lld, d.sigma = int(dense), lld, sigma
+        d.normalize_by_framesum = int(bool(normalize_by_framesum))
         self._h = C.c_void_p()
         check(lib().xpcs_series_create(C.byref(d), C.byref(self._h)))
         self.width, self.height, self.frames = width, height, frames
