@@ -277,6 +277,85 @@ def framesum_normalize(rows: Rows, frames_sum, frames: int) -> Rows:
     return Rows(rows.row_ptr, rows.frame, value)
 
 
+def _seq_sum_f32(x) -> np.float32:
+    """Left-to-right float32 sum (the reference's `acc += x` loops)."""
+    x = np.ascontiguousarray(x, np.float32)
+    return np.add.accumulate(x)[-1] if x.size else np.float32(0.0)
+
+
+def twotime(qm: QMap, rows: Rows, frames: int, qlist, static_map: bool, average: bool,
+            wsize: int, sort_pixels: bool = False):
+    """Corr::twotime (src/xpcs/corr.cpp:433-924, 1166-1305), float32 throughout
+    in the reference's operation order.
+
+    Smoothing (SmoothingStaticMap / SmoothingSymmetric, :433-547): sg per
+    static bin of the processed q bins (static map) or per processed q bin
+    (symmetric), per frame: the float sum over the bin's pixels in mapping
+    order of the value at that frame, divided by the pixel count; with the
+    average filter sg is then the float mean over frames.  Every value of a
+    pixel of a processed q bin is divided by its sg.
+    Per processed q bin (twotimeQBinThreading, :781-924): for every pixel in
+    mapping order (ascending pixel index with frame threading, :573-779), for
+    every pair of its events j <= k, C[f_j][f_k] += v_j * v_k; then C /= the
+    pixel count.  g2full[ff] = mean of diagonal ff (float sum in order),
+    g2partials[ff][w] = the diagonal's sum over window w of `wsize` entries
+    divided by wsize (ff < wsize, w < (frames - wsize) / wsize).
+    Returns dict(sg, c2t {q: F x F}, g2full [F][Q'], g2partials [wsize][TP][Q'])."""
+    F = frames
+    qset = set(int(q) for q in qlist)
+    value = rows.value.copy()
+    bins = []  # (q, [pixel lists of the bins]) for static map; (q, [plist]) for symmetric
+    for i, q in enumerate(qm.q_ids):
+        if int(q) not in qset:
+            continue
+        lists = [qm.pix[qm.sb_pix_ptr[k]:qm.sb_pix_ptr[k + 1]]
+                 for k in range(qm.q_sb_ptr[i], qm.q_sb_ptr[i + 1])]
+        bins.append((int(q), lists))
+    groups = ([l for _, lists in bins for l in lists] if static_map
+              else [np.concatenate(lists) for _, lists in bins])
+    sg = np.zeros((len(groups), F), np.float32)
+    for g, pl in enumerate(groups):
+        for p in pl:
+            a, b = rows.row_ptr[p], rows.row_ptr[p + 1]
+            sg[g, rows.frame[a:b]] = (sg[g, rows.frame[a:b]] + value[a:b]).astype(np.float32)
+        sg[g] = (sg[g] / np.float32(len(pl))).astype(np.float32)
+    if average:
+        sg = np.array([[_seq_sum_f32(sg[g]) / np.float32(F)] for g in range(len(groups))],
+                      np.float32)
+    for g, pl in enumerate(groups):
+        for p in pl:
+            a, b = rows.row_ptr[p], rows.row_ptr[p + 1]
+            den = sg[g, 0] if average else sg[g, rows.frame[a:b]]
+            value[a:b] = (value[a:b] / den).astype(np.float32)
+    tp = (F - wsize) // wsize
+    c2t, full, part = {}, [], []
+    for q, lists in bins:
+        plist = np.concatenate(lists)
+        if sort_pixels:
+            plist = np.sort(plist)
+        C = np.zeros((F, F), np.float32)
+        for p in plist:
+            a, b = rows.row_ptr[p], rows.row_ptr[p + 1]
+            t, v = rows.frame[a:b], value[a:b]
+            j, k = np.triu_indices(t.size)
+            C[t[j], t[k]] = (C[t[j], t[k]] + (v[j] * v[k]).astype(np.float32)).astype(np.float32)
+        C = (C / np.float32(plist.size)).astype(np.float32)
+        c2t[q] = C
+        g2f = np.zeros(F, np.float32)
+        g2p = np.zeros((wsize, max(tp, 0)), np.float32)
+        for ff in range(F):
+            diag = np.diagonal(C, ff).astype(np.float32)
+            g2f[ff] = _seq_sum_f32(diag) / np.float32(diag.size)
+            if ff < wsize:
+                for w in range(tp):
+                    seg = diag[w * wsize:(w + 1) * wsize]
+                    g2p[ff, w] = _seq_sum_f32(seg) / np.float32(wsize)
+        full.append(g2f)
+        part.append(g2p)
+    return dict(sg=sg, c2t=c2t, g2full=np.stack(full, 1) if full else np.zeros((F, 0), np.float32),
+                g2partials=np.stack(part, 2) if part else np.zeros((wsize, tp, 0), np.float32))
+
+
 def multitau2(rows: Rows, frames: int, dpl: int, mode: int = 0, threads: int = 0):
     """Corr::multiTau2 (src/xpcs/corr.cpp:315). mode 0 = reference, 1 = exact."""
     lv, _ = delays(frames, dpl)

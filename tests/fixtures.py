@@ -12,7 +12,8 @@ import numpy as np
 import oracle
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("twotime"))
+TWOTIME_CASES = sorted(p.stem for p in GOLDEN.glob("twotime*.npz"))
 SPARSE_CASES = [c for c in CASES if not c.startswith("dense")]
 
 
@@ -25,6 +26,22 @@ def load(name: str) -> dict:
     fx["flatfield"] = fx["flat"] if fx["flat"].size else None
     fx["framesum"] = int(fx["framesum"]) if "framesum" in fx else 0
     return fx
+
+
+def load_twotime(name: str) -> dict:
+    with np.load(GOLDEN / f"{name}.npz") as z:
+        fx = {k: z[k] for k in z.files}
+    W, H, F, wsize, frame_threading, static_map, average = (int(x) for x in fx["params"])
+    fx.update(W=W, H=H, F=F, wsize=wsize, frame_threading=bool(frame_threading),
+              static_map=bool(static_map), average=bool(average))
+    return fx
+
+
+def oracle_twotime(fx):
+    qm = oracle.QMap(fx["dqmap"], fx["sqmap"])
+    rows, side = oracle.sparse_filter(qm, fx["nnz"], fx["idx"], fx["val"], fx["F"])
+    return oracle.twotime(qm, rows, fx["F"], fx["qlist"], fx["static_map"], fx["average"],
+                          fx["wsize"], sort_pixels=fx["frame_threading"]), side
 
 
 def oracle_filter(fx):

@@ -204,6 +204,48 @@ def make(name, corr: Path):
     return arrays
 
 
+# two-time cases: (acquisition, q bins to process, smoothing method, filter, window, threading)
+TWOTIME = {
+    "twotime_symmetric_avg": (dict(width=40, height=40, frames=256, n_static=8, n_dynamic=4,
+                                   mean=0.05, tau_min=5, tau_max=40, seed=21, dpl=4),
+                              [1, 3], "symmetric", "Average", 4, False),
+    "twotime_staticmap": (dict(width=48, height=40, frames=300, n_static=12, n_dynamic=6,
+                               mean=0.03, tau_min=3, tau_max=100, seed=22, dpl=4),
+                          [2, 4, 5], "StaticMap", "None", 3, False),
+    "twotime_frame_threading": (dict(width=36, height=36, frames=200, n_static=8, n_dynamic=4,
+                                     mean=0.06, tau_min=4, tau_max=30, seed=23, dpl=4),
+                                [1, 2, 4], "symmetric", "None", 5, True),
+}
+
+
+def make_twotime(name, corr: Path):
+    kw, qlist, method, filt, wsize, frame_threading = TWOTIME[name]
+    acq = xs.Acquisition(**kw)
+    W, H = acq.width, acq.height
+    dq, sq, _, _ = xs.maps(acq)
+    nnz, idx, val = xs.sparse_frames(acq)
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        imm = wd / "frames.imm"
+        refio.write_imm_sparse(imm, H, W, nnz, idx, val)
+        cfg = refio.config_entries(W, H, dq, sq, imm, first=1, last=acq.frames, dpl=acq.dpl,
+                                   twotime=(qlist, method, filt, wsize))
+        cpath = wd / "config.h5"
+        refio.write_xh5c(cpath, cfg)
+        out = refio.run_reference(corr, cpath, wd, g2out=False,
+                                  extra_args=["--frame_threading"] if frame_threading else [])
+    arrays = dict(nnz=nnz, idx=idx, val=val, dqmap=dq, sqmap=sq,
+                  params=np.array([W, H, acq.frames, wsize, 1 if frame_threading else 0,
+                                   1 if method.lower() == "staticmap" else 0,
+                                   1 if filt.lower() == "average" else 0], np.int64),
+                  qlist=np.asarray(qlist, np.int32))
+    for k, v in out.items():
+        if k != "_stdout":
+            arrays["ref_" + k.replace("-", "_")] = v
+    np.savez_compressed(HERE / f"{name}.npz", **arrays)
+    return arrays
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -218,6 +260,12 @@ def main():
         arr = make(name, corr)
         G2 = arr["ref_G2"]
         print(f"{name}: D={G2.shape[0]} P={G2.shape[1]} -> {name}.npz")
+    for name in TWOTIME:
+        if a.only and name != a.only:
+            continue
+        arr = make_twotime(name, corr)
+        print(f"{name}: " + ", ".join(f"{k} {v.shape}" for k, v in arr.items()
+                                      if k.startswith("ref_")) + f" -> {name}.npz")
 
 
 if __name__ == "__main__":

@@ -104,7 +104,7 @@ def write_imm_dense(path, rows, cols, frames: np.ndarray, clock=None, ticks=None
 def config_entries(width, height, dqmap, sqmap, imm_path, first=1, last=None, dpl=4,
                    stride=1, average=1, static_window=None, compression=True, flat=None,
                    dark=(0, 0), lld=0.0, sigma=0.0, entry="/xpcs", output="/exchange",
-                   normalize_by_framesum=0) -> dict:
+                   normalize_by_framesum=0, twotime=None) -> dict:
     """The /xpcs and /measurement datasets Configuration::init reads.  Scalars
     are int32 (getInteger reads into a 4-byte int, quirk Q10); tables are 2-D."""
     assert last is not None
@@ -144,6 +144,13 @@ def config_entries(width, height, dqmap, sqmap, imm_path, first=1, last=None, dp
     if flat is not None:
         e["/measurement/instrument/detector/flatfield"] = np.asarray(flat, np.float64).reshape(
             height, width)
+    if twotime is not None:  # (q bins to process, smoothing method, smoothing filter, window)
+        qlist, method, filt, wsize = twotime
+        e[entry + "/analysis_type"] = "Twotime"
+        e[entry + "/smoothing_method"] = method
+        e[entry + "/smoothing_filter"] = filt
+        e[entry + "/qphi_bin_to_process"] = np.asarray(qlist, np.int64).reshape(-1, 1)
+        e[entry + "/twotime2onetime_window_size"] = np.int32(wsize)
     if dark[0] != dark[1]:
         e[entry + "/lld"] = np.float32(lld)
         e[entry + "/sigma"] = np.float32(sigma)
@@ -151,14 +158,14 @@ def config_entries(width, height, dqmap, sqmap, imm_path, first=1, last=None, dp
 
 
 def run_reference(corr: Path, config: Path, workdir: Path, threads: int | None = None,
-                  g2out: bool = True, timeout: int = 3600) -> dict:
+                  g2out: bool = True, timeout: int = 3600, extra_args=()) -> dict:
     """Run the reference `corr` on an XH5C config; return its /exchange datasets
     and the stdout (stage timers)."""
     import os
     env = dict(os.environ)
     if threads:
         env["OMP_NUM_THREADS"] = str(threads)
-    args = [str(corr), str(config)] + (["--g2out"] if g2out else [])
+    args = [str(corr), str(config)] + (["--g2out"] if g2out else []) + list(extra_args)
     r = subprocess.run(args, cwd=workdir, env=env, capture_output=True, text=True,
                        timeout=timeout)
     if r.returncode != 0:
