@@ -250,6 +250,41 @@ int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *frame, const f
                            int32_t delays_per_level, int32_t mode, float *G2, float *IP,
                            float *IF, void *stream);
 
+/* Two-time correlation (Corr::twotime, corr.cpp:560-924, with the smoothing of
+ * corr.cpp:433-547 and 1166-1305) of the ingested frames, per processed q bin:
+ * C2T [F][F] (upper triangle, zeros below, as the reference writes
+ * C2T_all/g2_<q>), g2full [F][Q'] and g2partials [window][P'][Q'] with
+ * P' = (F - window) / window, and the smoothing array sg [G][F] (static-map
+ * smoothing: G = static bins of the processed q bins; symmetric: G = Q') or
+ * [G][1] with the average filter.  Q' = processed q bins present in the
+ * partition map, in mapping order.
+ * mode REFERENCE: float32 in the reference's operation order (bit-identical to
+ * its outputs); the pixel order of the sums is the mapping order
+ * (twotimeQBinThreading) or ascending pixel index with frame_threading
+ * (twotimeFrameThreading).  Runs the filter/transpose itself. */
+typedef struct {
+  const int32_t *qbins;     /* /xpcs/qphi_bin_to_process */
+  int32_t nqbins;
+  int32_t static_map;       /* 1: smoothing_method StaticMap, 0: symmetric */
+  int32_t average;          /* 1: smoothing_filter Average */
+  int32_t window;           /* /xpcs/twotime2onetime_window_size (>= 1) */
+  int32_t frame_threading;  /* --frame_threading */
+} xpcs_twotime_desc;
+typedef struct {
+  int32_t qbins;            /* Q' */
+  int32_t frames;           /* F */
+  int32_t window;
+  int32_t partials;         /* (F - window) / window */
+  int32_t sg_rows, sg_cols;
+} xpcs_twotime_info;
+int xpcs_twotime(xpcs_series *s, const xpcs_twotime_desc *d, int32_t mode,
+                 xpcs_twotime_info *info);
+/* Copies the last two-time results; any pointer may be NULL.  qbins [Q'],
+ * sg [sg_rows][sg_cols], c2t [Q'][F][F], g2full [F][Q'], g2partials
+ * [window][partials][Q']. */
+int xpcs_get_twotime(xpcs_series *s, int32_t *qbins, float *sg, float *c2t, float *g2full,
+                     float *g2partials);
+
 /* Batches: no counterpart in the reference, which runs one series per
  * process.  A batch holds several series handles of one device (uneven frame
  * counts, detector sizes and occupancies) and runs the whole path for all of

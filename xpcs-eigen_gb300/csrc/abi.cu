@@ -112,6 +112,11 @@ void free_series(Series *s) {
     s->n_part.release(st);
     s->side_pos.release(st);
     s->side_out.release(st);
+    DBuf<int32_t> *tti[] = {&s->tt_row_pix, &s->tt_row_grp, &s->tt_grp_ptr, &s->tt_order};
+    for (auto *b : tti) b->release(st);
+    DBuf<float> *ttf[] = {&s->tt_V, &s->tt_sg, &s->tt_sga, &s->tt_C, &s->tt_full, &s->tt_part};
+    for (auto *b : ttf) b->release(st);
+    s->d_fscale.release(st);
     s->n_g2.release(st);
     s->n_se.release(st);
     s->keyA.release(st);
@@ -442,6 +447,46 @@ int xpcs_side_stats(xpcs_series *h, float *pixel_sum, float *frame_sum,
     DeviceGuard g(s.device);
     sync_and_check(s);
     run_side_stats(s, SideOut{pixel_sum, frame_sum, partition_mean_total, partition_mean_partial});
+  });
+}
+
+int xpcs_twotime(xpcs_series *h, const xpcs_twotime_desc *d, int32_t mode,
+                 xpcs_twotime_info *info) {
+  return guarded([&] {
+    need(h && d, "null argument");
+    need(mode == XPCS_MODE_REFERENCE, "two-time supports REFERENCE mode");
+    need(d->nqbins >= 0 && (d->nqbins == 0 || d->qbins), "bad q-bin list");
+    need(d->window >= 1, "window must be >= 1");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    TwoTimeReq req;
+    req.qbins.assign(d->qbins, d->qbins + d->nqbins);
+    req.static_map = d->static_map != 0;
+    req.average = d->average != 0;
+    req.window = d->window;
+    req.frame_threading = d->frame_threading != 0;
+    run_filter_transpose(s);
+    run_twotime(s, req);
+    sync_and_check(s);
+    if (info) {
+      info->qbins = (int32_t)s.tt.qbins.size();
+      info->frames = s.tt.frames;
+      info->window = s.tt.window;
+      info->partials = s.tt.partials;
+      info->sg_rows = s.tt.sg_rows;
+      info->sg_cols = s.tt.sg_cols;
+    }
+  });
+}
+
+int xpcs_get_twotime(xpcs_series *h, int32_t *qbins, float *sg, float *c2t, float *g2full,
+                     float *g2partials) {
+  return guarded([&] {
+    need(h, "null handle");
+    Series &s = *(Series *)h;
+    if (!s.tt.ready) throw Error(XPCS_ERR_STATE, "xpcs_twotime has not run");
+    DeviceGuard g(s.device);
+    get_twotime(s, qbins, sg, c2t, g2full, g2partials);
   });
 }
 

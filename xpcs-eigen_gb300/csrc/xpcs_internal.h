@@ -174,6 +174,18 @@ struct DevStats {
   unsigned long long events;
 };
 
+// -------------------------------------------------------------- two-time
+
+struct TwoTimeReq {
+  std::vector<int32_t> qbins;  // q bins to process
+  int32_t static_map = 0, average = 0, window = 1, frame_threading = 0;
+};
+struct TwoTimeOut {
+  bool ready = false;
+  std::vector<int32_t> qbins;  // processed q bins present in the mapping, in mapping order
+  int32_t frames = 0, window = 1, partials = 0, sg_rows = 0, sg_cols = 0;
+};
+
 // --------------------------------------------------------------- a series
 
 struct Series {
@@ -253,6 +265,11 @@ struct Series {
   DBuf<double> n_g2, n_se;
   DBuf<float> n_g2f, n_sef;
 
+  // two-time
+  TwoTimeOut tt;
+  DBuf<int32_t> tt_row_pix, tt_row_grp, tt_grp_ptr, tt_order;
+  DBuf<float> tt_V, tt_sg, tt_sga, tt_C, tt_full, tt_part;
+
   // tracer
   cudaEvent_t ev[12] = {};
   int32_t launches = 0;     // kernels launched since the last xpcs_multitau began
@@ -327,6 +344,10 @@ struct SideOut {
 };
 void run_side_stats(Series &s, const SideOut &out);
 void prepare_framesum_scale(Series &s);  // k_side.cu
+
+// Two-time (k_twotime.cu): needs the event lists of run_filter_transpose
+void run_twotime(Series &s, const TwoTimeReq &req);
+void get_twotime(Series &s, int32_t *qbins, float *sg, float *c2t, float *g2full, float *g2part);
 
 // Dense frames (k_dense.cu)
 void dense_set_dark(Series &s, const int16_t *dark_host, int32_t ndark);

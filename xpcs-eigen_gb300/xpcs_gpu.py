@@ -37,7 +37,7 @@ EXPORTS = [
     "xpcs_batch_create", "xpcs_batch_run", "xpcs_batch_stats", "xpcs_batch_destroy",
     "xpcs_autotune", "xpcs_server_create", "xpcs_server_destroy", "xpcs_server_submit",
     "xpcs_server_push_sparse", "xpcs_server_finish", "xpcs_server_state", "xpcs_server_result",
-    "xpcs_server_release", "xpcs_server_get_stats",
+    "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
 ]
 
 BATCH_F64 = 1
@@ -45,6 +45,17 @@ BATCH_F32 = 2
 BATCH_AUTOTUNE = 4
 
 NOALLOC_MAX_EVENTS = 4194304
+
+
+class TwoTimeDesc(C.Structure):
+    _fields_ = [("qbins", C.POINTER(C.c_int32)), ("nqbins", C.c_int32),
+                ("static_map", C.c_int32), ("average", C.c_int32), ("window", C.c_int32),
+                ("frame_threading", C.c_int32)]
+
+
+class TwoTimeInfo(C.Structure):
+    _fields_ = [("qbins", C.c_int32), ("frames", C.c_int32), ("window", C.c_int32),
+                ("partials", C.c_int32), ("sg_rows", C.c_int32), ("sg_cols", C.c_int32)]
 
 
 class ServerStats(C.Structure):
@@ -141,6 +152,9 @@ def lib() -> C.CDLL:
         L.xpcs_server_result.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 5
         L.xpcs_server_release.argtypes = [C.c_void_p, C.c_int64]
         L.xpcs_server_get_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+        L.xpcs_twotime.argtypes = [C.c_void_p, C.POINTER(TwoTimeDesc), C.c_int32,
+                                   C.POINTER(TwoTimeInfo)]
+        L.xpcs_get_twotime.argtypes = [C.c_void_p] + [C.c_void_p] * 5
         L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                              C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -281,6 +295,25 @@ class Series:
                    np.empty(shp, np.float32) if f32 else None)
         check(lib().xpcs_normalize(self._h, *[_ptr(a) for a in out]))
         return out
+
+    def twotime(self, qbins, static_map=False, average=False, window=1, frame_threading=False,
+                mode=MODE_REFERENCE) -> dict:
+        """xpcs_twotime + xpcs_get_twotime: sg, C2T per q bin, g2full, g2partials."""
+        q = np.ascontiguousarray(qbins, np.int32)
+        d = TwoTimeDesc(q.ctypes.data_as(C.POINTER(C.c_int32)), q.size, int(static_map),
+                        int(average), int(window), int(frame_threading))
+        info = TwoTimeInfo()
+        check(lib().xpcs_twotime(self._h, C.byref(d), mode, C.byref(info)))
+        Q, F = info.qbins, info.frames
+        qs = np.empty(Q, np.int32)
+        sg = np.empty((info.sg_rows, info.sg_cols), np.float32)
+        c2t = np.empty((Q, F, F), np.float32)
+        full = np.empty((F, Q), np.float32)
+        part = np.empty((info.window, info.partials, Q), np.float32)
+        check(lib().xpcs_get_twotime(self._h, _ptr(qs), _ptr(sg), _ptr(c2t), _ptr(full),
+                                     _ptr(part)))
+        return dict(qbins=qs, sg=sg, c2t={int(k): c2t[i] for i, k in enumerate(qs)},
+                    g2full=full, g2partials=part)
 
     def autotune(self, mode=MODE_REFERENCE) -> int:
         """xpcs_autotune: pick this series' thread-kernel row capacity; returns it."""
