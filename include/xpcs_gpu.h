@@ -183,7 +183,7 @@ int xpcs_normalize(xpcs_series *s, double *g2, double *stderr_, float *g2_f32,
  *   partition_mean_total   partition-mean-total, float32 [total_static]
  *   partition_mean_partial partition-mean-partial, float32
  *                          [frames / static_window][total_static]
- * Any pointer may be NULL.  Needs xpcs_multitau to have run. */
+ * Any pointer may be NULL.  Needs xpcs_multitau or xpcs_twotime to have run. */
 int xpcs_side_stats(xpcs_series *s, float *pixel_sum, float *frame_sum,
                     float *partition_mean_total, float *partition_mean_partial);
 

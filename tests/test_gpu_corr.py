@@ -10,7 +10,7 @@ import pytest
 
 import build
 import refio
-from fixtures import CASES, load, same_bits_nan
+from fixtures import CASES, TWOTIME_CASES, load, load_twotime, same_bits_nan
 
 DATASETS = ["G2", "IP", "IF", "norm-0-g2", "norm-0-stderr", "pixelSum", "frameSum",
             "partition-mean-total", "partition-mean-partial", "timestamp_clock",
@@ -63,6 +63,30 @@ def test_corr_matches_reference_outputs(corr, case, tmp_path):
         assert out["DarkAvg"].size == n and out["DarkStd"].size == n
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", TWOTIME_CASES)
+def test_corr_twotime_matches_reference_outputs(corr, case, tmp_path):
+    fx = load_twotime(case)
+    imm = tmp_path / "frames.imm"
+    refio.write_imm_sparse(imm, fx["H"], fx["W"], fx["nnz"], fx["idx"], fx["val"])
+    tt = (fx["qlist"], "StaticMap" if fx["static_map"] else "symmetric",
+          "Average" if fx["average"] else "None", fx["wsize"])
+    cfg = tmp_path / "analysis.h5"
+    refio.write_xh5c(cfg, refio.config_entries(fx["W"], fx["H"], fx["dqmap"], fx["sqmap"], imm,
+                                               first=1, last=fx["F"], dpl=4, twotime=tt))
+    args = [str(corr), str(cfg)] + (["--frame_threading"] if fx["frame_threading"] else [])
+    r = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = {k.split("/")[-1]: v for k, v in refio.read_xh5c(cfg).items() if k.startswith("/exchange/")}
+    names = ["sg", "g2full", "g2partials", "pixelSum", "frameSum"] + \
+        [k[4:] for k in fx if k.startswith("ref_g2_")]
+    for name in names:
+        ref = fx["ref_" + name]
+        assert name in out, name
+        assert same_bits_nan(np.asarray(out[name]).reshape(ref.shape), ref), name
+    assert "tau" not in out
+
+
 def test_corr_rejects_unsupported_reader_flags(corr, tmp_path):
     r = subprocess.run([str(corr), str(tmp_path / "x.h5"), "--ufxc"], capture_output=True,
                        text=True)
@@ -74,9 +98,12 @@ def test_corr_rejects_unsupported_analyses(corr, tmp_path):
     cfg = _write_inputs(fx, tmp_path)
     ent = refio.read_xh5c(cfg)
     ent["/xpcs/analysis_type"] = "Twotime"
+    ent["/xpcs/smoothing_method"] = "boxcar"
+    ent["/xpcs/smoothing_filter"] = "None"
+    ent["/xpcs/qphi_bin_to_process"] = np.ones((1, 1), np.int64)
     refio.write_xh5c(cfg, ent)
     r = subprocess.run([str(corr), str(cfg)], capture_output=True, text=True)
-    assert r.returncode != 0 and "two-time" in r.stderr
+    assert r.returncode != 0 and "Smoothing method is not valid" in r.stderr
 
 
 def test_corr_reads_config_and_frames_without_a_device(corr, tmp_path):

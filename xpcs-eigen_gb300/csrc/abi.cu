@@ -229,6 +229,7 @@ int xpcs_series_reset(xpcs_series *h) {
     s.frame_off_dirty = true;
     s.have_multitau = false;
     s.have_norm64 = s.have_norm32 = false;
+    s.tt.ready = false;
     s.timed_h2d = false;
     s.h2d_ms_acc = 0.f;
     s.generation++;
@@ -287,6 +288,7 @@ static void ingest_common(Series &s, const int32_t *idx, const int16_t *val, con
   s.raw_frames += nframes;
   s.frame_off_dirty = true;
   s.have_multitau = false;
+  s.tt.ready = false;
   s.generation++;
 }
 
@@ -335,6 +337,7 @@ static int ingest_dense_common(xpcs_series *h, const int16_t *frames, int32_t nf
     dense_ingest(s, frames, nframes, dev);
     s.generation++;
     s.have_multitau = false;
+    s.tt.ready = false;
     XG_CUDA(cudaEventRecord(s.ev[1], s.stream));
   });
 }
@@ -443,7 +446,8 @@ int xpcs_side_stats(xpcs_series *h, float *pixel_sum, float *frame_sum,
   return guarded([&] {
     need(h, "null handle");
     Series &s = *(Series *)h;
-    if (!s.have_multitau) throw Error(XPCS_ERR_STATE, "xpcs_multitau has not run");
+    if (!s.have_multitau && !s.tt.ready)
+      throw Error(XPCS_ERR_STATE, "neither xpcs_multitau nor xpcs_twotime has run");
     DeviceGuard g(s.device);
     sync_and_check(s);
     run_side_stats(s, SideOut{pixel_sum, frame_sum, partition_mean_total, partition_mean_partial});

@@ -5,14 +5,16 @@
 // default) names the IMM frame file; the results are written into the same
 // file under the configured output group:
 //   pixelSum, frameSum, partition-mean-total, partition-mean-partial,
-//   partition_norm_factor, timestamp_clock, timestamp_tick, tau,
-//   norm-0-g2, norm-0-stderr, and with --g2out G2/IP/IF, with --darkout
-//   DarkAvg/DarkStd.
+//   partition_norm_factor, timestamp_clock, timestamp_tick, then for the
+//   multi-tau analysis tau, norm-0-g2, norm-0-stderr (and with --g2out
+//   G2/IP/IF), for the two-time analysis (analysis_type Twotime) sg,
+//   C2T_all/g2_<q>, g2full, g2partials; with --darkout DarkAvg/DarkStd.
 // The analysis file is read and written in the XH5C container format
 // (xh5c.h).  Extra flags: --mode=exact (lookup over the live prefix only),
 // --fp64 (write the float64 normalisation), --device=N, --block=N (frames
 // per ingest call).
 #include <algorithm>
+#include <cctype>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -29,7 +31,7 @@
 namespace {
 
 struct Flags {
-  bool g2out = false, darkout = false, fp64 = false;
+  bool g2out = false, darkout = false, fp64 = false, frame_threading = false;
   int frameout = 0, device = 0, block = 512;
   std::string imm, inpath, outpath, exchange, entry, mode = "reference";
   std::vector<std::string> positional;
@@ -63,8 +65,8 @@ bool parse(int argc, char **argv, Flags &f, std::string &err) {
     else if (k == "exchange") f.exchange = v;
     else if (k == "entry") f.entry = v;
     else if (k == "mode") f.mode = v;
-    else if (k == "ufxc" || k == "rigaku" || k == "hdf5" || k == "frame_threading" ||
-             k == "transposed") {
+    else if (k == "frame_threading") boolean(f.frame_threading);
+    else if (k == "ufxc" || k == "rigaku" || k == "hdf5" || k == "transposed") {
       err = "--" + k + " selects a reader or analysis outside the multi-tau IMM path";
       return false;
     } else {
@@ -73,6 +75,11 @@ bool parse(int argc, char **argv, Flags &f, std::string &err) {
     }
   }
   return true;
+}
+
+std::string lower(std::string s) {
+  for (auto &c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
 }
 
 struct Timer {
@@ -94,6 +101,25 @@ struct Timer {
       return 1;                                                         \
     }                                                                   \
   } while (0)
+
+// The filter's side datasets (main.cpp:314-411): pixelSum, frameSum, the
+// partition means, the normalisation factor and the timestamps.
+int write_side(xh5c::File &cfg, xpcs_series *s, const std::string &g, int W, int H, int F,
+               int swin, int S, float nf, const std::vector<double> &clock,
+               const std::vector<double> &ticks, int real) {
+  const int nwin = swin > 0 ? F / swin : 0;
+  std::vector<float> psum((size_t)W * H), fsum(2 * (size_t)F), ptot(S), ppart((size_t)nwin * S);
+  const int rc = xpcs_side_stats(s, psum.data(), fsum.data(), ptot.data(), ppart.data());
+  if (rc != XPCS_OK) return rc;
+  cfg.put(g + "pixelSum", xh5c::F32, {(uint64_t)H, (uint64_t)W}, psum.data());
+  cfg.put(g + "frameSum", xh5c::F32, {2, (uint64_t)F}, fsum.data());
+  cfg.put(g + "partition-mean-total", xh5c::F32, {1, (uint64_t)S}, ptot.data());
+  cfg.put(g + "partition-mean-partial", xh5c::F32, {(uint64_t)nwin, (uint64_t)S}, ppart.data());
+  cfg.put(g + "partition_norm_factor", xh5c::F32, {1, 1}, &nf);
+  cfg.put(g + "timestamp_clock", xh5c::F64, {2, (uint64_t)real}, clock.data());
+  cfg.put(g + "timestamp_tick", xh5c::F64, {2, (uint64_t)real}, ticks.data());
+  return XPCS_OK;
+}
 
 }  // namespace
 
@@ -142,9 +168,26 @@ int main(int argc, char **argv) {
     const int swin = (int)cfg.get_scalar(entry + "/static_mean_window_size");
     const bool by_framesum = cfg.has(entry + "/normalize_by_framesum") &&
                              cfg.get_scalar(entry + "/normalize_by_framesum") != 0;
-    if (cfg.has(entry + "/analysis_type") && cfg.get_string(entry + "/analysis_type") == "Twotime") {
-      fprintf(stderr, "corr: the two-time analysis is not supported by this build\n");
-      return 1;
+    // two-time options (configuration.cpp:150-151, 216-231; main.cpp:161-164)
+    const bool twotime = cfg.has(entry + "/analysis_type") &&
+                         cfg.get_string(entry + "/analysis_type") == "Twotime";
+    xpcs_twotime_desc tdesc{};
+    std::vector<int32_t> tq;
+    if (twotime) {
+      const std::string method = lower(cfg.get_string(entry + "/smoothing_method"));
+      if (method != "staticmap" && method != "symmetric") {
+        fprintf(stderr, "Smoothing method is not valid\n");
+        return 1;
+      }
+      tdesc.static_map = method == "staticmap";
+      tdesc.average = lower(cfg.get_string(entry + "/smoothing_filter")) == "average";
+      for (double q : cfg.get_f64(entry + "/qphi_bin_to_process")) tq.push_back((int32_t)q);
+      tdesc.qbins = tq.data();
+      tdesc.nqbins = (int32_t)tq.size();
+      tdesc.window = cfg.has(entry + "/twotime2onetime_window_size")
+                         ? (int32_t)cfg.get_scalar(entry + "/twotime2onetime_window_size")
+                         : 1;
+      tdesc.frame_threading = fl.frame_threading;
     }
     int darks = 0;
     float lld = 0.f, sigma = 0.f;
@@ -244,30 +287,41 @@ int main(int argc, char **argv) {
       }
       if (got < want) fprintf(stderr, "corr: warning: IMM file ends after %d of %d frames\n", got, want);
     }
-    {
-      Timer t("Computing G2 MultiTau");
-      CHECK(xpcs_multitau(s, fl.mode == "exact" ? XPCS_MODE_EXACT : XPCS_MODE_REFERENCE));
-      CHECK(xpcs_synchronize(s));
-    }
-    const int nwin = swin > 0 ? F / swin : 0;
-    std::vector<float> psum(P), fsum(2 * (size_t)F), ptot(S), ppart((size_t)nwin * S);
-    CHECK(xpcs_side_stats(s, psum.data(), fsum.data(), ptot.data(), ppart.data()));
     const std::string g = output + "/";
-    cfg.put(g + "pixelSum", xh5c::F32, {(uint64_t)H, (uint64_t)W}, psum.data());
-    cfg.put(g + "frameSum", xh5c::F32, {2, (uint64_t)F}, fsum.data());
-    cfg.put(g + "partition-mean-total", xh5c::F32, {1, (uint64_t)S}, ptot.data());
-    cfg.put(g + "partition-mean-partial", xh5c::F32, {(uint64_t)nwin, (uint64_t)S}, ppart.data());
-    float nfv = nf;
-    cfg.put(g + "partition_norm_factor", xh5c::F32, {1, 1}, &nfv);
-    cfg.put(g + "timestamp_clock", xh5c::F64, {2, (uint64_t)real}, clock.data());
-    cfg.put(g + "timestamp_tick", xh5c::F64, {2, (uint64_t)real}, ticks.data());
-    std::vector<int32_t> lv(D), tau(D);
-    int32_t nd = 0;
-    CHECK(xpcs_delay_schedule(F, dpl, lv.data(), tau.data(), D, &nd));
-    std::vector<float> tauf(D);
-    for (int k = 0; k < D; k++) tauf[k] = (float)tau[k];
-    cfg.put(g + "tau", xh5c::F32, {1, (uint64_t)D}, tauf.data());
-    {
+    if (twotime) {
+      xpcs_twotime_info ti{};
+      {
+        Timer t("Computing G2 TwoTimes");
+        CHECK(xpcs_twotime(s, &tdesc, XPCS_MODE_REFERENCE, &ti));
+      }
+      CHECK(write_side(cfg, s, g, W, H, F, swin, S, nf, clock, ticks, real));
+      const uint64_t NQ = (uint64_t)ti.qbins, FF = (uint64_t)ti.frames;
+      std::vector<int32_t> qs(NQ);
+      std::vector<float> sg((size_t)ti.sg_rows * ti.sg_cols), c2t(NQ * FF * FF), full(FF * NQ),
+          part((size_t)ti.window * ti.partials * NQ);
+      CHECK(xpcs_get_twotime(s, qs.data(), sg.data(), c2t.data(), full.data(), part.data()));
+      cfg.put(g + "sg", xh5c::F32, {(uint64_t)ti.sg_rows, (uint64_t)ti.sg_cols}, sg.data());
+      for (uint64_t i = 0; i < NQ; i++) {
+        char name[32];
+        snprintf(name, sizeof(name), "g2_%05d", qs[i]);
+        cfg.put(g + "C2T_all/" + name, xh5c::F32, {FF, FF}, c2t.data() + i * FF * FF);
+      }
+      cfg.put(g + "g2full", xh5c::F32, {FF, NQ}, full.data());
+      cfg.put(g + "g2partials", xh5c::F32, {(uint64_t)ti.window, (uint64_t)ti.partials, NQ},
+              part.data());
+    } else {
+      {
+        Timer t("Computing G2 MultiTau");
+        CHECK(xpcs_multitau(s, fl.mode == "exact" ? XPCS_MODE_EXACT : XPCS_MODE_REFERENCE));
+        CHECK(xpcs_synchronize(s));
+      }
+      CHECK(write_side(cfg, s, g, W, H, F, swin, S, nf, clock, ticks, real));
+      std::vector<int32_t> lv(D), tau(D);
+      int32_t nd = 0;
+      CHECK(xpcs_delay_schedule(F, dpl, lv.data(), tau.data(), D, &nd));
+      std::vector<float> tauf(D);
+      for (int k = 0; k < D; k++) tauf[k] = (float)tau[k];
+      cfg.put(g + "tau", xh5c::F32, {1, (uint64_t)D}, tauf.data());
       Timer t("Normalizing Data");
       std::vector<double> g2d((size_t)D * Q), sed((size_t)D * Q);
       std::vector<float> g2f((size_t)D * Q), sef((size_t)D * Q);
