@@ -261,7 +261,16 @@ int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *frame, const f
  * mode REFERENCE: float32 in the reference's operation order (bit-identical to
  * its outputs); the pixel order of the sums is the mapping order
  * (twotimeQBinThreading) or ascending pixel index with frame_threading
- * (twotimeFrameThreading).  Runs the filter/transpose itself. */
+ * (twotimeFrameThreading).
+ * mode EXACT: needs integer counts; the Gram products of the raw counts of
+ * every smoothing group are exact integers, computed on the tensor cores
+ * (fp16 operands, fp32 accumulation: exact while the counts are <= 2048 and
+ * sum over pixels of (max count)^2 < 2^24; other groups use an int64 CUDA-core
+ * Gram), and the smoothing and reductions are applied in float64 (rounded to
+ * float32 on output).  XPCS_TWOTIME_EXACT_CUDA_CORES computes the same with
+ * the int64 CUDA-core Gram for every group.
+ * Runs the filter/transpose itself. */
+#define XPCS_TWOTIME_EXACT_CUDA_CORES 2
 typedef struct {
   const int32_t *qbins;     /* /xpcs/qphi_bin_to_process */
   int32_t nqbins;

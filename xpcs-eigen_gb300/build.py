@@ -31,7 +31,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompile
                      "-I", str(INCLUDE), "-I", str(CSRC)]
 GPU_SOURCES = ["abi.cu", "scan.cu", "k_transpose.cu", "k_multitau.cu", "k_normalize.cu",
                "qmap.cpp", "noalloc.cu", "k_dense.cu", "k_side.cu", "batch.cu",
-               "server.cpp", "k_twotime.cu"]
+               "server.cpp", "k_twotime.cu", "k_twotime_tc.cu"]
 
 LIB_GPU = BUILD / "libxpcs_gpu.so"
 LIB_SYNTH = BUILD / "libxpcs_synth.so"

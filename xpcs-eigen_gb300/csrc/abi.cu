@@ -117,6 +117,16 @@ void free_series(Series *s) {
     DBuf<float> *ttf[] = {&s->tt_V, &s->tt_sg, &s->tt_sga, &s->tt_C, &s->tt_full, &s->tt_part};
     for (auto *b : ttf) b->release(st);
     s->d_fscale.release(st);
+    s->tt_err.release(st);
+    s->tt_flags.release(st);
+    s->tt_XT.release(st);
+    s->tt_S.release(st);
+    s->tt_bound.release(st);
+    s->tt_Gi.release(st);
+    s->tt_sgd.release(st);
+    s->tt_Cacc.release(st);
+    s->tt_Cq.release(st);
+    s->tt_Gf.release(st);
     s->n_g2.release(st);
     s->n_se.release(st);
     s->keyA.release(st);
@@ -458,7 +468,9 @@ int xpcs_twotime(xpcs_series *h, const xpcs_twotime_desc *d, int32_t mode,
                  xpcs_twotime_info *info) {
   return guarded([&] {
     need(h && d, "null argument");
-    need(mode == XPCS_MODE_REFERENCE, "two-time supports REFERENCE mode");
+    need(mode == XPCS_MODE_REFERENCE || mode == XPCS_MODE_EXACT ||
+             mode == XPCS_TWOTIME_EXACT_CUDA_CORES,
+         "unknown two-time mode");
     need(d->nqbins >= 0 && (d->nqbins == 0 || d->qbins), "bad q-bin list");
     need(d->window >= 1, "window must be >= 1");
     Series &s = *(Series *)h;
@@ -470,7 +482,8 @@ int xpcs_twotime(xpcs_series *h, const xpcs_twotime_desc *d, int32_t mode,
     req.window = d->window;
     req.frame_threading = d->frame_threading != 0;
     run_filter_transpose(s);
-    run_twotime(s, req);
+    run_twotime(s, req, mode == XPCS_MODE_REFERENCE ? XPCS_MODE_REFERENCE : XPCS_MODE_EXACT,
+                mode == XPCS_TWOTIME_EXACT_CUDA_CORES);
     sync_and_check(s);
     if (info) {
       info->qbins = (int32_t)s.tt.qbins.size();

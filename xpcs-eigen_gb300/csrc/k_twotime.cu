@@ -152,7 +152,7 @@ __global__ void k_tt_diag(int32_t Q, int32_t F, int32_t window, int32_t tp,
 
 }  // namespace
 
-void run_twotime(Series &s, const TwoTimeReq &req) {
+void run_twotime(Series &s, const TwoTimeReq &req, int mode, bool force_i64) {
   cudaStream_t st = s.stream;
   const QMap &qm = s.qmap;
   const int32_t F = s.F;
@@ -162,25 +162,45 @@ void run_twotime(Series &s, const TwoTimeReq &req) {
   o.window = req.window;
   o.partials = req.window > 0 ? std::max(0, (F - req.window) / req.window) : 0;
   // rows of the processed q bins in mapping order; smoothing groups; q row ranges
-  std::vector<int32_t> row_pix, row_grp, grp_ptr{0}, q_ptr{0};
+  TwoTimeLayout lay;
   for (int32_t i = 0; i < qm.nq(); i++) {
     const int32_t q = qm.q_ids[i];
     if (std::find(req.qbins.begin(), req.qbins.end(), q) == req.qbins.end()) continue;
     for (int32_t e = qm.q_entry_ptr[i]; e < qm.q_entry_ptr[i + 1]; e++) {
       for (int32_t k = qm.entry_pix_ptr[e]; k < qm.entry_pix_ptr[e + 1]; k++) {
-        row_pix.push_back(qm.pix[k]);
-        row_grp.push_back((int32_t)grp_ptr.size() - 1);
+        lay.row_pix.push_back(qm.pix[k]);
+        lay.row_grp.push_back((int32_t)lay.grp_ptr.size() - 1);
       }
-      if (req.static_map) grp_ptr.push_back((int32_t)row_pix.size());
+      if (req.static_map) lay.grp_ptr.push_back((int32_t)lay.row_pix.size());
     }
-    if (!req.static_map) grp_ptr.push_back((int32_t)row_pix.size());
-    q_ptr.push_back((int32_t)row_pix.size());
+    if (!req.static_map) lay.grp_ptr.push_back((int32_t)lay.row_pix.size());
+    lay.q_ptr.push_back((int32_t)lay.row_pix.size());
+    lay.q_grp_end.push_back((int32_t)lay.grp_ptr.size() - 1);
     o.qbins.push_back(q);
   }
+  const std::vector<int32_t> &row_pix = lay.row_pix, &row_grp = lay.row_grp,
+                             &grp_ptr = lay.grp_ptr, &q_ptr = lay.q_ptr;
   const int32_t R = (int32_t)row_pix.size(), G = (int32_t)grp_ptr.size() - 1,
                 Q = (int32_t)o.qbins.size();
   o.sg_rows = G;
   o.sg_cols = req.average ? 1 : F;
+  auto up = [&](DBuf<int32_t> &b, const std::vector<int32_t> &v) {
+    b.reserve(v.size() ? v.size() : 1, st);
+    if (!v.empty())
+      XG_CUDA(cudaMemcpyAsync(b.p, v.data(), 4 * v.size(), cudaMemcpyHostToDevice, st));
+  };
+  up(s.tt_row_pix, row_pix);
+  s.tt_sg.reserve((size_t)(G ? G : 1) * (F ? F : 1), st);
+  s.tt_sga.reserve(G ? G : 1, st);
+  s.tt_C.reserve((size_t)(Q ? Q : 1) * F * F + 1, st);
+  s.tt_full.reserve((size_t)F * (Q ? Q : 1) + 1, st);
+  s.tt_part.reserve((size_t)req.window * o.partials * (Q ? Q : 1) + 1, st);
+  XG_CUDA(cudaMemsetAsync(s.tt_C.p, 0, 4 * ((size_t)Q * F * F + 1), st));
+  if (mode == XPCS_MODE_EXACT) {
+    if (R > 0 && F > 0) run_twotime_exact(s, req, lay, force_i64);
+    o.ready = true;
+    return;
+  }
   // Gram order of every q bin's rows
   std::vector<int32_t> order(R);
   std::iota(order.begin(), order.end(), 0);
@@ -188,24 +208,12 @@ void run_twotime(Series &s, const TwoTimeReq &req) {
     for (int32_t q = 0; q < Q; q++)
       std::sort(order.begin() + q_ptr[q], order.begin() + q_ptr[q + 1],
                 [&](int32_t a, int32_t b) { return row_pix[a] < row_pix[b]; });
-  auto up = [&](DBuf<int32_t> &b, const std::vector<int32_t> &v) {
-    b.reserve(v.size() ? v.size() : 1, st);
-    if (!v.empty())
-      XG_CUDA(cudaMemcpyAsync(b.p, v.data(), 4 * v.size(), cudaMemcpyHostToDevice, st));
-  };
-  up(s.tt_row_pix, row_pix);
   up(s.tt_row_grp, row_grp);
   up(s.tt_grp_ptr, grp_ptr);
   up(s.tt_order, order);
   const size_t nV = (size_t)R * F;
   s.tt_V.reserve(nV ? nV : 1, st);
-  s.tt_sg.reserve((size_t)(G ? G : 1) * (F ? F : 1), st);
-  s.tt_sga.reserve(G ? G : 1, st);
-  s.tt_C.reserve((size_t)(Q ? Q : 1) * F * F + 1, st);
-  s.tt_full.reserve((size_t)F * (Q ? Q : 1) + 1, st);
-  s.tt_part.reserve((size_t)req.window * o.partials * (Q ? Q : 1) + 1, st);
   if (nV) XG_CUDA(cudaMemsetAsync(s.tt_V.p, 0, 4 * nV, st));
-  XG_CUDA(cudaMemsetAsync(s.tt_C.p, 0, 4 * ((size_t)Q * F * F + 1), st));
   if (R > 0 && F > 0) {
     k_tt_scatter<<<(R + 127) / 128, 128, 0, st>>>(R, F, s.tt_row_pix.p, s.row_ptr.p, s.row_len.p,
                                                   s.ev_frame.p, s.ev_val.p, s.tt_V.p);
@@ -217,8 +225,8 @@ void run_twotime(Series &s, const TwoTimeReq &req) {
       XG_CHECK_LAUNCH();
     }
     k_tt_smooth<<<(unsigned)((nV + 255) / 256), 256, 0, st>>>(R, F, req.average, s.tt_row_grp.p,
-                                                         req.average ? s.tt_sga.p : s.tt_sg.p,
-                                                         s.tt_V.p);
+                                                             req.average ? s.tt_sga.p : s.tt_sg.p,
+                                                             s.tt_V.p);
     XG_CHECK_LAUNCH();
     const int T = (F + TT_TILE - 1) / TT_TILE;
     for (int32_t q = 0; q < Q; q++) {

@@ -180,6 +180,13 @@ struct TwoTimeReq {
   std::vector<int32_t> qbins;  // q bins to process
   int32_t static_map = 0, average = 0, window = 1, frame_threading = 0;
 };
+// Rows of the processed q bins in mapping order and their grouping.
+struct TwoTimeLayout {
+  std::vector<int32_t> row_pix, row_grp;  // per row: its pixel, its smoothing group
+  std::vector<int32_t> grp_ptr{0};        // rows of each smoothing group (contiguous)
+  std::vector<int32_t> q_ptr{0};          // rows of each processed q bin (contiguous)
+  std::vector<int32_t> q_grp_end;         // static map: end group index of each q bin
+};
 struct TwoTimeOut {
   bool ready = false;
   std::vector<int32_t> qbins;  // processed q bins present in the mapping, in mapping order
@@ -269,6 +276,12 @@ struct Series {
   TwoTimeOut tt;
   DBuf<int32_t> tt_row_pix, tt_row_grp, tt_grp_ptr, tt_order;
   DBuf<float> tt_V, tt_sg, tt_sga, tt_C, tt_full, tt_part;
+  DBuf<int32_t> tt_err, tt_flags;       // tensor-core path: wait timeouts, range flags
+  DBuf<uint16_t> tt_XT;                 // fp16 counts X^T [Fp][Kp] of one group
+  DBuf<long long> tt_S;                 // per-frame count sums of one group
+  DBuf<unsigned long long> tt_bound, tt_Gi;
+  DBuf<double> tt_sgd, tt_Cacc, tt_Cq;
+  DBuf<float> tt_Gf;
 
   // tracer
   cudaEvent_t ev[12] = {};
@@ -346,7 +359,9 @@ void run_side_stats(Series &s, const SideOut &out);
 void prepare_framesum_scale(Series &s);  // k_side.cu
 
 // Two-time (k_twotime.cu): needs the event lists of run_filter_transpose
-void run_twotime(Series &s, const TwoTimeReq &req);
+void run_twotime(Series &s, const TwoTimeReq &req, int mode, bool force_i64);
+void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &lay,
+                       bool force_i64);  // k_twotime_tc.cu
 void get_twotime(Series &s, int32_t *qbins, float *sg, float *c2t, float *g2full, float *g2part);
 
 // Dense frames (k_dense.cu)

@@ -43,6 +43,7 @@ EXPORTS = [
 BATCH_F64 = 1
 BATCH_F32 = 2
 BATCH_AUTOTUNE = 4
+TWOTIME_EXACT_CUDA_CORES = 2
 
 NOALLOC_MAX_EVENTS = 4194304
 
