@@ -361,6 +361,61 @@ def run_serving(args, dev):
             "peak_footprint_gb": st["peak_used_bytes"] / (1 << 30)}
 
 
+def run_twotime_bench(args, dev):
+    """Two-time on 8 series of 512x512 x 4096 sparse frames (the batch mix's
+    two-time option): the EXACT mode (integer Gram of the counts on the tensor
+    cores, float64 smoothing) on every series, and the REFERENCE mode (float32
+    in the reference's order on CUDA cores) on the first, with the largest
+    relative difference between the two.  Symmetric smoothing, all 9 q rings."""
+    import xpcs_gpu as xg
+
+    rng = np.random.default_rng(777)
+    n = args.twotime_series
+    exact_ms, gram_ms, gram_flop, ref_ms, dev_rel = [], 0.0, 0.0, None, None
+    for i in range(n):
+        mean = float(np.exp(rng.uniform(np.log(0.001), np.log(0.05))))
+        acq = xs.Acquisition(width=512, height=512, frames=args.twotime_frames, n_static=18,
+                             n_dynamic=9, mean=mean, tau_min=2.0, tau_max=2000.0,
+                             seed=9000 + i, dpl=4)
+        dq, sq, _, _ = xs.maps(acq)
+        d = xs.DeviceFrames(acq)
+        with xg.Series(acq.width, acq.height, acq.frames, 4, dq, sq, device=dev) as s:
+            s.ingest_sparse_device(d.nnz, d.idx, d.val)
+            s.synchronize()
+            d.close()
+            qs = list(range(1, 10))
+            s.twotime(qs, mode=xg.MODE_EXACT, window=8)  # sizes buffers
+            t0 = time.perf_counter()
+            r = s.twotime(qs, mode=xg.MODE_EXACT, window=8)
+            exact_ms.append((time.perf_counter() - t0) * 1e3)
+            gram_ms += r["gram_ms"]
+            gram_flop += r["gram_flop"]
+            if i == 0:
+                t0 = time.perf_counter()
+                ref = s.twotime(qs, mode=xg.MODE_REFERENCE, window=8)
+                ref_ms = (time.perf_counter() - t0) * 1e3
+                dev_rel = max(float(np.max(np.abs(r["c2t"][q].astype(np.float64) - ref["c2t"][q]))
+                                    / max(float(np.max(np.abs(ref["c2t"][q]))), 1e-30))
+                              for q in ref["c2t"])
+    peak = 1916.2
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peak = float(json.loads(pk.read_text()).get("bf16_tflops", peak))
+    achieved = gram_flop / (gram_ms * 1e-3) / 1e12 if gram_ms > 0 else None
+    return {"workload": (f"{n} sparse series, 512x512 x {args.twotime_frames} frames, mean "
+                         "photons/pixel/frame log-uniform [0.1 %, 5 %], tau_c log-uniform "
+                         "[2, 2000], 18 static / 9 dynamic rings, all 9 q rings, symmetric "
+                         "smoothing, window 8, seed 777"),
+            "series": n, "exact_ms_per_series": statistics.median(exact_ms),
+            "reference_order_ms_one_series": ref_ms,
+            "exact_vs_reference_order_max_rel": dev_rel,
+            "gram_roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                              "peak_kind": "measured bf16 dense (fp16 runs at the same rate)",
+                              "unit": "TFLOP/s",
+                              "frac": achieved / peak if achieved else None,
+                              "flop": gram_flop, "kernel_ms": gram_ms}}
+
+
 def run_gpu_arm(args, dist):
     import xpcs_gpu as xg
 
@@ -471,6 +526,8 @@ def run_gpu_arm(args, dist):
         result["batch"] = run_batch(args, dev)
     if not args.no_serving:
         result["serving"] = run_serving(args, dev)
+    if not args.no_twotime:
+        result["twotime"] = run_twotime_bench(args, dev)
     if dist.rank == 0 and world == 1 and not args.no_cpu_baseline:
         frames = args.cpu_sample_frames
         t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
@@ -495,6 +552,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-series batch measure")
     ap.add_argument("--no-serving", action="store_true", help="skip the streaming measure")
+    ap.add_argument("--no-twotime", action="store_true", help="skip the two-time measure")
+    ap.add_argument("--twotime-series", type=int, default=8)
+    ap.add_argument("--twotime-frames", type=int, default=4096)
     ap.add_argument("--serve-streams", type=int, default=16)
     ap.add_argument("--serve-hz", type=float, default=200.0)
     ap.add_argument("--serve-stagger", type=float, default=0.2, help="seconds between starts")

@@ -285,6 +285,8 @@ typedef struct {
   int32_t window;
   int32_t partials;         /* (F - window) / window */
   int32_t sg_rows, sg_cols;
+  float gram_ms;            /* EXACT mode: device time of the tensor-core Gram kernels */
+  double gram_flop;         /* EXACT mode: their multiply-add work, 2 x M x N x K per tile */
 } xpcs_twotime_info;
 int xpcs_twotime(xpcs_series *s, const xpcs_twotime_desc *d, int32_t mode,
                  xpcs_twotime_info *info);

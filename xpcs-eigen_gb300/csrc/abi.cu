@@ -492,6 +492,8 @@ int xpcs_twotime(xpcs_series *h, const xpcs_twotime_desc *d, int32_t mode,
       info->partials = s.tt.partials;
       info->sg_rows = s.tt.sg_rows;
       info->sg_cols = s.tt.sg_cols;
+      info->gram_ms = s.tt.gram_ms;
+      info->gram_flop = s.tt.gram_flop;
     }
   });
 }

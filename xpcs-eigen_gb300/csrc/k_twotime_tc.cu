@@ -340,6 +340,16 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
   s.tt_Cq.reserve((size_t)F * F + 1, st);
   std::vector<double> sg_host((size_t)G * (req.average ? 1 : F));
   const size_t smem = sizeof(TcSmem) + 1024;
+  cudaEvent_t g0 = nullptr, g1 = nullptr;
+  XG_CUDA(cudaEventCreate(&g0));
+  XG_CUDA(cudaEventCreate(&g1));
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } evg{g0, g1};
   XG_CUDA(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int32_t gq = 0;  // group index across q bins
   for (int32_t q = 0; q < Q; q++) {
@@ -396,9 +406,12 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
                                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (cr != CUDA_SUCCESS) throw Error(XPCS_ERR_CUDA, "tensor map encoding failed");
+        XG_CUDA(cudaEventRecord(g0, st));
         k_gram_tc<<<ntile * (ntile + 1) / 2, 128, smem, st>>>(tm, (int32_t)(Kp / TC_BK), ntile,
                                                             s.tt_Gf.p, Fp, s.tt_err.p);
         XG_CHECK_LAUNCH();
+        XG_CUDA(cudaEventRecord(g1, st));
+        o.gram_flop += (double)ntile * (ntile + 1) / 2 * 2.0 * TC_BM * TC_BN * (double)Kp;
         k_tc_accum<false><<<(unsigned)((nF2 + 255) / 256), 256, 0, st>>>(
             F, s.tt_Gf.p, Fp, s.tt_sgd.p, req.average, s.tt_Cacc.p);
         XG_CHECK_LAUNCH();
@@ -414,6 +427,11 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
         XG_CHECK_LAUNCH();
       }
       XG_CUDA(cudaStreamSynchronize(st));  // sgd is reused by the next group
+      if (tensor) {
+        float ms = 0.f;
+        XG_CUDA(cudaEventElapsedTime(&ms, g0, g1));
+        o.gram_ms += ms;
+      }
     }
     const int32_t npix = lay.q_ptr[q + 1] - lay.q_ptr[q];
     k_tc_final<<<(unsigned)(((size_t)F * F + 255) / 256), 256, 0, st>>>(

@@ -191,6 +191,8 @@ struct TwoTimeOut {
   bool ready = false;
   std::vector<int32_t> qbins;  // processed q bins present in the mapping, in mapping order
   int32_t frames = 0, window = 1, partials = 0, sg_rows = 0, sg_cols = 0;
+  float gram_ms = 0.f;      // EXACT: tensor-core Gram kernel time
+  double gram_flop = 0.0;
 };
 
 // --------------------------------------------------------------- a series

@@ -56,7 +56,8 @@ class TwoTimeDesc(C.Structure):
 
 class TwoTimeInfo(C.Structure):
     _fields_ = [("qbins", C.c_int32), ("frames", C.c_int32), ("window", C.c_int32),
-                ("partials", C.c_int32), ("sg_rows", C.c_int32), ("sg_cols", C.c_int32)]
+                ("partials", C.c_int32), ("sg_rows", C.c_int32), ("sg_cols", C.c_int32),
+                ("gram_ms", C.c_float), ("gram_flop", C.c_double)]
 
 
 class ServerStats(C.Structure):
@@ -314,7 +315,8 @@ class Series:
         check(lib().xpcs_get_twotime(self._h, _ptr(qs), _ptr(sg), _ptr(c2t), _ptr(full),
                                      _ptr(part)))
         return dict(qbins=qs, sg=sg, c2t={int(k): c2t[i] for i, k in enumerate(qs)},
-                    g2full=full, g2partials=part)
+                    g2full=full, g2partials=part, gram_ms=info.gram_ms,
+                    gram_flop=info.gram_flop)
 
     def autotune(self, mode=MODE_REFERENCE) -> int:
         """xpcs_autotune: pick this series' thread-kernel row capacity; returns it."""
