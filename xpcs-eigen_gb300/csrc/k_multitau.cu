@@ -42,6 +42,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstring>
 
 #include "xpcs_internal.h"
 
@@ -86,11 +87,19 @@ __device__ __forceinline__ int lower_bound_packed(const uint32_t *row, int n, in
 
 __device__ __forceinline__ float pow2_neg(int e) { return __int_as_float((127 - e) << 23); }
 
-// (float)num * 2^-shift / den as the reference's float arithmetic produces it.
-__device__ __forceinline__ float scaled_quotient(int num, int shift, float den) {
+// (float)num * 2^-shift / den as the reference's float arithmetic produces it
+// (num is an integer below 2^24, den an integer below 2^16 as a float).  The
+// IEEE quotient comes from the correctly rounded reciprocal by one residual
+// correction (Markstein 1990; Muller et al., Handbook of Floating-Point
+// Arithmetic, ch. 4): q0 = x*y, r = x - q0*den (exact by FMA), q = q0 + r*y.
+// It equals the IEEE division for every 24-bit significand x and every integer
+// den in [1, 65536] (checked exhaustively on the GPU against __fdiv_rn).
+__device__ __forceinline__ float scaled_quotient(int num, int shift, float den, float rcp) {
   if (num == 0) return 0.f;
-  float x = __fmul_rn((float)num, pow2_neg(shift));
-  return den > 0.f ? __fdiv_rn(x, den) : x;
+  const float x = __fmul_rn((float)num, pow2_neg(shift));
+  if (!(den > 0.f)) return x;
+  const float q0 = __fmul_rn(x, rcp);
+  return __fmaf_rn(__fmaf_rn(-q0, den, x), rcp, q0);
 }
 
 __device__ __forceinline__ int32_t pk_t(uint32_t w) { return (int32_t)(w >> 16); }
@@ -181,7 +190,7 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
         j--;
       }
       const int lvl = pl->lv[ar.gi[d]].level;
-      if (p < P) IP[(size_t)d * P + p] = mine ? scaled_quotient(total - rsum, lvl, ar.denom[d]) : 0.f;
+      if (p < P) IP[(size_t)d * P + p] = mine ? scaled_quotient(total - rsum, lvl, ar.denom[d], ar.rcp[d]) : 0.f;
     }
   }
   // IF: thresholds tau (in frames) increasing with the delay index
@@ -196,7 +205,7 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
       const int g = ar.gi[d];
       const int lvl = pl->lv[g].level;
       if (p < P)
-        IF[(size_t)d * P + p] = mine ? scaled_quotient(acc[g * 32] - ssum, lvl, ar.denom[d]) : 0.f;
+        IF[(size_t)d * P + p] = mine ? scaled_quotient(acc[g * 32] - ssum, lvl, ar.denom[d], ar.rcp[d]) : 0.f;
     }
   }
 
@@ -271,7 +280,7 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
     if (p < P) {
       for (int k = 0; k < L.count; k++) {
         const int d = L.first + k;
-        G2[(size_t)d * P + p] = mine ? scaled_quotient(acc[k * 32], 2 * L.level, ar.denom[d]) : 0.f;
+        G2[(size_t)d * P + p] = mine ? scaled_quotient(acc[k * 32], 2 * L.level, ar.denom[d], ar.rcp[d]) : 0.f;
       }
     }
   }
@@ -387,8 +396,8 @@ k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
       const int c_tau = lower_bound_row(row, n0, ar.tau_abs[d]);
       const int ip = c_ip ? S[c_ip - 1] : 0;
       const int iff = (c_end ? S[c_end - 1] : 0) - (c_tau ? S[c_tau - 1] : 0);
-      IP[(size_t)d * P + p] = scaled_quotient(ip, lvl, ar.denom[d]);
-      IF[(size_t)d * P + p] = scaled_quotient(iff, lvl, ar.denom[d]);
+      IP[(size_t)d * P + p] = scaled_quotient(ip, lvl, ar.denom[d], ar.rcp[d]);
+      IF[(size_t)d * P + p] = scaled_quotient(iff, lvl, ar.denom[d], ar.rcp[d]);
     }
     int m = n0;
     bool J = true, U = true;  // junction at m sorted; stale suffix [m, n0) sorted
@@ -427,7 +436,7 @@ k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
       }
       if (lane < L.count) {
         const int d = L.first + lane;
-        G2[(size_t)d * P + p] = scaled_quotient(mine, 2 * L.level, ar.denom[d]);
+        G2[(size_t)d * P + p] = scaled_quotient(mine, 2 * L.level, ar.denom[d], ar.rcp[d]);
       }
       __syncwarp();
     }
@@ -513,6 +522,26 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   }
 }
 
+// The float nearest to 1/b (ties to even) for an integer b in [1, 2^24]:
+// candidates around the double quotient compared by their exact residuals
+// (g*b has at most 48 significant bits, so 1 - g*b is exact in double).
+float recip_rn(int32_t b) {
+  const float f = (float)(1.0 / (double)b);
+  float best = f;
+  double be = std::fabs(1.0 - (double)f * b);
+  for (float g : {std::nextafter(f, 0.f), std::nextafter(f, 2.f * f)}) {
+    const double e = std::fabs(1.0 - (double)g * b);
+    uint32_t gb, bb;
+    std::memcpy(&gb, &g, 4);
+    std::memcpy(&bb, &best, 4);
+    if (e < be || (e == be && (gb & 1u) == 0 && (bb & 1u) != 0)) {
+      best = g;
+      be = e;
+    }
+  }
+  return best;
+}
+
 // Host-side plan: level groups of the delay schedule with the lastframe each
 // sees and whether the reference compacts before it (corr.cpp:341-391).
 std::vector<uint8_t> make_plan(const Series &s, int mode) {
@@ -523,6 +552,7 @@ std::vector<uint8_t> make_plan(const Series &s, int mode) {
   int32_t *tau_lvl = base;
   float *denom = (float *)(base + D);
   int32_t *tau_abs = base + 2 * D, *t_ip = base + 3 * D, *gi = base + 4 * D;
+  float *rcp = (float *)(base + 5 * D);
   pl->P = s.P;
   pl->D = D;
   pl->F = s.F;
@@ -542,6 +572,7 @@ std::vector<uint8_t> make_plan(const Series &s, int mode) {
     tau_lvl[k] = tau;
     tau_abs[k] = s.delays.tau[k];
     denom[k] = (lastframe - tau) > 0 ? (float)(lastframe - tau) : 0.f;
+    rcp[k] = denom[k] > 0.f ? recip_rn((int32_t)(lastframe - tau)) : 0.f;
     t_ip[k] = (int32_t)std::max<int64_t>(0, (int64_t)(lastframe - tau) << level);
     if (newgroup) {
       if (nlev >= MAX_LEVELS) throw Error(XPCS_ERR_INVALID_ARGUMENT, "too many multi-tau levels");

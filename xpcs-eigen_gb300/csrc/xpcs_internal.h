@@ -126,14 +126,16 @@ struct McArrays {
   const int32_t *tau_abs;  // delay in frames = first frame counted by IF
   const int32_t *t_ip;     // (lastframe - tau) << level: IP counts frames below it
   const int32_t *gi;       // level group of the delay
+  const float *rcp;        // correctly rounded 1 / denom (0 when denom is 0)
 };
 __host__ __device__ inline size_t mc_align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t mc_plan_bytes(int D) {
-  return mc_align16(sizeof(McPlan) + (size_t)D * 5 * sizeof(int32_t));
+  return mc_align16(sizeof(McPlan) + (size_t)D * 6 * sizeof(int32_t));
 }
 __host__ __device__ inline McArrays mc_arrays(const void *plan, int D) {
   const int32_t *b = (const int32_t *)((const uint8_t *)plan + sizeof(McPlan));
-  return McArrays{b, (const float *)(b + D), b + 2 * D, b + 3 * D, b + 4 * D};
+  return McArrays{b, (const float *)(b + D), b + 2 * D, b + 3 * D, b + 4 * D,
+                  (const float *)(b + 5 * D)};
 }
 
 // Pixel classes assigned by the filter's merge pass.  The integer kernels
