@@ -13,9 +13,10 @@
 // 2048 are exact in fp16, and when sum_p max_t X_g[p][t]^2 < 2^24 every
 // partial sum is an integer below 2^24, exact in fp32.  A group outside that
 // range takes an int64 CUDA-core Gram instead.  Operands are loaded by TMA
-// (128-byte swizzle, 128 x 64 fp16 tiles, 4 stages), one thread issues the
-// MMAs into a 128 x 128 fp32 accumulator in tensor memory, and four warps
-// read it back with tcgen05.ld.  Only the upper-triangle tiles are computed.
+// (128-byte swizzle, 128 x 64 and 256 x 64 fp16 tiles, 4 stages), one thread
+// issues M=128, N=256 MMAs into a 128 x 256 fp32 accumulator in tensor
+// memory, and four warps read it back with tcgen05.ld.  Only tiles that meet
+// the upper triangle are computed.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -28,15 +29,16 @@ namespace xg {
 namespace {
 
 constexpr int TC_BM = 128;  // tile rows (frames t1), = tensor-memory lanes
-constexpr int TC_BN = 128;  // tile columns (frames t2), = tensor-memory columns
+constexpr int TC_BN = 256;  // tile columns (frames t2), = tensor-memory columns
 constexpr int TC_BK = 64;   // pixels per stage: 64 fp16 = one 128-byte swizzle row
 constexpr int TC_STAGES = 4;
-constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;  // 16 KB
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;  // 16 KB
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;  // 32 KB
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;      // bounded mbarrier waits
 
 struct TcSmem {
-  uint8_t a[TC_STAGES][TC_TILE_BYTES];
-  uint8_t b[TC_STAGES][TC_TILE_BYTES];
+  uint8_t a[TC_STAGES][TC_A_BYTES];
+  uint8_t b[TC_STAGES][TC_B_BYTES];
   uint64_t full[TC_STAGES], empty[TC_STAGES], done;
   uint32_t tmem;
 };
@@ -123,21 +125,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// One CTA (4 warps) per upper-triangle 128 x 128 tile of G = X^T X, X^T given
-// as an fp16 tensor [Fp][Kp] (K-major).  Thread 0 loads by TMA, thread 32
-// issues the MMAs, all four warps read the accumulator back.  G: [Fp][Fp].
+// One CTA (4 warps) per 128 x 256 tile of G = X^T X that meets the upper
+// triangle, X^T given as an fp16 tensor [Fp][Kp] (K-major, Fp a multiple of
+// 256), read through two tensor maps (128- and 256-row boxes).  Thread 0 loads
+// by TMA, thread 32 issues the MMAs, all four warps read the accumulator back.
+// G: [Fp][Fp]; tile row bi covers frames [128 bi, 128 bi + 128), tile column
+// bj frames [256 bj, 256 bj + 256), bj >= bi / 2.
 __global__ void __launch_bounds__(128)
-k_gram_tc(const __grid_constant__ CUtensorMap tm, int32_t nkt, int32_t ntile,
-          float *__restrict__ G, int64_t ldg, int32_t *__restrict__ err) {
+k_gram_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb,
+          int32_t nkt, int32_t nrow, int32_t ncol, float *__restrict__ G, int64_t ldg,
+          int32_t *__restrict__ err) {
   extern __shared__ uint8_t tc_raw[];
   TcSmem &sm = *reinterpret_cast<TcSmem *>(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int id = blockIdx.x, bi = 0;
-  while (id >= ntile - bi) {
-    id -= ntile - bi;
+  while (bi < nrow && id >= ncol - bi / 2) {
+    id -= ncol - bi / 2;
     bi++;
   }
-  const int bj = bi + id;
+  const int bj = bi / 2 + id;
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; s++) {
       mbar_init(&sm.full[s], 1);
@@ -163,9 +169,9 @@ k_gram_tc(const __grid_constant__ CUtensorMap tm, int32_t nkt, int32_t ntile,
       const int s = kt % TC_STAGES;
       if (kt >= TC_STAGES) ok = mbar_wait(&sm.empty[s], ((kt / TC_STAGES) - 1) & 1);
       if (!ok) break;
-      mbar_expect_tx(&sm.full[s], 2 * TC_TILE_BYTES);
-      tma_load_2d(sm.a[s], &tm, kt * TC_BK, bi * TC_BM, &sm.full[s]);
-      tma_load_2d(sm.b[s], &tm, kt * TC_BK, bj * TC_BN, &sm.full[s]);
+      mbar_expect_tx(&sm.full[s], TC_A_BYTES + TC_B_BYTES);
+      tma_load_2d(sm.a[s], &tma, kt * TC_BK, bi * TC_BM, &sm.full[s]);
+      tma_load_2d(sm.b[s], &tmb, kt * TC_BK, bj * TC_BN, &sm.full[s]);
     }
     if (!ok) atomicOr(err, 8);
   } else if (threadIdx.x == 32) {  // MMA issuer
@@ -328,8 +334,10 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
   cudaStream_t st = s.stream;
   TwoTimeOut &o = s.tt;
   const int32_t F = s.F, G = (int32_t)lay.grp_ptr.size() - 1, Q = (int32_t)lay.q_ptr.size() - 1;
-  const int64_t Fp = ((int64_t)F + TC_BM - 1) / TC_BM * TC_BM;
-  const int ntile = (int)(Fp / TC_BM);
+  const int64_t Fp = ((int64_t)F + TC_BN - 1) / TC_BN * TC_BN;
+  const int nrow = (int)(Fp / TC_BM), ncol = (int)(Fp / TC_BN);
+  int ntiles = 0;
+  for (int bi = 0; bi < nrow; bi++) ntiles += ncol - bi / 2;
   s.tt_err.reserve(1, st);
   s.tt_flags.reserve(1, st);
   XG_CUDA(cudaMemsetAsync(s.tt_err.p, 0, sizeof(int32_t), st));
@@ -395,23 +403,26 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
       const size_t nF2 = (size_t)F * F;
       if (tensor) {
         s.tt_Gf.reserve((size_t)(Fp * Fp), st);
-        CUtensorMap tm;
+        CUtensorMap tma, tmb;
         const cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)Fp};
         const cuuint64_t strides[1] = {(cuuint64_t)(Kp * 2)};
-        const cuuint32_t box[2] = {TC_BK, TC_BM};
+        const cuuint32_t boxa[2] = {TC_BK, TC_BM}, boxb[2] = {TC_BK, TC_BN};
         const cuuint32_t es[2] = {1, 1};
-        const CUresult cr = encode_fn()(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, s.tt_XT.p, dims,
-                                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                        CU_TENSOR_MAP_SWIZZLE_128B,
-                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (cr != CUDA_SUCCESS) throw Error(XPCS_ERR_CUDA, "tensor map encoding failed");
+        for (int w = 0; w < 2; w++) {
+          const CUresult cr = encode_fn()(w ? &tmb : &tma, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                                          s.tt_XT.p, dims, strides, w ? boxb : boxa, es,
+                                          CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                          CU_TENSOR_MAP_SWIZZLE_128B,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+          if (cr != CUDA_SUCCESS) throw Error(XPCS_ERR_CUDA, "tensor map encoding failed");
+        }
         XG_CUDA(cudaEventRecord(g0, st));
-        k_gram_tc<<<ntile * (ntile + 1) / 2, 128, smem, st>>>(tm, (int32_t)(Kp / TC_BK), ntile,
-                                                            s.tt_Gf.p, Fp, s.tt_err.p);
+        k_gram_tc<<<ntiles, 128, smem, st>>>(tma, tmb, (int32_t)(Kp / TC_BK), nrow, ncol,
+                                             s.tt_Gf.p, Fp, s.tt_err.p);
         XG_CHECK_LAUNCH();
         XG_CUDA(cudaEventRecord(g1, st));
-        o.gram_flop += (double)ntile * (ntile + 1) / 2 * 2.0 * TC_BM * TC_BN * (double)Kp;
+        o.gram_flop += (double)ntiles * 2.0 * TC_BM * TC_BN * (double)Kp;
         k_tc_accum<false><<<(unsigned)((nF2 + 255) / 256), 256, 0, st>>>(
             F, s.tt_Gf.p, Fp, s.tt_sgd.p, req.average, s.tt_Cacc.p);
         XG_CHECK_LAUNCH();
