@@ -265,19 +265,18 @@ __global__ void k_gram_i64(int32_t nrows, int32_t F, int32_t r0,
     }
 }
 
-// C_acc[t1][t2] += G[t1][t2] / (sg[t1] sg[t2]) on the upper triangle
+// C_acc[t1][t2] += G[t1][t2] / (sg[t1] sg[t2]) on the upper triangle; block
+// row t1 = blockIdx.y, columns t2 from blockIdx.x
 template <bool I64>
 __global__ void k_tc_accum(int32_t F, const void *__restrict__ Gv, int64_t ldg,
                            const double *__restrict__ sg, int32_t avg, double *__restrict__ Cacc) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)F * F) return;
-  const int t1 = (int)(i / F), t2 = (int)(i % F);
-  if (t1 > t2) return;
+  const int t1 = blockIdx.y, t2 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t2 >= F || t2 < t1) return;
   const double g = I64 ? (double)(long long)((const unsigned long long *)Gv)[(size_t)t1 * ldg + t2]
                        : (double)((const float *)Gv)[(size_t)t1 * ldg + t2];
   if (g == 0.0) return;
   const double d = avg ? sg[0] * sg[0] : sg[t1] * sg[t2];
-  Cacc[i] += g / d;
+  Cacc[(size_t)t1 * F + t2] += g / d;
 }
 
 __global__ void k_tc_final(int32_t F, double inv_npix, const double *__restrict__ Cacc,
@@ -289,20 +288,29 @@ __global__ void k_tc_final(int32_t F, double inv_npix, const double *__restrict_
   C[i] = (float)v;
 }
 
-__global__ void k_tc_diag(int32_t Q, int32_t q, int32_t F, int32_t window, int32_t tp,
-                          const double *__restrict__ Cq, float *__restrict__ g2full,
-                          float *__restrict__ g2part) {
-  const int ff = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ff >= F) return;
+// one block per diagonal ff: g2full = its mean; for ff < window, one thread
+// per window w sums g2partials
+__global__ void __launch_bounds__(256)
+k_tc_diag(int32_t Q, int32_t q, int32_t F, int32_t window, int32_t tp,
+          const double *__restrict__ Cq, float *__restrict__ g2full,
+          float *__restrict__ g2part) {
+  __shared__ double red[256];
+  const int ff = blockIdx.x;
   double acc = 0.0;
-  for (int fx = 0; fx < F - ff; fx++) acc += Cq[(size_t)fx * F + fx + ff];
-  g2full[(size_t)ff * Q + q] = (float)(acc / (F - ff));
+  for (int fx = threadIdx.x; fx < F - ff; fx += blockDim.x) acc += Cq[(size_t)fx * F + fx + ff];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) g2full[(size_t)ff * Q + q] = (float)(red[0] / (F - ff));
   if (ff < window)
-    for (int w = 0; w < tp; w++) {
-      double s = 0.0;
+    for (int w = threadIdx.x; w < tp; w += blockDim.x) {
+      double sw = 0.0;
       for (int fx = w * window; fx < (w + 1) * window && fx < F - ff; fx++)
-        s += Cq[(size_t)fx * F + fx + ff];
-      g2part[((size_t)ff * tp + w) * Q + q] = (float)(s / window);
+        sw += Cq[(size_t)fx * F + fx + ff];
+      g2part[((size_t)ff * tp + w) * Q + q] = (float)(sw / window);
     }
 }
 
@@ -334,6 +342,7 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
   cudaStream_t st = s.stream;
   TwoTimeOut &o = s.tt;
   const int32_t F = s.F, G = (int32_t)lay.grp_ptr.size() - 1, Q = (int32_t)lay.q_ptr.size() - 1;
+  if (F > 65535) throw Error(XPCS_ERR_INVALID_ARGUMENT, "EXACT two-time supports up to 65535 frames");
   const int64_t Fp = ((int64_t)F + TC_BN - 1) / TC_BN * TC_BN;
   const int nrow = (int)(Fp / TC_BM), ncol = (int)(Fp / TC_BN);
   int ntiles = 0;
@@ -423,7 +432,7 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
         XG_CHECK_LAUNCH();
         XG_CUDA(cudaEventRecord(g1, st));
         o.gram_flop += (double)ntiles * 2.0 * TC_BM * TC_BN * (double)Kp;
-        k_tc_accum<false><<<(unsigned)((nF2 + 255) / 256), 256, 0, st>>>(
+        k_tc_accum<false><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
             F, s.tt_Gf.p, Fp, s.tt_sgd.p, req.average, s.tt_Cacc.p);
         XG_CHECK_LAUNCH();
       } else {
@@ -433,7 +442,7 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
                                                     s.row_ptr.p, s.row_len.p, s.ev_frame.p,
                                                     s.ev_val.p, s.tt_Gi.p, F);
         XG_CHECK_LAUNCH();
-        k_tc_accum<true><<<(unsigned)((nF2 + 255) / 256), 256, 0, st>>>(
+        k_tc_accum<true><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
             F, s.tt_Gi.p, F, s.tt_sgd.p, req.average, s.tt_Cacc.p);
         XG_CHECK_LAUNCH();
       }
@@ -448,8 +457,8 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
     k_tc_final<<<(unsigned)(((size_t)F * F + 255) / 256), 256, 0, st>>>(
         F, npix ? 1.0 / npix : 0.0, s.tt_Cacc.p, s.tt_Cq.p, s.tt_C.p + (size_t)q * F * F);
     XG_CHECK_LAUNCH();
-    k_tc_diag<<<(F + 127) / 128, 128, 0, st>>>(Q, q, F, req.window, o.partials, s.tt_Cq.p,
-                                              s.tt_full.p, s.tt_part.p);
+    k_tc_diag<<<F, 256, 0, st>>>(Q, q, F, req.window, o.partials, s.tt_Cq.p, s.tt_full.p,
+                                 s.tt_part.p);
     XG_CHECK_LAUNCH();
   }
   // sg as float, [G][F] or [G][1]

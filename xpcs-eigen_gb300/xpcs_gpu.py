@@ -299,13 +299,17 @@ class Series:
         return out
 
     def twotime(self, qbins, static_map=False, average=False, window=1, frame_threading=False,
-                mode=MODE_REFERENCE) -> dict:
-        """xpcs_twotime + xpcs_get_twotime: sg, C2T per q bin, g2full, g2partials."""
+                mode=MODE_REFERENCE, fetch=True) -> dict:
+        """xpcs_twotime + xpcs_get_twotime: sg, C2T per q bin, g2full, g2partials
+        (fetch=False: compute only, results stay on the device)."""
         q = np.ascontiguousarray(qbins, np.int32)
         d = TwoTimeDesc(q.ctypes.data_as(C.POINTER(C.c_int32)), q.size, int(static_map),
                         int(average), int(window), int(frame_threading))
         info = TwoTimeInfo()
         check(lib().xpcs_twotime(self._h, C.byref(d), mode, C.byref(info)))
+        if not fetch:
+            return dict(gram_ms=info.gram_ms, gram_flop=info.gram_flop, qbins=info.qbins,
+                        frames=info.frames)
         Q, F = info.qbins, info.frames
         qs = np.empty(Q, np.int32)
         sg = np.empty((info.sg_rows, info.sg_cols), np.float32)
