@@ -227,6 +227,61 @@ def test_dense_medium_vs_oracle():
     assert same_bits_nan(g32, og) and same_bits_nan(s32, os_)
 
 
+@pytest.mark.parametrize("mode,dpl", [(xg.MODE_REFERENCE, 8), (xg.MODE_EXACT, 8),
+                                      (xg.MODE_REFERENCE, 4), (xg.MODE_REFERENCE, 16)])
+def test_dense_long_float_rows_vs_oracle(mode, dpl):
+    """Dark-subtracted, flat-fielded CCD rows of hundreds to thousands of float
+    events (gain below 1 lifts the dark residual over the threshold): the
+    warp-per-pixel float kernel on long, densely occupied rows."""
+    acq = xs.Acquisition(width=40, height=36, frames=5000, n_static=12, n_dynamic=6, mean=0.03,
+                         tau_min=3, tau_max=400, seed=41 + dpl, dpl=dpl, dense=True,
+                         dark_frames=30, gain_min=0.85, gain_max=1.1)
+    dq, sq, flat, _ = xs.maps(acq)
+    ds = xs.DenseStream(acq)
+    raw = ds.next(acq.dark_frames + acq.frames)
+    ds.close()
+    lld, sigma = 0.0, 3.0
+    with xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, flatfield=flat,
+                   dense=True, lld=lld, sigma=sigma) as s:
+        s.set_dark(raw[:acq.dark_frames])
+        s.ingest_dense(raw[acq.dark_frames:])
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+        info = s.info()
+    qm = oracle.QMap(dq, sq)
+    da, dsd = oracle.dark_image(raw[:acq.dark_frames], flat.ravel())
+    rows, _ = oracle.dense_filter(qm, raw[acq.dark_frames:], acq.frames, da, dsd, lld, sigma,
+                                  flat=flat.ravel())
+    lens = np.diff(rows.row_ptr)
+    assert info.float_path_pixels > 0 and lens.max() > 1500
+    oG2, oIP, oIF = oracle.multitau2(rows, acq.frames, acq.dpl, mode)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
+@pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
+def test_sparse_float_rows_with_stale_tail_misses_vs_oracle(mode):
+    """Sparse counts times a flatfield are float rows; on these the reference's
+    lower_bound over the out-of-order buffer misses some partners (the
+    REFERENCE and EXACT results differ), which the float kernel reproduces."""
+    acq = xs.Acquisition(width=64, height=64, frames=10000, n_static=12, n_dynamic=6,
+                         mean=0.005, tau_min=5, tau_max=500, seed=5, dpl=8, gain_min=0.9,
+                         gain_max=1.1)
+    dq, sq, flat, _ = xs.maps(acq)
+    nnz, idx, val = xs.sparse_frames(acq)
+    with xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, flatfield=flat) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+        info = s.info()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, acq.frames, flat=flat.ravel())
+    assert info.float_path_pixels > 1000
+    oG2, oIP, oIF = oracle.multitau2(rows, acq.frames, acq.dpl, mode)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+    other = oracle.multitau2(rows, acq.frames, acq.dpl, 1 - mode)[0]
+    assert np.count_nonzero(other != oG2) > 10  # the stale-tail searches matter here
+
+
 # ------------------------------------------------------------- side statistics
 
 def _side_gpu(fx):

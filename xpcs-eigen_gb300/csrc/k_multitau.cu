@@ -522,6 +522,212 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   }
 }
 
+// ------------------------------------------------ float rows, warp per pixel
+//
+// The same operations as k_mt_float, in the same order per sum, with the work
+// of one pixel spread over a warp:
+//   * the row is compacted in place in the scratch buffer exactly as the
+//     reference does it (so the stale tail is the reference's), 32 entries per
+//     step: each entry's half index, a ballot of the group starts and the pair
+//     sum (v[i] + v[i+1]) / 2 of merged neighbours;
+//   * lower_bound over the whole buffer lands on a prefix entry j exactly when
+//     lower_bound(idx[j]) == j ("findable"); the search result is monotone in
+//     its argument, so a pair (r, j) counts iff idx[j] == idx[r] + tau and j is
+//     findable.  While the buffer is sorted (tracked per level from the
+//     junctions between the prefix and the older segments) every entry is
+//     findable; otherwise each lane runs the reference's search for its entry;
+//   * each float sum (G2, IP, IF of every delay of the level) is a chain that
+//     one lane accumulates in the reference's order: per 32 entries the lanes
+//     first write their terms (v*v' of the pair with distance tau, or v inside
+//     the IP / IF ranges, else +0, which leaves a sum unchanged) to shared
+//     memory, then each chain's lane adds its 32 terms in entry order.
+// Partners lie at most tau entries ahead (distinct ascending indices), so a
+// ring of two 32-entry tiles holds every partner of the current tile.
+constexpr int FW_WARPS = 8;
+constexpr int FW_MAXC = 32;  // delays per level and largest delay in level units
+constexpr int FW_TSTRIDE = 33;
+
+__device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x) {
+  int first = 0, len = n;
+  while (len > 0) {
+    const int half = len >> 1;
+    if (a[first + half] < x) {
+      first += half + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  return first;
+}
+
+__global__ void __launch_bounds__(FW_WARPS * 32)
+k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
+           const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
+           const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
+           const float *__restrict__ ev_val, const float *__restrict__ fscale,
+           int32_t *__restrict__ sc_frame, float *__restrict__ sc_val, float *__restrict__ G2,
+           float *__restrict__ IP, float *__restrict__ IF) {
+  extern __shared__ __align__(16) uint8_t fw_smem[];
+  const McPlan *pl = (const McPlan *)plan_g;
+  const int D = pl->D, P = pl->P, nlev = pl->nlev, acc_max = pl->acc;
+  const bool ref = pl->mode == XPCS_MODE_REFERENCE;
+  const McArrays ar = mc_arrays(plan_g, D);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // per warp: ring idx[64], val[64], findable[64]; terms [3 * acc][33]
+  const size_t wbytes = 64 * 9 + 3 * (size_t)acc_max * FW_TSTRIDE * 4;
+  uint8_t *wb = fw_smem + (size_t)w * ((wbytes + 15) & ~(size_t)15);
+  int32_t *ridx = (int32_t *)wb;
+  float *rval = (float *)(wb + 256);
+  uint8_t *rfind = wb + 512;
+  float *terms = (float *)(wb + 576);
+  const int nf = stats->nfloat;
+  const int wg = (blockIdx.x * FW_WARPS + w), nw = gridDim.x * FW_WARPS;
+  for (int q = wg; q < nf; q += nw) {
+    const int p = flist[q];
+    const int64_t b = row_ptr[p];
+    const int n0 = row_len[p];
+    int32_t *idx = sc_frame + b;
+    float *val = sc_val + b;
+    for (int i = lane; i < n0; i += 32) {
+      const int32_t f = ev_frame[b + i];
+      idx[i] = f;
+      // normalize_by_framesum: v / (frameSum[f] / mean) (main.cpp:330-333)
+      val[i] = fscale ? __fdiv_rn(ev_val[b + i], fscale[f]) : ev_val[b + i];
+    }
+    __syncwarp();
+    int L = n0;
+    bool tail_sorted = true, dead = false;
+    for (int gi = 0; gi < nlev; gi++) {
+      const McLevel lv = pl->lv[gi];
+      const int lastframe = lv.lastframe, cnt = lv.count, t0 = lv.tau_lo;
+      if (lv.compact && !dead) {
+        const int prevL = L;
+        // the junction between the previous prefix and the older tail
+        bool junction_ok = true;
+        if (prevL < n0) junction_ok = idx[prevL - 1] <= idx[prevL];
+        if ((idx[0] >> 1) >= lastframe) {
+          dead = true;  // nothing is kept: lastIndex becomes 1 on a stale entry
+        } else {
+          int out = 0, carry_h = -1;
+          for (int base = 0; base < prevL; base += 32) {
+            const int a = base + lane;
+            const bool in = a < prevL;
+            const int32_t ia = in ? idx[a] : INT_MAX;
+            const float va = in ? val[a] : 0.f;
+            const bool has_b = a + 1 < prevL;
+            const int32_t ib = has_b ? idx[a + 1] : INT_MAX;
+            const int h = ia >> 1, hb = ib >> 1;
+            int hp = __shfl_up_sync(0xffffffffu, h, 1);
+            if (lane == 0) hp = carry_h;
+            const bool keep = in && (a == 0 || h != hp) && h < lastframe;
+            const bool merge = keep && has_b && hb == h;
+            float sv = va;
+            if (merge) sv = __fadd_rn(va, val[a + 1]);
+            sv = __fmul_rn(sv, 0.5f);  // == sv / 2 (exact scaling)
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            const bool stop = __any_sync(0xffffffffu, in && h >= lastframe);
+            carry_h = __shfl_sync(0xffffffffu, h, 31);
+            __syncwarp();
+            if (keep) {
+              const int o = out + __popc(bal & ((1u << lane) - 1u));
+              idx[o] = h;
+              val[o] = sv;
+            }
+            out += __popc(bal);
+            __syncwarp();
+            if (stop) break;
+          }
+          L = out;
+          tail_sorted = tail_sorted && (L >= prevL || junction_ok);
+        }
+      }
+      if (dead) {
+        for (int c = lane; c < cnt; c += 32) {
+          const size_t o = (size_t)(lv.first + c) * P + p;
+          G2[o] = 0.f;
+          IP[o] = 0.f;
+          IF[o] = 0.f;
+        }
+        continue;
+      }
+      // every prefix entry is findable unless the reference searches a buffer
+      // that is out of order
+      const bool all_find = !ref || (tail_sorted && (L >= n0 || idx[L - 1] <= idx[L]));
+      const int kmax = t0 + cnt - 1;
+      const int nchain = 3 * cnt;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      auto load_tile = [&](int tb) {
+        const int j = tb + lane, slot = j & 63;
+        if (j < L) {
+          const int32_t x = idx[j];
+          ridx[slot] = x;
+          rval[slot] = val[j];
+          rfind[slot] = all_find ? 1 : (lower_bound_g(idx, n0, x) == j);
+        } else {
+          ridx[slot] = INT_MAX;
+          rval[slot] = 0.f;
+          rfind[slot] = 0;
+        }
+      };
+      load_tile(0);
+      load_tile(32);
+      for (int base = 0; base < L; base += 32) {
+        __syncwarp();
+        const int r = base + lane;
+        const bool valid = r < L;
+        const int32_t src = ridx[r & 63];
+        const float v = rval[r & 63];
+        for (int c = 0; c < cnt; c++) {
+          const int tau = t0 + c;
+          terms[(size_t)c * FW_TSTRIDE + lane] = 0.f;
+          terms[(size_t)(cnt + c) * FW_TSTRIDE + lane] = (valid && src < lastframe - tau) ? v : 0.f;
+          terms[(size_t)(2 * cnt + c) * FW_TSTRIDE + lane] =
+              (valid && src >= tau && src < lastframe) ? v : 0.f;
+        }
+        if (valid) {
+          for (int k = t0 > 0 ? 1 : 0; k <= kmax; k++) {
+            const int qk = r + k;
+            if (qk >= L) break;
+            const int d = ridx[qk & 63] - src;
+            if (d > kmax) break;
+            if (d >= t0 && rfind[qk & 63] && src < lastframe - d)
+              terms[(size_t)(d - t0) * FW_TSTRIDE + lane] = __fmul_rn(v, rval[qk & 63]);
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int ch = lane + 32 * j;
+          if (ch < nchain) {
+            const float *tr = terms + (size_t)ch * FW_TSTRIDE;
+            float a = acc[j];
+#pragma unroll 8
+            for (int i = 0; i < 32; i++) a = __fadd_rn(a, tr[i]);
+            acc[j] = a;
+          }
+        }
+        __syncwarp();
+        // the tile after next replaces this one in the ring
+        load_tile(base + 64);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int ch = lane + 32 * j;
+        if (ch < nchain) {
+          const int type = ch / cnt, c = ch - type * cnt;
+          const int d = lv.first + c;
+          const float den = ar.denom[d];
+          const float x = den > 0.f ? __fdiv_rn(acc[j], den) : acc[j];
+          float *dst = type == 0 ? G2 : (type == 1 ? IP : IF);
+          dst[(size_t)d * P + p] = x;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // The float nearest to 1/b (ties to even) for an integer b in [1, 2^24]:
 // candidates around the double quotient compared by their exact residuals
 // (g*b has at most 48 significant bits, so 1 - g*b is exact in double).
@@ -688,9 +894,21 @@ void run_multitau(Series &s, int mode) {
     prepare_framesum_scale(s);
     fscale = s.d_fscale.p;
   }
-  k_mt_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p,
-                                   s.ev_frame.p, s.ev_val.p, fscale, s.sc_frame.p, s.sc_val.p,
-                                   s.G2.p, s.IP.p, s.IF.p);
+  int kmax = 0;
+  for (int g = 0; g < hp->nlev; g++) kmax = std::max(kmax, hp->lv[g].tau_lo + hp->lv[g].count - 1);
+  if (kmax <= FW_MAXC && hp->acc <= FW_MAXC) {
+    const size_t wb = (64 * 9 + 3 * (size_t)hp->acc * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
+    const size_t smf = FW_WARPS * wb;
+    XG_CUDA(cudaFuncSetAttribute(k_mt_fwarp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smf));
+    k_mt_fwarp<<<sms * 8, FW_WARPS * 32, smf, st>>>(
+        s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p, s.ev_frame.p, s.ev_val.p,
+        fscale, s.sc_frame.p, s.sc_val.p, s.G2.p, s.IP.p, s.IF.p);
+  } else {
+    k_mt_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p,
+                                     s.ev_frame.p, s.ev_val.p, fscale, s.sc_frame.p, s.sc_val.p,
+                                     s.G2.p, s.IP.p, s.IF.p);
+  }
   XG_CHECK_LAUNCH();
   XG_CUDA(cudaEventRecord(s.ev[6], st));
 }

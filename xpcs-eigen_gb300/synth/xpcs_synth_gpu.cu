@@ -1,6 +1,7 @@
-// xpcs_synth_gpu — the sparse frames of xpcs_synth (xs_sparse) drawn on the
-// GPU, for benchmark inputs too large to draw on the host in reasonable time
-// (64 uneven series, 16 concurrent 1 Mpx streams).
+// xpcs_synth_gpu — the sparse frames of xpcs_synth (xs_sparse) and its dense
+// CCD frames (xs_dense_next) drawn on the GPU, for benchmark inputs too large
+// to draw on the host in reasonable time (64 uneven series, 16 concurrent
+// 1 Mpx streams, 20,100 frames of 960x960).
 //
 // Same model and the same per-pixel random streams as the host generator: one
 // thread per pixel runs its splitmix64 stream through the frames in order
@@ -132,6 +133,63 @@ __global__ void k_block_write(int32_t P, const uint16_t *__restrict__ counts,
   }
 }
 
+constexpr uint64_t STREAM_DARK = 4, STREAM_NOISE = 6;
+
+__device__ inline uint64_t stream_seed(uint64_t seed, uint64_t stream, uint64_t i) {
+  return mix64(seed ^ mix64(stream * 0x9E3779B97F4A7C15ull + i + 1));
+}
+
+// dense frames: the dark level and the read-noise stream of every pixel
+__global__ void k_dense_init(int32_t P, uint64_t seed, double dark_mean, double dark_sigma,
+                             float *__restrict__ dark, uint64_t *__restrict__ noise,
+                             PixelState *__restrict__ st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  uint64_t d = stream_seed(seed, STREAM_DARK, (uint64_t)i);
+  dark[i] = __double2float_rn(__dadd_rn(dark_mean, __dmul_rn(dark_sigma, (double)normal(d))));
+  noise[i] = stream_seed(seed, STREAM_NOISE, (uint64_t)i);
+  st[i].rng = stream_seed(seed, STREAM_SPECKLE, (uint64_t)i);
+}
+
+// sequence frames [f0, f0 + nf) ("dark_frames" darks, then data frames) of
+// every pixel: dark level + read noise, plus adu * photons / gain on data
+// frames, rounded and clipped to [0, 65535], stored as the int16 bit pattern
+__global__ void k_dense_draw(int32_t P, int64_t f0, int32_t nf, int32_t dark_frames, double mean,
+                             double read_noise, double adu, const float *__restrict__ fa,
+                             const float *__restrict__ fs, const float *__restrict__ dark,
+                             const double *__restrict__ flat, uint64_t *__restrict__ noise,
+                             PixelState *__restrict__ st, int16_t *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  PixelState x = st[i];
+  uint64_t nz = noise[i];
+  const float a = fa[i], sc = fs[i], dk = dark[i];
+  const double g = flat[i];
+  for (int k = 0; k < nf; k++) {
+    const int64_t fr = f0 + k;
+    double v = __dadd_rn((double)dk, __dmul_rn(read_noise, (double)normal(nz)));
+    if (fr >= dark_frames) {
+      if (fr == dark_frames) {
+        x.er = __fmul_rn(normal(x.rng), 0.70710678f);
+        x.ei = __fmul_rn(normal(x.rng), 0.70710678f);
+      } else {
+        const float nr = __fmul_rn(normal(x.rng), 0.70710678f);
+        const float ni = __fmul_rn(normal(x.rng), 0.70710678f);
+        x.er = __fadd_rn(__fmul_rn(a, x.er), __fmul_rn(sc, nr));
+        x.ei = __fadd_rn(__fmul_rn(a, x.ei), __fmul_rn(sc, ni));
+      }
+      const float inten = __fadd_rn(__fmul_rn(x.er, x.er), __fmul_rn(x.ei, x.ei));
+      const int n = poisson(x.rng, mean * (double)inten);
+      v = __dadd_rn(v, __ddiv_rn(__dmul_rn(adu, (double)n), g));
+    }
+    double r = floor(__dadd_rn(v, 0.5));
+    r = r < 0.0 ? 0.0 : (r > 65535.0 ? 65535.0 : r);
+    out[(size_t)k * P + i] = (int16_t)(uint16_t)r;
+  }
+  st[i] = x;
+  noise[i] = nz;
+}
+
 bool grow(void **p, size_t &cap, size_t need, size_t used, size_t elem) {
   if (need <= cap) return true;
   size_t nc = cap ? cap : 1;
@@ -219,6 +277,55 @@ int64_t xsg_sparse(const xs_params *p, const float *a, const float *s, uint32_t 
   *idx_dev = (int32_t *)idx;
   *val_dev = (int16_t *)val;
   return ok ? total : -1;
+}
+
+/* Dense frames of xs_dense_next drawn on the current CUDA device: the whole
+ * sequence of dark_frames darks and then frames data frames, int16
+ * [dark_frames + frames][P] in one device allocation (*out_dev, free with
+ * xsg_free).  a/s: xs_pixel_fields; flat: the flatfield of xs_make_maps
+ * (host arrays).  Returns 0, or 1 on failure. */
+int xsg_dense(const xs_params *p, const float *a, const float *s, const double *flat,
+              int16_t **out_dev) {
+  const int32_t P = p->width * p->height;
+  const int64_t NF = (int64_t)p->dark_frames + p->frames;
+  float *da = nullptr, *ds = nullptr, *dark = nullptr;
+  double *dflat = nullptr;
+  uint64_t *noise = nullptr;
+  PixelState *st = nullptr;
+  int16_t *out = nullptr;
+  bool ok = cudaMalloc(&da, sizeof(float) * P) == cudaSuccess &&
+            cudaMalloc(&ds, sizeof(float) * P) == cudaSuccess &&
+            cudaMalloc(&dark, sizeof(float) * P) == cudaSuccess &&
+            cudaMalloc(&dflat, sizeof(double) * P) == cudaSuccess &&
+            cudaMalloc(&noise, sizeof(uint64_t) * P) == cudaSuccess &&
+            cudaMalloc(&st, sizeof(PixelState) * P) == cudaSuccess &&
+            cudaMalloc(&out, sizeof(int16_t) * (size_t)(NF > 0 ? NF : 1) * P) == cudaSuccess;
+  ok = ok && cudaMemcpy(da, a, sizeof(float) * P, cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(ds, s, sizeof(float) * P, cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(dflat, flat, sizeof(double) * P, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {
+    k_dense_init<<<(P + 255) / 256, 256>>>(P, p->seed, p->dark_mean, p->dark_sigma, dark, noise,
+                                           st);
+    for (int64_t f0 = 0; f0 < NF; f0 += 256) {
+      const int32_t nf = (int32_t)(NF - f0 < 256 ? NF - f0 : 256);
+      k_dense_draw<<<(P + 127) / 128, 128>>>(P, f0, nf, p->dark_frames, p->mean, p->read_noise,
+                                             p->adu_per_photon, da, ds, dark, dflat, noise, st,
+                                             out + (size_t)f0 * P);
+    }
+    ok = cudaDeviceSynchronize() == cudaSuccess;
+  }
+  cudaFree(da);
+  cudaFree(ds);
+  cudaFree(dark);
+  cudaFree(dflat);
+  cudaFree(noise);
+  cudaFree(st);
+  if (!ok) {
+    cudaFree(out);
+    return 1;
+  }
+  *out_dev = out;
+  return 0;
 }
 
 void xsg_free(void *dev) { cudaFree(dev); }

@@ -257,6 +257,10 @@ class Series:
         n = frames.size // (self.width * self.height)
         check(lib().xpcs_ingest_dense(self._h, _ptr(frames), n))
 
+    def ingest_dense_device(self, frames_dev_ptr: int, nframes: int):
+        """Dense frames already on this series' device: int16 [nframes][P]."""
+        check(lib().xpcs_ingest_dense_device(self._h, C.c_void_p(frames_dev_ptr), nframes))
+
     def dark(self):
         avg = np.empty(self.width * self.height, np.float64)
         std = np.empty_like(avg)

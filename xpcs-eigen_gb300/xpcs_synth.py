@@ -161,6 +161,9 @@ def glib():
         L.xsg_sparse.argtypes = [C.POINTER(_Params), C.c_void_p, C.c_void_p,
                                  C.POINTER(C.c_uint32), C.POINTER(C.c_void_p),
                                  C.POINTER(C.c_void_p)]
+        L.xsg_dense.restype = C.c_int
+        L.xsg_dense.argtypes = [C.POINTER(_Params), C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.POINTER(C.c_void_p)]
         L.xsg_free.argtypes = [C.c_void_p]
         L.xsg_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
         _glib = L
@@ -208,6 +211,44 @@ class DeviceFrames:
             glib().xsg_free(self.idx)
             glib().xsg_free(self.val)
             self.idx = self.val = None
+
+    def __del__(self):
+        self.close()
+
+
+class DeviceDenseFrames:
+    """The dense frames of ``DenseStream(acq)`` (``dark_frames`` darks, then
+    ``frames`` data frames) drawn on the current CUDA device: ``ptr`` is an
+    int16 [dark_frames + frames][P] device array.  Free with close()."""
+
+    def __init__(self, acq: Acquisition):
+        p = acq._struct()
+        a, s = pixel_fields(acq)
+        _, _, flat, _ = maps(acq)
+        flat = np.ascontiguousarray(flat.ravel(), np.float64)
+        out = C.c_void_p()
+        if glib().xsg_dense(C.byref(p), a.ctypes.data_as(C.c_void_p), s.ctypes.data_as(C.c_void_p),
+                            flat.ctypes.data_as(C.c_void_p), C.byref(out)) != 0:
+            raise MemoryError("xsg_dense failed")
+        self.P = acq.width * acq.height
+        self.dark_frames, self.frames = acq.dark_frames, acq.frames
+        self.ptr = out.value
+
+    def frame_ptr(self, k: int) -> int:
+        """Device address of sequence frame k (darks first)."""
+        return self.ptr + 2 * self.P * k
+
+    def to_host(self, first: int, count: int) -> np.ndarray:
+        out = np.empty((count, self.P), np.int16)
+        if count:
+            glib().xsg_to_host(out.ctypes.data_as(C.c_void_p), C.c_void_p(self.frame_ptr(first)),
+                               out.nbytes)
+        return out
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            glib().xsg_free(self.ptr)
+            self.ptr = None
 
     def __del__(self):
         self.close()
