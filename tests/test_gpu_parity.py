@@ -258,6 +258,35 @@ def test_dense_long_float_rows_vs_oracle(mode, dpl):
     assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
 
 
+def test_dense_stride_average_ragged_chunks_vs_oracle():
+    """Dense frames with stride 2 and averaging over 3, a detector width whose
+    rows are not a multiple of 8 pixels (no 16-byte loads), ingested in three
+    uneven parts."""
+    stride, avg, F = 2, 3, 150
+    acq = xs.Acquisition(width=37, height=29, frames=F * stride * avg, n_static=8, n_dynamic=4,
+                         mean=0.05, tau_min=3, tau_max=60, seed=19, dpl=4, dense=True,
+                         dark_frames=20, gain_min=0.9, gain_max=1.1)
+    dq, sq, flat, _ = xs.maps(acq)
+    ds = xs.DenseStream(acq)
+    raw = ds.next(acq.dark_frames + acq.frames)
+    ds.close()
+    data = raw[acq.dark_frames:]
+    lld, sigma = 1.0, 2.5
+    with xg.Series(acq.width, acq.height, F, acq.dpl, dq, sq, flatfield=flat, stride=stride,
+                   average=avg, dense=True, lld=lld, sigma=sigma) as s:
+        s.set_dark(raw[:acq.dark_frames])
+        for a, b in ((0, 250), (250, 650), (650, data.shape[0])):
+            s.ingest_dense(data[a:b])
+        s.multitau()
+        G2, IP, IF = s.g2ipif()
+    qm = oracle.QMap(dq, sq)
+    da, dsd = oracle.dark_image(raw[:acq.dark_frames], flat.ravel())
+    rows, _ = oracle.dense_filter(qm, data, F, da, dsd, lld, sigma, stride=stride, average=avg,
+                                  flat=flat.ravel())
+    oG2, oIP, oIF = oracle.multitau2(rows, F, acq.dpl, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
 @pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
 def test_sparse_float_rows_with_stale_tail_misses_vs_oracle(mode):
     """Sparse counts times a flatfield are float rows; on these the reference's

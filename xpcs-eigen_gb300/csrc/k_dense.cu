@@ -12,22 +12,22 @@
 // reference's own double/float operations; the streaming kernels then compare
 // int16 values only and evaluate the exact float arithmetic for kept pixels.
 //
-// Streaming is two passes over each chunk of frames, tile by tile (a block
-// keeps its pixels' R_min in registers across the chunk's frames): count the
-// kept pixels per (frame, tile), scan, then write (pixel, value) at the
-// scanned offsets, in pixel order within a frame.  Events stay frame-major,
-// as sparse frames are, and sub-frames that stride skips are not emitted.
+// Streaming is two passes over each chunk of frames.  A warp owns a tile of
+// 256 pixels (8 per lane, one 16-byte load per frame, R_min in registers) and
+// walks a slice of the chunk's frames, 4 frames in flight: the first pass
+// counts the kept pixels per (frame, tile), a scan turns the counts into
+// offsets, and the second pass writes (pixel, value) at the offsets, in pixel
+// order within a frame.  Events stay frame-major, as sparse frames are, and
+// frames that the stride skips are not emitted.
 #include <algorithm>
 #include <vector>
 
+#include "f64emu.cuh"
 #include "xpcs_internal.h"
 
 namespace xg {
 namespace {
 
-constexpr int KB_THREADS = 256;
-constexpr int KB_PPT = 4;                         // pixels per thread
-constexpr int KB_TILE = KB_THREADS * KB_PPT;      // pixels per tile
 constexpr int32_t KB_NEVER = 32768;               // R_min of a pixel that never passes
 
 // DarkImage::Compute: running mean and M2 in double over the dark frames of
@@ -54,6 +54,24 @@ __device__ __forceinline__ float dense_value(int32_t raw, bool dark, double avg)
   if (dark) {
     v = __double2float_rn(__dsub_rn((double)v, avg));
     v = v > 0.0f ? v : 0.0f;  // std::max(v, 0.0f)
+  }
+  return v;
+}
+
+// dense_value followed by the flatfield, as the reference forms a kept
+// event's value; the two double-rounded steps in integer arithmetic
+// (f64emu.cuh), in double precision only where that does not apply
+__device__ __forceinline__ float dense_event_value(int32_t raw, bool dark, double avg,
+                                                   const double *flat, int p) {
+  float v = (float)raw;
+  if (dark) {
+    if (!f32_int_minus_f64(raw, avg, v)) v = __double2float_rn(__dsub_rn((double)v, avg));
+    v = v > 0.0f ? v : 0.0f;  // std::max(v, 0.0f)
+  }
+  if (flat) {
+    const double g = flat[p];
+    float w;
+    v = f32_mul_f64(v, g, w) ? w : __double2float_rn(__dmul_rn((double)v, g));
   }
   return v;
 }
@@ -89,11 +107,19 @@ __global__ void k_rmin(int32_t P, const uint8_t *__restrict__ mask, int32_t has_
 
 struct ChunkCfg {
   const int16_t *raw;     // [n][P] frames of this chunk
-  int32_t n, P, T;        // frames, pixels, tiles
+  int32_t n, P, T;        // frames, pixels, warp tiles of KB_WPIX pixels
   int32_t r0;             // raw index of the chunk's first frame
   int32_t R_in, stride, F;
+  int32_t vec;            // rows are 16-byte aligned and P % 8 == 0
+  int32_t fslice;         // frames per block row of the grid
   const int32_t *rmin;
 };
+
+constexpr int KB_LPIX = 8;                 // pixels per lane (one 16-byte load)
+constexpr int KB_WPIX = 32 * KB_LPIX;      // pixels per warp tile
+constexpr int KB_WARPS = 8;                // warps (tiles) per block
+constexpr int KB_FU = 4;                   // frames a lane loads ahead (k_dense_write
+                                           // selects among exactly 4)
 
 __device__ __forceinline__ bool frame_used(const ChunkCfg &c, int f) {
   const int r = c.r0 + f;
@@ -101,80 +127,131 @@ __device__ __forceinline__ bool frame_used(const ChunkCfg &c, int f) {
   return k < c.F && ((r - k * c.R_in) % c.stride) == 0;
 }
 
-__global__ void __launch_bounds__(KB_THREADS)
-k_dense_count(ChunkCfg c, int32_t *__restrict__ counts) {
-  __shared__ int32_t wsum[KB_THREADS / 32];
-  const int t = blockIdx.x;
-  const int p0 = t * KB_TILE + threadIdx.x * KB_PPT;
-  int32_t rm[KB_PPT];
+// the lane's 8 raw values of frame f (pixels p0 .. p0+7, zero past P)
+__device__ __forceinline__ void load8(const ChunkCfg &c, int f, int p0, int16_t (&x)[KB_LPIX]) {
+  const int16_t *row = c.raw + (size_t)f * c.P;
+  if (c.vec && p0 + KB_LPIX <= c.P) {
+    const int4 u = __ldcs((const int4 *)(row + p0));
+    const int16_t *h = (const int16_t *)&u;
 #pragma unroll
-  for (int j = 0; j < KB_PPT; j++) rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
-  for (int f = 0; f < c.n; f++) {
-    int cnt = 0;
-    if (frame_used(c, f)) {
-      const int16_t *row = c.raw + (size_t)f * c.P;
+    for (int j = 0; j < KB_LPIX; j++) x[j] = h[j];
+  } else {
 #pragma unroll
-      for (int j = 0; j < KB_PPT; j++)
-        if (p0 + j < c.P && (int32_t)row[p0 + j] >= rm[j]) cnt++;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int s = 0;
-      for (int w = 0; w < KB_THREADS / 32; w++) s += wsum[w];
-      counts[(size_t)f * c.T + t] = s;
-    }
-    __syncthreads();
+    for (int j = 0; j < KB_LPIX; j++) x[j] = p0 + j < c.P ? __ldcs(row + p0 + j) : (int16_t)0;
   }
 }
 
-__global__ void __launch_bounds__(KB_THREADS)
+__device__ __forceinline__ unsigned keep_mask(const int16_t (&x)[KB_LPIX],
+                                              const int32_t (&rm)[KB_LPIX]) {
+  unsigned m = 0;
+#pragma unroll
+  for (int j = 0; j < KB_LPIX; j++) m |= ((int32_t)x[j] >= rm[j] ? 1u : 0u) << j;
+  return m;
+}
+
+// Grid: x = groups of KB_WARPS warp tiles, y = slices of c.fslice frames.
+// counts[f * T + t] = kept pixels of frame f in warp tile t (0 for frames the
+// stride skips).
+__global__ void __launch_bounds__(KB_WARPS * 32)
+k_dense_count(ChunkCfg c, int32_t *__restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const int t = blockIdx.x * KB_WARPS + (threadIdx.x >> 5);
+  if (t >= c.T) return;
+  const int p0 = t * KB_WPIX + lane * KB_LPIX;
+  int32_t rm[KB_LPIX];
+#pragma unroll
+  for (int j = 0; j < KB_LPIX; j++) rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
+  const int f0 = blockIdx.y * c.fslice, f1 = min(c.n, f0 + c.fslice);
+  for (int fb = f0; fb < f1; fb += KB_FU) {
+    int16_t x[KB_FU][KB_LPIX];
+    bool used[KB_FU];
+#pragma unroll
+    for (int u = 0; u < KB_FU; u++) {
+      used[u] = fb + u < f1 && frame_used(c, fb + u);
+      if (used[u]) load8(c, fb + u, p0, x[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < KB_FU; u++) {
+      const int k = used[u] ? __popc(keep_mask(x[u], rm)) : 0;
+      const int n = __reduce_add_sync(0xffffffffu, k);
+      if (lane == 0 && fb + u < f1) counts[(size_t)(fb + u) * c.T + t] = n;
+    }
+  }
+}
+
+// Writes (pixel, value) of every kept pixel at its scanned offset, in pixel
+// order within a frame, with value (float)((float)(raw - avg) * flat) as the
+// reference forms it.  The warp first gathers the kept pixels of its frames
+// in flight into shared memory (tile-local pixel, raw value), then all lanes
+// evaluate them in order, so the per-event arithmetic runs on full warps and
+// the stores are contiguous.
+__global__ void __launch_bounds__(KB_WARPS * 32)
 k_dense_write(ChunkCfg c, const int64_t *__restrict__ offsets, int64_t base,
               const double *__restrict__ avg, const double *__restrict__ flat, int32_t has_dark,
               int32_t *__restrict__ out_idx, float *__restrict__ out_val) {
-  __shared__ int32_t wsum[KB_THREADS / 32];
-  const int t = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int p0 = t * KB_TILE + threadIdx.x * KB_PPT;
-  int32_t rm[KB_PPT];
+  __shared__ uint8_t s_loc[KB_WARPS][KB_FU * KB_WPIX];
+  __shared__ int16_t s_raw[KB_WARPS][KB_FU * KB_WPIX];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = blockIdx.x * KB_WARPS + w;
+  if (t >= c.T) return;
+  const int tile0 = t * KB_WPIX, p0 = tile0 + lane * KB_LPIX;
+  int32_t rm[KB_LPIX];
 #pragma unroll
-  for (int j = 0; j < KB_PPT; j++) rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
-  for (int f = 0; f < c.n; f++) {
-    if (!frame_used(c, f)) continue;  // block-uniform
-    const int16_t *row = c.raw + (size_t)f * c.P;
-    int16_t rv[KB_PPT];
-    int cnt = 0;
+  for (int j = 0; j < KB_LPIX; j++) rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
+  const int f0 = blockIdx.y * c.fslice, f1 = min(c.n, f0 + c.fslice);
+  for (int fb = f0; fb < f1; fb += KB_FU) {
+    int16_t x[KB_FU][KB_LPIX];
+    int64_t o0[KB_FU];
+    bool used[KB_FU];
 #pragma unroll
-    for (int j = 0; j < KB_PPT; j++) {
-      rv[j] = p0 + j < c.P ? row[p0 + j] : (int16_t)0;
-      if (p0 + j < c.P && (int32_t)rv[j] >= rm[j]) cnt++;
+    for (int u = 0; u < KB_FU; u++) {
+      used[u] = fb + u < f1 && frame_used(c, fb + u);
+      o0[u] = used[u] ? offsets[(size_t)(fb + u) * c.T + t] : 0;
+      if (used[u]) load8(c, fb + u, p0, x[u]);
     }
-    // exclusive prefix of counts over the block (pixel order)
-    int x = cnt;
+    int start[KB_FU + 1];
+    start[0] = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[w] = x;
-    __syncthreads();
-    int before = 0;
-    for (int ww = 0; ww < w; ww++) before += wsum[ww];
-    int64_t o = base + offsets[(size_t)f * c.T + t] + before + x - cnt;
+    for (int u = 0; u < KB_FU; u++) {
+      const unsigned m = used[u] ? keep_mask(x[u], rm) : 0u;
+      const int cnt = __popc(m);
+      int incl = cnt;
 #pragma unroll
-    for (int j = 0; j < KB_PPT; j++) {
-      const int p = p0 + j;
-      if (p < c.P && (int32_t)rv[j] >= rm[j]) {
-        float v = dense_value(rv[j], has_dark, has_dark ? avg[p] : 0.0);
-        if (flat) v = __double2float_rn(__dmul_rn((double)v, flat[p]));
-        out_idx[o] = p;
-        out_val[o] = v;
-        o++;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
       }
+      int k = start[u] + incl - cnt;
+#pragma unroll
+      for (int j = 0; j < KB_LPIX; j++) {
+        if ((m >> j) & 1u) {
+          s_loc[w][k] = (uint8_t)(lane * KB_LPIX + j);
+          s_raw[w][k] = x[u][j];
+          k++;
+        }
+      }
+      start[u + 1] = start[u] + __shfl_sync(0xffffffffu, incl, 31);
     }
-    __syncthreads();
+    __syncwarp();
+    const int total = start[KB_FU];
+    for (int i = lane; i < total; i += 32) {
+      const int u = (i >= start[1]) + (i >= start[2]) + (i >= start[3]);
+      const int64_t ob = u == 0 ? o0[0] : (u == 1 ? o0[1] : (u == 2 ? o0[2] : o0[3]));
+      const int su = u == 0 ? 0 : (u == 1 ? start[1] : (u == 2 ? start[2] : start[3]));
+      const int p = tile0 + s_loc[w][i];
+      const int64_t o = base + ob + (i - su);
+      out_idx[o] = p;
+      out_val[o] = dense_event_value(s_raw[w][i], has_dark, has_dark ? avg[p] : 0.0, flat, p);
+    }
+    __syncwarp();
   }
+}
+
+// frame_end[f] = offsets[(f + 1) * T]: the end of frame f's events in the chunk
+__global__ void k_frame_ends(int32_t n, int32_t T, const int64_t *__restrict__ offsets,
+                             int64_t *__restrict__ frame_end) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < n) frame_end[f] = offsets[(size_t)(f + 1) * T];
 }
 
 }  // namespace
@@ -204,15 +281,22 @@ void dense_set_dark(Series &s, const int16_t *dark_host, int32_t nd) {
 
 void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_device) {
   cudaStream_t st = s.stream;
-  const int32_t P = s.P, T = (P + KB_TILE - 1) / KB_TILE;
+  const int32_t P = s.P, T = (P + KB_WPIX - 1) / KB_WPIX;
   if (!s.rmin_ready) dense_set_dark(s, nullptr, 0);
-  const int32_t chunk = std::max(1, std::min(nframes, (int32_t)std::max<int64_t>(1, (256ll << 20) / (2ll * P))));
+  // frames per pass: host frames go through a 256 MB staging buffer; frames
+  // already on the device are taken up to 4096 at a time (one host sync each)
+  const int64_t by_bytes = std::max<int64_t>(1, (256ll << 20) / (2ll * P));
+  const int32_t chunk = std::max(1, std::min(nframes, (int32_t)(on_device ? 4096 : by_bytes)));
   DBuf<int16_t> staging;
   if (!on_device) staging.reserve((size_t)chunk * P, st);
   s.dn_counts.reserve((size_t)chunk * T, st);
   s.dn_offsets.reserve((size_t)chunk * T + 1, st);
+  s.dn_frame_end.reserve((size_t)chunk, st);
   s.scan_tmp.reserve(scan_workspace_bytes((int64_t)chunk * T), st);
-  std::vector<int64_t> offs((size_t)chunk * T + 1);
+  std::vector<int64_t> ends((size_t)chunk);
+  int sms = 0;
+  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
+  const int gx = (T + KB_WARPS - 1) / KB_WARPS;
   for (int32_t f0 = 0; f0 < nframes; f0 += chunk) {
     const int32_t n = std::min(chunk, nframes - f0);
     const int16_t *src = frames + (size_t)f0 * P;
@@ -222,24 +306,32 @@ void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_dev
                               cudaMemcpyHostToDevice, st));
       raw = staging.p;
     }
-    ChunkCfg c{raw, n, P, T, s.raw_frames, s.R_in, s.desc.stride_frames, s.F, s.rmin.p};
-    k_dense_count<<<T, KB_THREADS, 0, st>>>(c, s.dn_counts.p);
+    // enough blocks for ~8 per SM, each over a slice of at least 16 frames
+    const int slices = std::max(1, std::min((n + 15) / 16, (8 * sms + gx - 1) / gx));
+    const int fslice = (n + slices - 1) / slices;
+    const int vec = (P % KB_LPIX == 0) && ((uintptr_t)raw % 16 == 0);
+    ChunkCfg c{raw, n, P, T, s.raw_frames, s.R_in, s.desc.stride_frames, s.F, vec, fslice,
+               s.rmin.p};
+    const dim3 grid(gx, (n + fslice - 1) / fslice);
+    k_dense_count<<<grid, KB_WARPS * 32, 0, st>>>(c, s.dn_counts.p);
     XG_CHECK_LAUNCH();
     exclusive_scan_i32_i64(s.dn_counts.p, s.dn_offsets.p, (int64_t)n * T, s.scan_tmp.p, st);
-    XG_CUDA(cudaMemcpyAsync(offs.data(), s.dn_offsets.p, sizeof(int64_t) * ((size_t)n * T + 1),
+    k_frame_ends<<<(n + 255) / 256, 256, 0, st>>>(n, T, s.dn_offsets.p, s.dn_frame_end.p);
+    XG_CHECK_LAUNCH();
+    XG_CUDA(cudaMemcpyAsync(ends.data(), s.dn_frame_end.p, sizeof(int64_t) * n,
                             cudaMemcpyDeviceToHost, st));
     XG_CUDA(cudaStreamSynchronize(st));
-    const int64_t add = offs[(size_t)n * T];
+    const int64_t add = ends[(size_t)n - 1];
     const int64_t old = s.raw_events, tot = old + add;
     if (tot >= ((int64_t)1 << 32))
       throw Error(XPCS_ERR_INVALID_ARGUMENT, "more than 2^32 events in one series");
     s.raw_idx.grow((size_t)(tot ? tot : 1), (size_t)old, st);
     s.raw_valf.grow((size_t)(tot ? tot : 1), (size_t)old, st);
-    k_dense_write<<<T, KB_THREADS, 0, st>>>(c, s.dn_offsets.p, old, s.dark_avg.p,
-                                            s.has_flat ? s.d_flat.p : nullptr, s.has_dark ? 1 : 0,
-                                            s.raw_idx.p, s.raw_valf.p);
+    k_dense_write<<<grid, KB_WARPS * 32, 0, st>>>(c, s.dn_offsets.p, old, s.dark_avg.p,
+                                                  s.has_flat ? s.d_flat.p : nullptr,
+                                                  s.has_dark ? 1 : 0, s.raw_idx.p, s.raw_valf.p);
     XG_CHECK_LAUNCH();
-    for (int32_t f = 0; f < n; f++) s.frame_off.push_back(old + offs[(size_t)(f + 1) * T]);
+    for (int32_t f = 0; f < n; f++) s.frame_off.push_back(old + ends[f]);
     s.raw_events = tot;
     s.raw_frames += n;
     s.frame_off_dirty = true;

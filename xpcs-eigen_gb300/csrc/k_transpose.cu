@@ -21,6 +21,7 @@
 //            160-172), pixelSum is accumulated in frame order, pixels outside
 //            the mask (sparse_filter.cpp:147) get empty rows, and every pixel
 //            is classified for the multi-tau kernels.
+#include "f64emu.cuh"
 #include "xpcs_internal.h"
 
 namespace xg {
@@ -101,7 +102,12 @@ __device__ __forceinline__ void raw_key(const RawCfg &c, int64_t i, int32_t &r, 
     return;
   }
   key = k >= 0 ? (uint32_t)p : (uint32_t)c.P;
-  if (!c.valf && c.flat) v = __double2float_rn(__dmul_rn((double)v, c.flat[p]));
+  if (!c.valf && c.flat) {
+    // (float)((double)v * flat), exactly, in integer arithmetic (f64emu.cuh)
+    const double g = c.flat[p];
+    float w;
+    v = f32_mul_f64(v, g, w) ? w : __double2float_rn(__dmul_rn((double)v, g));
+  }
 }
 
 // Item i of a tile in warp-striped order: warp w owns [w*32*IPT, (w+1)*32*IPT),

@@ -231,6 +231,7 @@ struct Series {
   bool has_dark = false, rmin_ready = false;
   DBuf<int32_t> dn_counts;
   DBuf<int64_t> dn_offsets;
+  DBuf<int64_t> dn_frame_end;
 
   // transpose / event lists
   DBuf<uint32_t> keyA, keyB;
