@@ -649,6 +649,8 @@ def main():
     ap.add_argument("--no-dense", action="store_true", help="skip the dense-frame measure")
     ap.add_argument("--dense-frames", type=int, default=20000)
     ap.add_argument("--dense-steps", type=int, default=3)
+    ap.add_argument("--dense-only", action="store_true",
+                    help="run only the dense-frame measure and print its object (profiling)")
     ap.add_argument("--serve-streams", type=int, default=16)
     ap.add_argument("--serve-hz", type=float, default=200.0)
     ap.add_argument("--serve-stagger", type=float, default=0.2, help="seconds between starts")
@@ -667,6 +669,10 @@ def main():
     try:
         if args.impl == "reference":
             run_reference_arm(args, dist)
+        elif args.dense_only:
+            r = run_dense(args, dist.local)
+            if dist.rank == 0:
+                print(json.dumps(r))
         else:
             run_gpu_arm(args, dist)
     finally:

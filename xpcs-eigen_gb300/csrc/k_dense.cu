@@ -127,25 +127,32 @@ __device__ __forceinline__ bool frame_used(const ChunkCfg &c, int f) {
   return k < c.F && ((r - k * c.R_in) % c.stride) == 0;
 }
 
-// the lane's 8 raw values of frame f (pixels p0 .. p0+7, zero past P)
-__device__ __forceinline__ void load8(const ChunkCfg &c, int f, int p0, int16_t (&x)[KB_LPIX]) {
+// the lane's 8 raw values of frame f (pixels p0 .. p0+7, zero past P), two
+// int16 per word
+__device__ __forceinline__ uint4 load8(const ChunkCfg &c, int f, int p0) {
   const int16_t *row = c.raw + (size_t)f * c.P;
   if (c.vec && p0 + KB_LPIX <= c.P) {
     const int4 u = __ldcs((const int4 *)(row + p0));
-    const int16_t *h = (const int16_t *)&u;
-#pragma unroll
-    for (int j = 0; j < KB_LPIX; j++) x[j] = h[j];
-  } else {
-#pragma unroll
-    for (int j = 0; j < KB_LPIX; j++) x[j] = p0 + j < c.P ? __ldcs(row + p0 + j) : (int16_t)0;
+    return make_uint4((uint32_t)u.x, (uint32_t)u.y, (uint32_t)u.z, (uint32_t)u.w);
   }
+  uint32_t h[KB_LPIX];
+#pragma unroll
+  for (int j = 0; j < KB_LPIX; j++)
+    h[j] = p0 + j < c.P ? (uint32_t)(uint16_t)__ldcs(row + p0 + j) : 0u;
+  return make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16),
+                    h[6] | (h[7] << 16));
 }
 
-__device__ __forceinline__ unsigned keep_mask(const int16_t (&x)[KB_LPIX],
-                                              const int32_t (&rm)[KB_LPIX]) {
+// raw value j (0..7) of a packed group
+__device__ __forceinline__ int32_t raw_at(const uint4 &x, int j) {
+  const uint32_t w = (j >> 1) == 0 ? x.x : ((j >> 1) == 1 ? x.y : ((j >> 1) == 2 ? x.z : x.w));
+  return (j & 1) ? ((int32_t)w >> 16) : ((int32_t)(w << 16) >> 16);
+}
+
+__device__ __forceinline__ unsigned keep_mask(const uint4 &x, const int32_t (&rm)[KB_LPIX]) {
   unsigned m = 0;
 #pragma unroll
-  for (int j = 0; j < KB_LPIX; j++) m |= ((int32_t)x[j] >= rm[j] ? 1u : 0u) << j;
+  for (int j = 0; j < KB_LPIX; j++) m |= (raw_at(x, j) >= rm[j] ? 1u : 0u) << j;
   return m;
 }
 
@@ -154,6 +161,7 @@ __device__ __forceinline__ unsigned keep_mask(const int16_t (&x)[KB_LPIX],
 // stride skips).
 __global__ void __launch_bounds__(KB_WARPS * 32)
 k_dense_count(ChunkCfg c, int32_t *__restrict__ counts) {
+  constexpr int FU = 2 * KB_FU;  // frames in flight: the count pass is load-bound
   const int lane = threadIdx.x & 31;
   const int t = blockIdx.x * KB_WARPS + (threadIdx.x >> 5);
   if (t >= c.T) return;
@@ -162,16 +170,16 @@ k_dense_count(ChunkCfg c, int32_t *__restrict__ counts) {
 #pragma unroll
   for (int j = 0; j < KB_LPIX; j++) rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
   const int f0 = blockIdx.y * c.fslice, f1 = min(c.n, f0 + c.fslice);
-  for (int fb = f0; fb < f1; fb += KB_FU) {
-    int16_t x[KB_FU][KB_LPIX];
-    bool used[KB_FU];
+  for (int fb = f0; fb < f1; fb += FU) {
+    uint4 x[FU];
+    bool used[FU];
 #pragma unroll
-    for (int u = 0; u < KB_FU; u++) {
+    for (int u = 0; u < FU; u++) {
       used[u] = fb + u < f1 && frame_used(c, fb + u);
-      if (used[u]) load8(c, fb + u, p0, x[u]);
+      if (used[u]) x[u] = load8(c, fb + u, p0);
     }
 #pragma unroll
-    for (int u = 0; u < KB_FU; u++) {
+    for (int u = 0; u < FU; u++) {
       const int k = used[u] ? __popc(keep_mask(x[u], rm)) : 0;
       const int n = __reduce_add_sync(0xffffffffu, k);
       if (lane == 0 && fb + u < f1) counts[(size_t)(fb + u) * c.T + t] = n;
@@ -185,7 +193,7 @@ k_dense_count(ChunkCfg c, int32_t *__restrict__ counts) {
 // in flight into shared memory (tile-local pixel, raw value), then all lanes
 // evaluate them in order, so the per-event arithmetic runs on full warps and
 // the stores are contiguous.
-__global__ void __launch_bounds__(KB_WARPS * 32)
+__global__ void __launch_bounds__(KB_WARPS * 32, 3)
 k_dense_write(ChunkCfg c, const int64_t *__restrict__ offsets, int64_t base,
               const double *__restrict__ avg, const double *__restrict__ flat, int32_t has_dark,
               int32_t *__restrict__ out_idx, float *__restrict__ out_val) {
@@ -200,14 +208,14 @@ k_dense_write(ChunkCfg c, const int64_t *__restrict__ offsets, int64_t base,
   for (int j = 0; j < KB_LPIX; j++) rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
   const int f0 = blockIdx.y * c.fslice, f1 = min(c.n, f0 + c.fslice);
   for (int fb = f0; fb < f1; fb += KB_FU) {
-    int16_t x[KB_FU][KB_LPIX];
+    uint4 x[KB_FU];
     int64_t o0[KB_FU];
     bool used[KB_FU];
 #pragma unroll
     for (int u = 0; u < KB_FU; u++) {
       used[u] = fb + u < f1 && frame_used(c, fb + u);
       o0[u] = used[u] ? offsets[(size_t)(fb + u) * c.T + t] : 0;
-      if (used[u]) load8(c, fb + u, p0, x[u]);
+      if (used[u]) x[u] = load8(c, fb + u, p0);
     }
     int start[KB_FU + 1];
     start[0] = 0;
@@ -226,7 +234,7 @@ k_dense_write(ChunkCfg c, const int64_t *__restrict__ offsets, int64_t base,
       for (int j = 0; j < KB_LPIX; j++) {
         if ((m >> j) & 1u) {
           s_loc[w][k] = (uint8_t)(lane * KB_LPIX + j);
-          s_raw[w][k] = x[u][j];
+          s_raw[w][k] = (int16_t)raw_at(x[u], j);
           k++;
         }
       }
@@ -306,8 +314,8 @@ void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_dev
                               cudaMemcpyHostToDevice, st));
       raw = staging.p;
     }
-    // enough blocks for ~8 per SM, each over a slice of at least 16 frames
-    const int slices = std::max(1, std::min((n + 15) / 16, (8 * sms + gx - 1) / gx));
+    // slices of up to 256 frames: many blocks per SM, R_min loaded once per slice
+    const int slices = std::max((n + 255) / 256, std::min((n + 15) / 16, (8 * sms + gx - 1) / gx));
     const int fslice = (n + slices - 1) / slices;
     const int vec = (P % KB_LPIX == 0) && ((uintptr_t)raw % 16 == 0);
     ChunkCfg c{raw, n, P, T, s.raw_frames, s.R_in, s.desc.stride_frames, s.F, vec, fslice,

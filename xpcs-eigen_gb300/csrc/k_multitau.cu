@@ -546,6 +546,7 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
 constexpr int FW_WARPS = 8;
 constexpr int FW_MAXC = 32;  // delays per level and largest delay in level units
 constexpr int FW_TSTRIDE = 33;
+constexpr int FW_WIN = 128;  // bins of the per-warp partner window
 
 __device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x) {
   int first = 0, len = n;
@@ -561,9 +562,23 @@ __device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x)
   return first;
 }
 
+// entries tb .. tb+31 of the level's row into their ring slots, with their
+// findable flags
+__device__ __forceinline__ void fw_load_tile(int tb, int lane, int L, int n0, bool all_find,
+                                             const int32_t *idx, const float *val, int32_t *ridx,
+                                             float *rval, uint8_t *rfind) {
+  const int j = tb + lane, slot = j & 63;
+  if (j < L) {
+    const int32_t x = idx[j];
+    ridx[slot] = x;
+    rval[slot] = val[j];
+    rfind[slot] = all_find ? 1 : (lower_bound_g(idx, n0, x) == j);
+  }
+}
+
 __global__ void __launch_bounds__(FW_WARPS * 32)
 k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
-           const DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
+           DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
            const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
            const float *__restrict__ ev_val, const float *__restrict__ fscale,
            int32_t *__restrict__ sc_frame, float *__restrict__ sc_val, float *__restrict__ G2,
@@ -574,16 +589,23 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   const bool ref = pl->mode == XPCS_MODE_REFERENCE;
   const McArrays ar = mc_arrays(plan_g, D);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // per warp: ring idx[64], val[64], findable[64]; terms [3 * acc][33]
-  const size_t wbytes = 64 * 9 + 3 * (size_t)acc_max * FW_TSTRIDE * 4;
+  // per warp: ring idx[64], val[64], findable[64]; bin window val[128],
+  // flag[128]; terms [3 * acc][33]
+  const size_t wbytes = 64 * 9 + FW_WIN * 5 + 3 * (size_t)acc_max * FW_TSTRIDE * 4;
   uint8_t *wb = fw_smem + (size_t)w * ((wbytes + 15) & ~(size_t)15);
   int32_t *ridx = (int32_t *)wb;
   float *rval = (float *)(wb + 256);
   uint8_t *rfind = wb + 512;
-  float *terms = (float *)(wb + 576);
+  float *bval = (float *)(wb + 576);
+  uint8_t *bflag = wb + 576 + FW_WIN * 4;
+  float *terms = (float *)(wb + 576 + FW_WIN * 5);
   const int nf = stats->nfloat;
-  const int wg = (blockIdx.x * FW_WARPS + w), nw = gridDim.x * FW_WARPS;
-  for (int q = wg; q < nf; q += nw) {
+  // pixels are handed out one per warp from a counter: rows differ in length
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(&stats->fnext, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= nf) break;
     const int p = flist[q];
     const int64_t b = row_ptr[p];
     const int n0 = row_len[p];
@@ -657,42 +679,62 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
       const int kmax = t0 + cnt - 1;
       const int nchain = 3 * cnt;
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      auto load_tile = [&](int tb) {
-        const int j = tb + lane, slot = j & 63;
-        if (j < L) {
-          const int32_t x = idx[j];
-          ridx[slot] = x;
-          rval[slot] = val[j];
-          rfind[slot] = all_find ? 1 : (lower_bound_g(idx, n0, x) == j);
-        } else {
-          ridx[slot] = INT_MAX;
-          rval[slot] = 0.f;
-          rfind[slot] = 0;
-        }
-      };
-      load_tile(0);
-      load_tile(32);
+      // ring slots past the row end are never read (partners stop at L)
+      fw_load_tile(0, lane, L, n0, all_find, idx, val, ridx, rval, rfind);
+      if (L > 32) fw_load_tile(32, lane, L, n0, all_find, idx, val, ridx, rval, rfind);
       for (int base = 0; base < L; base += 32) {
         __syncwarp();
         const int r = base + lane;
         const bool valid = r < L;
-        const int32_t src = ridx[r & 63];
-        const float v = rval[r & 63];
-        for (int c = 0; c < cnt; c++) {
-          const int tau = t0 + c;
-          terms[(size_t)c * FW_TSTRIDE + lane] = 0.f;
-          terms[(size_t)(cnt + c) * FW_TSTRIDE + lane] = (valid && src < lastframe - tau) ? v : 0.f;
-          terms[(size_t)(2 * cnt + c) * FW_TSTRIDE + lane] =
-              (valid && src >= tau && src < lastframe) ? v : 0.f;
+        const int nt = min(32, L - base);  // entries in this tile
+        const int32_t src = valid ? ridx[r & 63] : 0;
+        const float v = valid ? rval[r & 63] : 0.f;
+        // partners: when the tile and its partners span fewer than FW_WIN
+        // bins, through a per-warp bin array (one lookup per delay), else by
+        // scanning the following entries
+        const int32_t b0 = ridx[base & 63];
+        const bool use_bins = ridx[(base + nt - 1) & 63] + kmax - b0 < FW_WIN;
+        if (use_bins) {
+          ((uint32_t *)bflag)[lane] = 0u;  // FW_WIN = 128 flags
+          __syncwarp();
+          if (valid) {
+            bval[src - b0] = v;
+            bflag[src - b0] = rfind[r & 63];
+          }
+          const int q2 = base + 32 + lane;
+          if (lane < kmax && q2 < L) {
+            const int tb = ridx[q2 & 63] - b0;
+            if (tb < FW_WIN) {
+              bval[tb] = rval[q2 & 63];
+              bflag[tb] = rfind[q2 & 63];
+            }
+          }
+          __syncwarp();
         }
         if (valid) {
-          for (int k = t0 > 0 ? 1 : 0; k <= kmax; k++) {
-            const int qk = r + k;
-            if (qk >= L) break;
-            const int d = ridx[qk & 63] - src;
-            if (d > kmax) break;
-            if (d >= t0 && rfind[qk & 63] && src < lastframe - d)
-              terms[(size_t)(d - t0) * FW_TSTRIDE + lane] = __fmul_rn(v, rval[qk & 63]);
+          for (int c = 0; c < cnt; c++) {
+            const int tau = t0 + c;
+            terms[(size_t)(cnt + c) * FW_TSTRIDE + lane] = src < lastframe - tau ? v : 0.f;
+            terms[(size_t)(2 * cnt + c) * FW_TSTRIDE + lane] =
+                (src >= tau && src < lastframe) ? v : 0.f;
+          }
+          if (use_bins) {
+            for (int c = 0; c < cnt; c++) {
+              const int tau = t0 + c, tb = src + tau - b0;
+              const float g = __fmul_rn(v, bval[tb]);
+              terms[(size_t)c * FW_TSTRIDE + lane] =
+                  (bflag[tb] && src < lastframe - tau) ? g : 0.f;
+            }
+          } else {
+            for (int c = 0; c < cnt; c++) terms[(size_t)c * FW_TSTRIDE + lane] = 0.f;
+            for (int k = t0 > 0 ? 1 : 0; k <= kmax; k++) {
+              const int qk = r + k;
+              if (qk >= L) break;
+              const int d = ridx[qk & 63] - src;
+              if (d > kmax) break;
+              if (d >= t0 && rfind[qk & 63] && src < lastframe - d)
+                terms[(size_t)(d - t0) * FW_TSTRIDE + lane] = __fmul_rn(v, rval[qk & 63]);
+            }
           }
         }
         __syncwarp();
@@ -702,14 +744,18 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
           if (ch < nchain) {
             const float *tr = terms + (size_t)ch * FW_TSTRIDE;
             float a = acc[j];
+            if (nt == 32) {
 #pragma unroll 8
-            for (int i = 0; i < 32; i++) a = __fadd_rn(a, tr[i]);
+              for (int i = 0; i < 32; i++) a = __fadd_rn(a, tr[i]);
+            } else {
+              for (int i = 0; i < nt; i++) a = __fadd_rn(a, tr[i]);
+            }
             acc[j] = a;
           }
         }
         __syncwarp();
         // the tile after next replaces this one in the ring
-        load_tile(base + 64);
+        if (base + 64 < L) fw_load_tile(base + 64, lane, L, n0, all_find, idx, val, ridx, rval, rfind);
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -897,11 +943,16 @@ void run_multitau(Series &s, int mode) {
   int kmax = 0;
   for (int g = 0; g < hp->nlev; g++) kmax = std::max(kmax, hp->lv[g].tau_lo + hp->lv[g].count - 1);
   if (kmax <= FW_MAXC && hp->acc <= FW_MAXC) {
-    const size_t wb = (64 * 9 + 3 * (size_t)hp->acc * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
+    const size_t wb =
+        (64 * 9 + FW_WIN * 5 + 3 * (size_t)hp->acc * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
     const size_t smf = FW_WARPS * wb;
     XG_CUDA(cudaFuncSetAttribute(k_mt_fwarp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smf));
-    k_mt_fwarp<<<sms * 8, FW_WARPS * 32, smf, st>>>(
+    int per_sm = 0;
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mt_fwarp, FW_WARPS * 32,
+                                                          smf));
+    XG_CUDA(cudaMemsetAsync(&s.stats.p->fnext, 0, sizeof(int32_t), st));
+    k_mt_fwarp<<<sms * std::max(1, per_sm), FW_WARPS * 32, smf, st>>>(
         s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p, s.ev_frame.p, s.ev_val.p,
         fscale, s.sc_frame.p, s.sc_val.p, s.G2.p, s.IP.p, s.IF.p);
   } else {

@@ -173,6 +173,7 @@ struct DevStats {
   int32_t nvalid;
   int32_t nwarp;
   int32_t nlong;
+  int32_t fnext;  // next float-path pixel to hand out (k_mt_fwarp)
   unsigned long long events;
 };
 
