@@ -11,6 +11,7 @@
 //    floats, g around 1 (gains) and over a wide exponent range, and g = m / v
 //    rounded to double for float midpoints m (products within a few double
 //    ulps of a midpoint).
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -70,7 +71,9 @@ static bool single_round_differs_sub(int32_t r, double A, float got) {
   return fbits((float)once) != fbits(got);
 }
 
+static void check_sub_fast(int32_t r, double A);
 static void check_sub(int32_t r, double A) {
+  check_sub_fast(r, A);
   const float want = (float)((double)r - A);
   float got;
   checked++;
@@ -85,7 +88,37 @@ static void check_sub(int32_t r, double A) {
   if (single_round_differs_sub(r, A, got)) dr_cases++;
 }
 
+// the per-pixel fast forms of the dense filter, where they apply
+static long long fast_checked = 0;
+static void check_sub_fast(int32_t r, double A) {
+  const EmuSubPrep q = emu_sub_prep(A);
+  if (q.c0 == INT32_MIN) return;
+  const int64_t n = (int64_t)r - q.c0;
+  if (n < 1 || n >= (1 << 24)) return;
+  const float want = (float)((double)r - A);
+  const float got = f32_sub_fast((int32_t)n, q.G);
+  fast_checked++;
+  if (fbits(got) != fbits(want)) {
+    if (mismatches < 5) printf("sub_fast mismatch r=%d A=%.17g want=%.9g got=%.9g\n", r, A, want, got);
+    mismatches++;
+  }
+}
+
+static void check_mul_fast(float v, double g) {
+  const EmuMulPrep q = emu_mul_prep(g);
+  if (q.eg == INT32_MIN || !(v > 0.f)) return;
+  float got;
+  if (!f32_mul_fast(v, q, got)) return;
+  const float want = (float)((double)v * g);
+  fast_checked++;
+  if (fbits(got) != fbits(want)) {
+    if (mismatches < 5) printf("mul_fast mismatch v=%.9g g=%.17g want=%.9g got=%.9g\n", v, g, want, got);
+    mismatches++;
+  }
+}
+
 static void check_mul(float v, double g) {
+  check_mul_fast(v, g);
   const float want = (float)((double)v * g);
   float got;
   checked++;
@@ -162,6 +195,7 @@ int main() {
   check_mul(0.f, 1.25);
   check_mul(-0.f, 1.25);
   check_mul(3.f, -0.0);
+  if (fast_checked < 10000000) printf("fast forms checked on %lld operands only\n", fast_checked);
   printf("%lld %lld %lld %lld\n", mismatches, fallbacks, dr_cases, checked);
   return mismatches != 0;
 }

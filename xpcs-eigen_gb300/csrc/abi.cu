@@ -101,6 +101,7 @@ void free_series(Series *s) {
     s->dn_counts.release(st);
     s->dn_offsets.release(st);
     s->dn_frame_end.release(st);
+    s->dn_prep.release(st);
     s->d_frame_off.release(st);
     s->d_frame_map.release(st);
     s->d_chunk_frame.release(st);

@@ -189,4 +189,98 @@ XG_EMU_HD bool f32_mul_f64(float v, double g, float &out) {
   return emu_pack_f32(neg, M, e, out);
 }
 
+// ---- per-pixel forms for the dense filter's inner loop
+//
+// The dark level A and the flatfield g are fixed per pixel, so their
+// decomposition is done once.  For A in [2^-12, 2^30): c0 = ceil(A) and
+// G = (c0 - A) * 2^64 (exact), so that r - A = (r - c0) + G * 2^-64.  For g
+// normal and positive: its 53-bit significand and exponent.
+
+struct EmuSubPrep {
+  int32_t c0;   // INT32_MIN: use f32_int_minus_f64
+  uint64_t G;
+};
+
+XG_EMU_HD EmuSubPrep emu_sub_prep(double A) {
+  EmuSubPrep q{INT32_MIN, 0};
+  const uint64_t b = emu_f64_bits(A);
+  const int eb = (int)((b >> 52) & 0x7ff);
+  const int E = eb - 1023;
+  if ((b >> 63) || eb == 0 || E < -12 || E > 29) return q;
+  const uint64_t mA = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  const int64_t Ai = E >= 0 ? (int64_t)(mA >> (52 - E)) : 0;
+  const uint64_t F = mA << (E + 12);
+  q.c0 = (int32_t)(Ai + (F ? 1 : 0));
+  q.G = F ? (uint64_t)0 - F : 0;
+  return q;
+}
+
+// (float)((double)r - A) given the prep, for 1 <= r - c0 < 2^24: the value
+// n + G 2^-64 with n = r - c0 >= 1 has b = bitlen(n) integer bits, so the
+// double keeps 53 - b fraction bits of G and the float 24 - b of those.
+XG_EMU_HD float f32_sub_fast(int32_t n, uint64_t G) {
+  if (G == 0) return (float)n;
+  const int b = 64 - emu_clz64((uint64_t)(uint32_t)n);  // bitlen(n), 1 .. 24
+  const int sh1 = 11 + b;                                            // 12 .. 35
+  uint64_t f = G >> sh1;
+  const uint64_t rem = G & ((1ull << sh1) - 1), half = 1ull << (sh1 - 1);
+  if (rem > half || (rem == half && (f & 1))) f += 1;
+  if (f >> (53 - b)) {  // the double rounded up to the integer n + 1
+    return (float)(n + 1);
+  }
+  uint64_t m = ((uint64_t)n << (24 - b)) | (f >> 29);
+  const uint64_t rem2 = f & ((1ull << 29) - 1), half2 = 1ull << 28;
+  if (rem2 > half2 || (rem2 == half2 && (m & 1))) m += 1;
+  // m <= 2^24 and the scale 2^-(24-b) are exact in float
+  return (float)(uint32_t)m * emu_f32_from_bits((uint32_t)(127 - (24 - b)) << 23);
+}
+
+struct EmuMulPrep {
+  int32_t eg;   // INT32_MIN: use f32_mul_f64
+  uint64_t mg;  // 53-bit significand of g
+};
+
+XG_EMU_HD EmuMulPrep emu_mul_prep(double g) {
+  EmuMulPrep q{INT32_MIN, 0};
+  const uint64_t b = emu_f64_bits(g);
+  const int eb = (int)((b >> 52) & 0x7ff);
+  if ((b >> 63) || eb == 0 || eb == 0x7ff) return q;
+  q.eg = eb - 1075;
+  q.mg = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  return q;
+}
+
+// (float)((double)v * g) given the prep, for a normal v > 0; false when the
+// result leaves the normal float range.  The significand product has 76 or
+// 77 bits.
+XG_EMU_HD bool f32_mul_fast(float v, const EmuMulPrep &g, float &out) {
+  const uint32_t vb = emu_f32_bits(v);
+  const int ev = (int)(vb >> 23);  // v > 0: no sign bit
+  if (ev == 0 || ev == 0xff) return false;
+  const uint64_t mv = (vb & 0x7fffffu) | 0x800000u;
+  const uint64_t plo = mv * (g.mg & 0xffffffffu), phi = mv * (g.mg >> 32);
+  const uint64_t lo = plo + (phi << 32);
+  const uint64_t hi = (phi >> 32) + (lo < plo ? 1 : 0);  // 2^11 <= hi < 2^13
+  int sh = (hi >> 12) ? 24 : 23;                          // bits beyond 53
+  uint64_t q = (hi << (64 - sh)) | (lo >> sh);
+  const uint64_t rem = lo & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (q & 1))) q += 1;
+  if (q >> 53) {
+    q >>= 1;
+    sh += 1;
+  }
+  uint64_t m = q >> 29;
+  const uint64_t rem2 = q & ((1ull << 29) - 1), half2 = 1ull << 28;
+  if (rem2 > half2 || (rem2 == half2 && (m & 1))) m += 1;
+  int e = (ev - 150) + g.eg + sh + 29;
+  if (m >> 24) {
+    m >>= 1;
+    e += 1;
+  }
+  const int E = e + 23;  // value = 1.m * 2^E
+  if (E < -126 || E > 127) return false;
+  out = emu_f32_from_bits(((uint32_t)(E + 127) << 23) | ((uint32_t)m & 0x7fffffu));
+  return true;
+}
+
 }  // namespace xg

@@ -20,6 +20,7 @@
 // order within a frame.  Events stay frame-major, as sparse frames are, and
 // frames that the stride skips are not emitted.
 #include <algorithm>
+#include <climits>
 #include <vector>
 
 #include "f64emu.cuh"
@@ -58,20 +59,39 @@ __device__ __forceinline__ float dense_value(int32_t raw, bool dark, double avg)
   return v;
 }
 
+// Per-pixel forms of the dark level and the gain (f64emu.cuh).
+struct DensePrep {
+  EmuSubPrep sub;
+  EmuMulPrep mul;
+};
+
 // dense_value followed by the flatfield, as the reference forms a kept
-// event's value; the two double-rounded steps in integer arithmetic
-// (f64emu.cuh), in double precision only where that does not apply
-__device__ __forceinline__ float dense_event_value(int32_t raw, bool dark, double avg,
-                                                   const double *flat, int p) {
+// event's value: the two double-rounded steps in integer arithmetic
+// (f64emu.cuh), by the per-pixel short forms where they apply, else by the
+// general ones, and in double precision only outside their range
+__device__ __forceinline__ float dense_event_value(int32_t raw, bool dark, const double *avg,
+                                                   const double *flat, const DensePrep *prep,
+                                                   int p) {
   float v = (float)raw;
   if (dark) {
-    if (!f32_int_minus_f64(raw, avg, v)) v = __double2float_rn(__dsub_rn((double)v, avg));
+    const EmuSubPrep q = prep[p].sub;
+    const int64_t n = (int64_t)raw - q.c0;
+    if (q.c0 != INT32_MIN && n >= 1 && n < (1 << 24)) {
+      v = f32_sub_fast((int32_t)n, q.G);
+    } else {
+      const double A = avg[p];
+      if (!f32_int_minus_f64(raw, A, v)) v = __double2float_rn(__dsub_rn((double)v, A));
+    }
     v = v > 0.0f ? v : 0.0f;  // std::max(v, 0.0f)
   }
   if (flat) {
-    const double g = flat[p];
+    const EmuMulPrep q = prep[p].mul;
     float w;
-    v = f32_mul_f64(v, g, w) ? w : __double2float_rn(__dmul_rn((double)v, g));
+    if (!(q.eg != INT32_MIN && v > 0.f && f32_mul_fast(v, q, w))) {
+      const double g = flat[p];
+      if (!f32_mul_f64(v, g, w)) w = __double2float_rn(__dmul_rn((double)v, g));
+    }
+    v = w;
   }
   return v;
 }
@@ -79,9 +99,12 @@ __device__ __forceinline__ float dense_event_value(int32_t raw, bool dark, doubl
 // Smallest raw value (int16 range) that the filter keeps, per pixel.
 __global__ void k_rmin(int32_t P, const uint8_t *__restrict__ mask, int32_t has_dark,
                        const double *__restrict__ avg, const double *__restrict__ sd, float lld,
-                       float sigma, int32_t *__restrict__ rmin) {
+                       float sigma, const double *__restrict__ flat, int32_t *__restrict__ rmin,
+                       DensePrep *__restrict__ prep) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
+  prep[p].sub = has_dark ? emu_sub_prep(avg[p]) : EmuSubPrep{INT32_MIN, 0};
+  prep[p].mul = flat ? emu_mul_prep(flat[p]) : EmuMulPrep{INT32_MIN, 0};
   if (!mask[p]) {
     rmin[p] = KB_NEVER;
     return;
@@ -196,7 +219,8 @@ k_dense_count(ChunkCfg c, int32_t *__restrict__ counts) {
 __global__ void __launch_bounds__(KB_WARPS * 32, 3)
 k_dense_write(ChunkCfg c, const int64_t *__restrict__ offsets, int64_t base,
               const double *__restrict__ avg, const double *__restrict__ flat, int32_t has_dark,
-              int32_t *__restrict__ out_idx, float *__restrict__ out_val) {
+              const DensePrep *__restrict__ prep, int32_t *__restrict__ out_idx,
+              float *__restrict__ out_val) {
   __shared__ uint8_t s_loc[KB_WARPS][KB_FU * KB_WPIX];
   __shared__ int16_t s_raw[KB_WARPS][KB_FU * KB_WPIX];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -249,7 +273,7 @@ k_dense_write(ChunkCfg c, const int64_t *__restrict__ offsets, int64_t base,
       const int p = tile0 + s_loc[w][i];
       const int64_t o = base + ob + (i - su);
       out_idx[o] = p;
-      out_val[o] = dense_event_value(s_raw[w][i], has_dark, has_dark ? avg[p] : 0.0, flat, p);
+      out_val[o] = dense_event_value(s_raw[w][i], has_dark, avg, flat, prep, p);
     }
     __syncwarp();
   }
@@ -281,8 +305,11 @@ void dense_set_dark(Series &s, const int16_t *dark_host, int32_t nd) {
     XG_CHECK_LAUNCH();
     tmp.release(st);
   }
+  s.dn_prep.reserve(sizeof(DensePrep) * (size_t)P, st);
   k_rmin<<<(P + 255) / 256, 256, 0, st>>>(P, s.d_mask.p, s.has_dark ? 1 : 0, s.dark_avg.p,
-                                           s.dark_std.p, s.desc.lld, s.desc.sigma, s.rmin.p);
+                                           s.dark_std.p, s.desc.lld, s.desc.sigma,
+                                           s.has_flat ? s.d_flat.p : nullptr, s.rmin.p,
+                                           (DensePrep *)s.dn_prep.p);
   XG_CHECK_LAUNCH();
   s.rmin_ready = true;
 }
@@ -337,7 +364,9 @@ void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_dev
     s.raw_valf.grow((size_t)(tot ? tot : 1), (size_t)old, st);
     k_dense_write<<<grid, KB_WARPS * 32, 0, st>>>(c, s.dn_offsets.p, old, s.dark_avg.p,
                                                   s.has_flat ? s.d_flat.p : nullptr,
-                                                  s.has_dark ? 1 : 0, s.raw_idx.p, s.raw_valf.p);
+                                                  s.has_dark ? 1 : 0,
+                                                  (const DensePrep *)s.dn_prep.p, s.raw_idx.p,
+                                                  s.raw_valf.p);
     XG_CHECK_LAUNCH();
     for (int32_t f = 0; f < n; f++) s.frame_off.push_back(old + ends[f]);
     s.raw_events = tot;

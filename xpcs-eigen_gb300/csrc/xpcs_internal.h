@@ -233,6 +233,7 @@ struct Series {
   DBuf<int32_t> dn_counts;
   DBuf<int64_t> dn_offsets;
   DBuf<int64_t> dn_frame_end;
+  DBuf<uint8_t> dn_prep;  // per pixel: EmuSubPrep of the dark level, EmuMulPrep of the gain
 
   // transpose / event lists
   DBuf<uint32_t> keyA, keyB;
