@@ -543,7 +543,7 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
 //     memory, then each chain's lane adds its 32 terms in entry order.
 // Partners lie at most tau entries ahead (distinct ascending indices), so a
 // ring of two 32-entry tiles holds every partner of the current tile.
-constexpr int FW_WARPS = 8;
+constexpr int FW_WARPS = 4;
 constexpr int FW_MAXC = 32;  // delays per level and largest delay in level units
 constexpr int FW_TSTRIDE = 33;
 constexpr int FW_WIN = 128;  // bins of the per-warp partner window

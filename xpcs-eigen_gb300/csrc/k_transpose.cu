@@ -29,8 +29,8 @@ namespace {
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_IPT = 16;                      // items per lane
-constexpr int RS_TILE = RS_THREADS * RS_IPT;    // 4096
+constexpr int RS_IPT = 8;                       // items per lane
+constexpr int RS_TILE = RS_THREADS * RS_IPT;    // 2048
 constexpr int RS_DIGITS = 256;
 static_assert(RS_THREADS == RS_DIGITS, "one digit per thread in the downsweep scan");
 
@@ -61,9 +61,9 @@ struct PassCfg {
   uint32_t sentinel;
 };
 
-// Raw frame of the first item of every 512-item chunk (one warp's share of a
-// tile): chunk c starts in frame r when off[r] <= 512 c < off[r + 1].
-constexpr int RS_CHUNK = 512;
+// Raw frame of the first item of every RS_CHUNK-item chunk (one warp's share of a
+// tile): chunk c starts in frame r when off[r] <= RS_CHUNK c < off[r + 1].
+constexpr int RS_CHUNK = 32 * RS_IPT;
 
 __global__ void k_chunk_frames(int32_t nframes, const int64_t *__restrict__ off, int64_t nchunks,
                                int32_t *__restrict__ chunk_frame) {
