@@ -7,7 +7,7 @@
 // pixel's events come out contiguous and in stream order (frame order).
 //
 //   pass 0   reads the raw events directly: per event it derives the filter
-//            frame (raw frame / (stride*avg), from a per-512-event table of
+//            frame (raw frame / (stride*avg), from a per-warp-chunk table of
 //            raw frames and a per-raw-frame table of filter frames), drops
 //            unused stride sub-frames and frames past the end (key = P, sorts
 //            last), and forms v = (float)(value * flatfield) as the reference
@@ -29,8 +29,9 @@ namespace {
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_IPT = 8;                       // items per lane
-constexpr int RS_TILE = RS_THREADS * RS_IPT;    // 2048
+// Items per lane: 8 (tiles of 2048) keeps more blocks resident; above
+// RS_BIG_N events 16 (tiles of 4096) halves the tile histograms.
+constexpr int64_t RS_BIG_N = (int64_t)1 << 27;
 constexpr int RS_DIGITS = 256;
 static_assert(RS_THREADS == RS_DIGITS, "one digit per thread in the downsweep scan");
 
@@ -40,7 +41,7 @@ struct RawCfg {
   const float *valf;    // dense series: values already filtered by K-b
   const int64_t *frame_off;  // [nframes+1]
   const int32_t *frame_map;  // [nframes]: filter frame of a raw frame, -1 if unused
-  const int32_t *chunk_frame;  // [ceil(n / 512)]: raw frame of item 512 c
+  const int32_t *chunk_frame;  // [ceil(n / chunk)]: raw frame of item chunk * c
   int32_t nframes;
   int64_t n;
   int32_t P, F, R_in, stride;
@@ -61,16 +62,14 @@ struct PassCfg {
   uint32_t sentinel;
 };
 
-// Raw frame of the first item of every RS_CHUNK-item chunk (one warp's share of a
-// tile): chunk c starts in frame r when off[r] <= RS_CHUNK c < off[r + 1].
-constexpr int RS_CHUNK = 32 * RS_IPT;
-
+// Raw frame of the first item of every chunk of 32 * IPT items (one warp's
+// share of a tile): chunk c starts in frame r when off[r] <= chunk c < off[r + 1].
 __global__ void k_chunk_frames(int32_t nframes, const int64_t *__restrict__ off, int64_t nchunks,
-                               int32_t *__restrict__ chunk_frame) {
+                               int32_t chunk, int32_t *__restrict__ chunk_frame) {
   const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nframes) return;
-  const int64_t c0 = (off[r] + RS_CHUNK - 1) / RS_CHUNK;
-  const int64_t c1 = min((off[r + 1] + RS_CHUNK - 1) / RS_CHUNK, nchunks);
+  const int64_t c0 = (off[r] + chunk - 1) / chunk;
+  const int64_t c1 = min((off[r + 1] + chunk - 1) / chunk, nchunks);
   for (int64_t c = c0; c < c1; c++) chunk_frame[c] = r;
 }
 
@@ -112,33 +111,34 @@ __device__ __forceinline__ void raw_key(const RawCfg &c, int64_t i, int32_t &r, 
 
 // Item i of a tile in warp-striped order: warp w owns [w*32*IPT, (w+1)*32*IPT),
 // round k, lane l -> w*32*IPT + k*32 + l.
+template <int IPT>
 __device__ __forceinline__ int64_t item_index(int tile, int w, int k, int lane) {
-  return (int64_t)tile * RS_TILE + (int64_t)w * 32 * RS_IPT + k * 32 + lane;
+  return (int64_t)tile * (RS_THREADS * IPT) + (int64_t)w * 32 * IPT + k * 32 + lane;
 }
 
-template <bool FIRST>
+template <int IPT, bool FIRST>
 __global__ void __launch_bounds__(RS_THREADS)
 k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restrict__ cnt) {
   __shared__ uint32_t h[RS_DIGITS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS) h[d] = 0;
   __syncthreads();
-  uint32_t key[RS_IPT];
+  uint32_t key[IPT];
   // all loads first, so that they are in flight together
   if (FIRST) {
-    const int64_t nch = (rc.n + RS_CHUNK - 1) / RS_CHUNK;
+    const int64_t nch = (rc.n + 32 * IPT - 1) / (32 * IPT);
     int32_t r = rc.chunk_frame[min((int64_t)tile * RS_WARPS + w, nch - 1)];
     int64_t nb = rc.frame_off[r + 1];
     int32_t kf = rc.frame_map[r];
-    int32_t pix[RS_IPT];
+    int32_t pix[IPT];
 #pragma unroll
-    for (int k = 0; k < RS_IPT; k++) {
-      const int64_t i = item_index(tile, w, k, lane);
+    for (int k = 0; k < IPT; k++) {
+      const int64_t i = item_index<IPT>(tile, w, k, lane);
       pix[k] = i < pc.n ? rc.idx[i] : 0;
     }
 #pragma unroll
-    for (int k = 0; k < RS_IPT; k++) {
-      int64_t i = item_index(tile, w, k, lane);
+    for (int k = 0; k < IPT; k++) {
+      int64_t i = item_index<IPT>(tile, w, k, lane);
       key[k] = 0xffffffffu;
       if (i < pc.n) {
         while (nb <= i) {
@@ -152,13 +152,13 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < RS_IPT; k++) {
-      int64_t i = item_index(tile, w, k, lane);
+    for (int k = 0; k < IPT; k++) {
+      int64_t i = item_index<IPT>(tile, w, k, lane);
       key[k] = i < pc.n ? pc.key_in[i] : 0xffffffffu;
     }
   }
 #pragma unroll
-  for (int k = 0; k < RS_IPT; k++) {
+  for (int k = 0; k < IPT; k++) {
     if (key[k] == 0xffffffffu) continue;
     if (FIRST && key[k] != pc.sentinel) atomicAdd(&cnt[key[k]], 1);
     atomicAdd(&h[(key[k] >> pc.shift) & (RS_DIGITS - 1)], 1u);
@@ -170,57 +170,58 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
 
 // Shared memory of the downsweep: per-warp digit counters, the tile's global
 // and local digit offsets, and the tile staged in digit order.
+template <int IPT>
 struct DsSmem {
   uint32_t wcnt[RS_WARPS][RS_DIGITS];
   uint32_t toff[RS_DIGITS];
   uint32_t tstart[RS_DIGITS];
   uint32_t wtot[RS_THREADS / 32];
-  uint32_t key[RS_TILE];
-  int32_t fr[RS_TILE];
-  float v[RS_TILE];
+  uint32_t key[RS_THREADS * IPT];
+  int32_t fr[RS_THREADS * IPT];
+  float v[RS_THREADS * IPT];
 };
 
-template <bool FIRST, bool LAST>
+template <int IPT, bool FIRST, bool LAST>
 __global__ void __launch_bounds__(RS_THREADS)
 k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   extern __shared__ __align__(16) uint8_t ds_raw[];
-  DsSmem &sm = *reinterpret_cast<DsSmem *>(ds_raw);
+  DsSmem<IPT> &sm = *reinterpret_cast<DsSmem<IPT> *>(ds_raw);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
   for (int d = lane; d < RS_DIGITS; d += 32) sm.wcnt[w][d] = 0;
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
     sm.toff[d] = offsets[(int64_t)d * pc.ntiles + tile];
   __syncwarp();
 
-  uint32_t key[RS_IPT];
-  int32_t fr[RS_IPT];
-  float v[RS_IPT];
-  uint32_t rank[RS_IPT];
+  uint32_t key[IPT];
+  int32_t fr[IPT];
+  float v[IPT];
+  uint32_t rank[IPT];
   const unsigned lt = (1u << lane) - 1u;
   // all loads first, so that they are in flight together
   if (FIRST) {
-    const int64_t nch = (rc.n + RS_CHUNK - 1) / RS_CHUNK;
+    const int64_t nch = (rc.n + 32 * IPT - 1) / (32 * IPT);
     int32_t r = rc.chunk_frame[min((int64_t)tile * RS_WARPS + w, nch - 1)];
     int64_t nb = rc.frame_off[r + 1];
     int32_t kf = rc.frame_map[r];
-    int32_t pix[RS_IPT];
+    int32_t pix[IPT];
 #pragma unroll
-    for (int k = 0; k < RS_IPT; k++) {
-      const int64_t i = item_index(tile, w, k, lane);
+    for (int k = 0; k < IPT; k++) {
+      const int64_t i = item_index<IPT>(tile, w, k, lane);
       pix[k] = 0;
       v[k] = 0.f;
       if (i < pc.n) raw_load(rc, i, pix[k], v[k]);
     }
 #pragma unroll
-    for (int k = 0; k < RS_IPT; k++) {
-      const int64_t i = item_index(tile, w, k, lane);
+    for (int k = 0; k < IPT; k++) {
+      const int64_t i = item_index<IPT>(tile, w, k, lane);
       key[k] = 0xffffffffu;
       fr[k] = 0;
       if (i < pc.n) raw_key(rc, i, r, nb, kf, pix[k], v[k], key[k], fr[k]);
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < RS_IPT; k++) {
-      int64_t i = item_index(tile, w, k, lane);
+    for (int k = 0; k < IPT; k++) {
+      int64_t i = item_index<IPT>(tile, w, k, lane);
       key[k] = 0xffffffffu;
       fr[k] = 0;
       v[k] = 0.f;
@@ -233,7 +234,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   }
   // stable rank within the warp: equal digits keep (round, lane) order
 #pragma unroll
-  for (int k = 0; k < RS_IPT; k++) {
+  for (int k = 0; k < IPT; k++) {
     const bool ok = key[k] != 0xffffffffu;
     uint32_t d = ok ? ((key[k] >> pc.shift) & (RS_DIGITS - 1)) : RS_DIGITS;
     unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -272,7 +273,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   __syncthreads();
   // stage the tile in digit order
 #pragma unroll
-  for (int k = 0; k < RS_IPT; k++) {
+  for (int k = 0; k < IPT; k++) {
     if (key[k] == 0xffffffffu) continue;
     const uint32_t d = (key[k] >> pc.shift) & (RS_DIGITS - 1);
     const uint32_t q = sm.tstart[d] + sm.wcnt[w][d] + rank[k];
@@ -451,13 +452,38 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
   record_class_warp(has, p, c, out, pclass, cl, stats);
 }
 
-template <bool FIRST, bool LAST>
-void launch_downsweep(int ntiles, size_t smem, cudaStream_t st, const RawCfg &rc,
-                      const PassCfg &pc, const uint32_t *offsets) {
-  XG_CUDA(cudaFuncSetAttribute(k_downsweep<FIRST, LAST>,
+template <int IPT, bool FIRST, bool LAST>
+void launch_downsweep(int ntiles, cudaStream_t st, const RawCfg &rc, const PassCfg &pc,
+                      const uint32_t *offsets) {
+  const size_t smem = sizeof(DsSmem<IPT>);
+  XG_CUDA(cudaFuncSetAttribute(k_downsweep<IPT, FIRST, LAST>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_downsweep<FIRST, LAST><<<ntiles, RS_THREADS, smem, st>>>(rc, pc, offsets);
+  k_downsweep<IPT, FIRST, LAST><<<ntiles, RS_THREADS, smem, st>>>(rc, pc, offsets);
 }
+
+// One radix pass: tile histograms, digit-major scan, stable scatter.
+template <int IPT>
+void radix_pass(Series &s, bool first, bool last, int ntiles, const RawCfg &rc,
+                const PassCfg &pc) {
+  cudaStream_t st = s.stream;
+  if (first)
+    k_upsweep<IPT, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+  else
+    k_upsweep<IPT, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+  XG_CHECK_LAUNCH();
+  exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
+  if (first && last)
+    launch_downsweep<IPT, true, true>(ntiles, st, rc, pc, s.hist_scan.p);
+  else if (first)
+    launch_downsweep<IPT, true, false>(ntiles, st, rc, pc, s.hist_scan.p);
+  else if (last)
+    launch_downsweep<IPT, false, true>(ntiles, st, rc, pc, s.hist_scan.p);
+  else
+    launch_downsweep<IPT, false, false>(ntiles, st, rc, pc, s.hist_scan.p);
+  XG_CHECK_LAUNCH();
+}
+
+int items_per_lane(int64_t n) { return n >= RS_BIG_N ? 16 : 8; }
 
 }  // namespace
 
@@ -469,7 +495,8 @@ bool radix_sort_triples(Series &s, uint32_t *key, int32_t *a, float *b, uint32_t
   cudaStream_t st = s.stream;
   if (n <= 0 || key_bits <= 0) return false;
   const int passes = (key_bits + 7) / 8;
-  const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+  const int ipt = items_per_lane(n);
+  const int ntiles = (int)((n + RS_THREADS * ipt - 1) / (RS_THREADS * ipt));
   s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
   s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);
   s.scan_tmp.reserve(scan_workspace_bytes((int64_t)RS_DIGITS * ntiles), st);
@@ -489,11 +516,10 @@ bool radix_sort_triples(Series &s, uint32_t *key, int32_t *a, float *b, uint32_t
     pc.key_out = kb[(pass + 1) & 1];
     pc.fr_out = ab[(pass + 1) & 1];
     pc.v_out = bb[(pass + 1) & 1];
-    k_upsweep<false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, nullptr);
-    XG_CHECK_LAUNCH();
-    exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
-    launch_downsweep<false, false>(ntiles, sizeof(DsSmem), st, rc, pc, s.hist_scan.p);
-    XG_CHECK_LAUNCH();
+    if (ipt == 16)
+      radix_pass<16>(s, false, false, ntiles, rc, pc);
+    else
+      radix_pass<8>(s, false, false, ntiles, rc, pc);
   }
   return (passes & 1) != 0;
 }
@@ -536,7 +562,8 @@ void run_filter_transpose(Series &s) {
   if (n > 0) {
     int nbits = 32 - __builtin_clz((unsigned)P);  // bits to hold P (the drop key)
     int passes = (nbits + 7) / 8;
-    int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+    const int ipt = items_per_lane(n);
+    int ntiles = (int)((n + RS_THREADS * ipt - 1) / (RS_THREADS * ipt));
     s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
     s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);
     size_t ws = scan_workspace_bytes((int64_t)RS_DIGITS * ntiles);
@@ -553,10 +580,11 @@ void run_filter_transpose(Series &s) {
       s.vB.reserve(n, st);
     }
     const bool dense = s.desc.dense != 0;
-    const int64_t nch = (n + RS_CHUNK - 1) / RS_CHUNK;
+    const int chunk = 32 * ipt;
+    const int64_t nch = (n + chunk - 1) / chunk;
     s.d_chunk_frame.reserve((size_t)nch, st);
     k_chunk_frames<<<(s.raw_frames + 255) / 256, 256, 0, st>>>(s.raw_frames, s.d_frame_off.p, nch,
-                                                              s.d_chunk_frame.p);
+                                                              chunk, s.d_chunk_frame.p);
     XG_CHECK_LAUNCH();
     RawCfg rc{s.raw_idx.p, dense ? nullptr : s.raw_val.p, dense ? s.raw_valf.p : nullptr,
               s.d_frame_off.p, s.d_frame_map.p, s.d_chunk_frame.p, s.raw_frames, n, P, s.F,
@@ -585,22 +613,10 @@ void run_filter_transpose(Series &s) {
         pc.fr_out = fbuf[pass & 1];
         pc.v_out = vbuf[pass & 1];
       }
-      if (first)
-        k_upsweep<true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+      if (ipt == 16)
+        radix_pass<16>(s, first, last, ntiles, rc, pc);
       else
-        k_upsweep<false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
-      XG_CHECK_LAUNCH();
-      exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
-      const size_t dsm = sizeof(DsSmem);
-      if (first && last)
-        launch_downsweep<true, true>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
-      else if (first)
-        launch_downsweep<true, false>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
-      else if (last)
-        launch_downsweep<false, true>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
-      else
-        launch_downsweep<false, false>(ntiles, dsm, st, rc, pc, s.hist_scan.p);
-      XG_CHECK_LAUNCH();
+        radix_pass<8>(s, first, last, ntiles, rc, pc);
     }
   } else {
     s.scan_tmp.reserve(scan_workspace_bytes(P), st);
