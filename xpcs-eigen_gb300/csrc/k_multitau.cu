@@ -590,8 +590,8 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   const McArrays ar = mc_arrays(plan_g, D);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // per warp: ring idx[64], val[64], findable[64]; bin window val[128],
-  // flag[128]; terms [3 * acc][33]
-  const size_t wbytes = 64 * 9 + FW_WIN * 5 + 3 * (size_t)acc_max * FW_TSTRIDE * 4;
+  // flag[128]; terms [3 * acc][33] and the shared IP/IF row [33]
+  const size_t wbytes = 64 * 9 + FW_WIN * 5 + (3 * (size_t)acc_max + 1) * FW_TSTRIDE * 4;
   uint8_t *wb = fw_smem + (size_t)w * ((wbytes + 15) & ~(size_t)15);
   int32_t *ridx = (int32_t *)wb;
   float *rval = (float *)(wb + 256);
@@ -599,6 +599,7 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   float *bval = (float *)(wb + 576);
   uint8_t *bflag = wb + 576 + FW_WIN * 4;
   float *terms = (float *)(wb + 576 + FW_WIN * 5);
+  float *vrow = terms + (size_t)3 * acc_max * FW_TSTRIDE;
   const int nf = stats->nfloat;
   // pixels are handed out one per warp from a counter: rows differ in length
   for (;;) {
@@ -711,19 +712,27 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
           }
           __syncwarp();
         }
+        // inside [kmax, lastframe - kmax) every IP and IF term of the tile is v:
+        // the IP/IF chains then read one shared row
+        const bool bulk = b0 >= kmax && ridx[(base + nt - 1) & 63] < lastframe - kmax;
         if (valid) {
-          for (int c = 0; c < cnt; c++) {
-            const int tau = t0 + c;
-            terms[(size_t)(cnt + c) * FW_TSTRIDE + lane] = src < lastframe - tau ? v : 0.f;
-            terms[(size_t)(2 * cnt + c) * FW_TSTRIDE + lane] =
-                (src >= tau && src < lastframe) ? v : 0.f;
+          if (bulk) {
+            vrow[lane] = v;
+          } else {
+            for (int c = 0; c < cnt; c++) {
+              const int tau = t0 + c;
+              terms[(size_t)(cnt + c) * FW_TSTRIDE + lane] = src < lastframe - tau ? v : 0.f;
+              terms[(size_t)(2 * cnt + c) * FW_TSTRIDE + lane] =
+                  (src >= tau && src < lastframe) ? v : 0.f;
+            }
           }
+          // a partner is a prefix entry, so it lies below lastframe and the
+          // reference's src < lastframe - tau test holds for every pair found
           if (use_bins) {
             for (int c = 0; c < cnt; c++) {
-              const int tau = t0 + c, tb = src + tau - b0;
+              const int tb = src + t0 + c - b0;
               const float g = __fmul_rn(v, bval[tb]);
-              terms[(size_t)c * FW_TSTRIDE + lane] =
-                  (bflag[tb] && src < lastframe - tau) ? g : 0.f;
+              terms[(size_t)c * FW_TSTRIDE + lane] = bflag[tb] ? g : 0.f;
             }
           } else {
             for (int c = 0; c < cnt; c++) terms[(size_t)c * FW_TSTRIDE + lane] = 0.f;
@@ -732,7 +741,7 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
               if (qk >= L) break;
               const int d = ridx[qk & 63] - src;
               if (d > kmax) break;
-              if (d >= t0 && rfind[qk & 63] && src < lastframe - d)
+              if (d >= t0 && rfind[qk & 63])
                 terms[(size_t)(d - t0) * FW_TSTRIDE + lane] = __fmul_rn(v, rval[qk & 63]);
             }
           }
@@ -742,7 +751,7 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
         for (int j = 0; j < 4; j++) {
           const int ch = lane + 32 * j;
           if (ch < nchain) {
-            const float *tr = terms + (size_t)ch * FW_TSTRIDE;
+            const float *tr = (bulk && ch >= cnt) ? vrow : terms + (size_t)ch * FW_TSTRIDE;
             float a = acc[j];
             if (nt == 32) {
 #pragma unroll 8
@@ -944,7 +953,7 @@ void run_multitau(Series &s, int mode) {
   for (int g = 0; g < hp->nlev; g++) kmax = std::max(kmax, hp->lv[g].tau_lo + hp->lv[g].count - 1);
   if (kmax <= FW_MAXC && hp->acc <= FW_MAXC) {
     const size_t wb =
-        (64 * 9 + FW_WIN * 5 + 3 * (size_t)hp->acc * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
+        (64 * 9 + FW_WIN * 5 + (3 * (size_t)hp->acc + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
     const size_t smf = FW_WARPS * wb;
     XG_CUDA(cudaFuncSetAttribute(k_mt_fwarp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smf));
