@@ -265,18 +265,49 @@ __global__ void k_gram_i64(int32_t nrows, int32_t F, int32_t r0,
     }
 }
 
-// C_acc[t1][t2] += G[t1][t2] / (sg[t1] sg[t2]) on the upper triangle; block
-// row t1 = blockIdx.y, columns t2 from blockIdx.x
+// The smoothing factors are reciprocals of sg (float64, one per frame, or one
+// for the averaged form), so that a matrix element costs multiplications
+// only: GB300 runs FP64 at a small fraction of its FP32 rate, and a float64
+// division is several times the cost of a multiplication.
+
+// C_acc[t1][t2] += G[t1][t2] * (1/sg[t1]) * (1/sg[t2]) on the upper triangle;
+// block row t1 = blockIdx.y, columns t2 from blockIdx.x
 template <bool I64>
 __global__ void k_tc_accum(int32_t F, const void *__restrict__ Gv, int64_t ldg,
-                           const double *__restrict__ sg, int32_t avg, double *__restrict__ Cacc) {
+                           const double *__restrict__ isg, int32_t avg,
+                           double *__restrict__ Cacc) {
   const int t1 = blockIdx.y, t2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (t2 >= F || t2 < t1) return;
   const double g = I64 ? (double)(long long)((const unsigned long long *)Gv)[(size_t)t1 * ldg + t2]
                        : (double)((const float *)Gv)[(size_t)t1 * ldg + t2];
   if (g == 0.0) return;
-  const double d = avg ? sg[0] * sg[0] : sg[t1] * sg[t2];
-  Cacc[(size_t)t1 * F + t2] += g / d;
+  const double a = avg ? isg[0] : isg[t1], b = avg ? isg[0] : isg[t2];
+  Cacc[(size_t)t1 * F + t2] += g * a * b;
+}
+
+// A q bin of one smoothing group: C_q = G / (sg sg) / pixels in one pass (the
+// same double operations as k_tc_accum into a zeroed C_acc and k_tc_final).
+// Only the upper triangle of the float64 scratch Cq is read later.
+template <bool I64>
+__global__ void k_tc_single(int32_t F, const void *__restrict__ Gv, int64_t ldg,
+                            const double *__restrict__ isg, int32_t avg, double inv_npix,
+                            double *__restrict__ Cq, float *__restrict__ C) {
+  const int t1 = blockIdx.y, t2 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t2 >= F) return;
+  const size_t i = (size_t)t1 * F + t2;
+  if (t2 < t1) {
+    C[i] = 0.f;
+    return;
+  }
+  const double g = I64 ? (double)(long long)((const unsigned long long *)Gv)[(size_t)t1 * ldg + t2]
+                       : (double)((const float *)Gv)[(size_t)t1 * ldg + t2];
+  double v = 0.0;
+  if (g != 0.0) {
+    const double a = avg ? isg[0] : isg[t1], b = avg ? isg[0] : isg[t2];
+    v = (0.0 + g * a * b) * inv_npix;
+  }
+  Cq[i] = v;
+  C[i] = (float)v;
 }
 
 __global__ void k_tc_final(int32_t F, double inv_npix, const double *__restrict__ Cacc,
@@ -357,21 +388,22 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
   s.tt_Cq.reserve((size_t)F * F + 1, st);
   std::vector<double> sg_host((size_t)G * (req.average ? 1 : F));
   const size_t smem = sizeof(TcSmem) + 1024;
-  cudaEvent_t g0 = nullptr, g1 = nullptr;
-  XG_CUDA(cudaEventCreate(&g0));
-  XG_CUDA(cudaEventCreate(&g1));
-  struct EvGuard {
-    cudaEvent_t a, b;
-    ~EvGuard() {
-      cudaEventDestroy(a);
-      cudaEventDestroy(b);
-    }
-  } evg{g0, g1};
   XG_CUDA(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int32_t gq = 0;  // group index across q bins
+  std::vector<cudaEvent_t> gram_ev;  // start/stop of every tensor-core Gram
+  struct EvList {
+    std::vector<cudaEvent_t> &v;
+    ~EvList() {
+      for (cudaEvent_t e : v) cudaEventDestroy(e);
+    }
+  } evl{gram_ev};
   for (int32_t q = 0; q < Q; q++) {
-    XG_CUDA(cudaMemsetAsync(s.tt_Cacc.p, 0, sizeof(double) * (size_t)F * F, st));
     const int32_t g_end = req.static_map ? lay.q_grp_end[q] : q + 1;
+    const bool single = g_end - gq == 1;  // C_q straight from the one Gram
+    const int32_t npix = lay.q_ptr[q + 1] - lay.q_ptr[q];
+    const double inv_npix = npix ? 1.0 / npix : 0.0;
+    float *Cout = s.tt_C.p + (size_t)q * F * F;
+    if (!single) XG_CUDA(cudaMemsetAsync(s.tt_Cacc.p, 0, sizeof(double) * (size_t)F * F, st));
     for (; gq < g_end; gq++) {
       const int32_t r0 = lay.grp_ptr[gq], nr = lay.grp_ptr[gq + 1] - r0;
       const int64_t Kp = std::max<int64_t>(TC_BK, ((int64_t)nr + TC_BK - 1) / TC_BK * TC_BK);
@@ -406,8 +438,14 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
           sgd[f] = v;
       }
       if (req.average) sgd[0] = mean / F;
-      XG_CUDA(cudaMemcpyAsync(s.tt_sgd.p, sgd, sizeof(double) * (req.average ? 1 : F),
-                              cudaMemcpyHostToDevice, st));
+      // every group has its own device copy of 1/sg, so no group waits for
+      // the previous one's kernels
+      const size_t nsg = req.average ? 1 : (size_t)F;
+      std::vector<double> isg(nsg);
+      for (size_t f = 0; f < nsg; f++) isg[f] = 1.0 / sgd[f];
+      double *sgdev = s.tt_sgd.p + (size_t)gq * (F + 1);
+      XG_CUDA(cudaMemcpyAsync(sgdev, isg.data(), sizeof(double) * nsg, cudaMemcpyHostToDevice,
+                              st));
       const bool tensor = !force_i64 && !(flags & 2) && bound < (1ull << 24);
       const size_t nF2 = (size_t)F * F;
       if (tensor) {
@@ -426,14 +464,23 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
                                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
           if (cr != CUDA_SUCCESS) throw Error(XPCS_ERR_CUDA, "tensor map encoding failed");
         }
-        XG_CUDA(cudaEventRecord(g0, st));
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        XG_CUDA(cudaEventCreate(&e0));
+        gram_ev.push_back(e0);
+        XG_CUDA(cudaEventCreate(&e1));
+        gram_ev.push_back(e1);
+        XG_CUDA(cudaEventRecord(e0, st));
         k_gram_tc<<<ntiles, 128, smem, st>>>(tma, tmb, (int32_t)(Kp / TC_BK), nrow, ncol,
                                              s.tt_Gf.p, Fp, s.tt_err.p);
         XG_CHECK_LAUNCH();
-        XG_CUDA(cudaEventRecord(g1, st));
+        XG_CUDA(cudaEventRecord(e1, st));
         o.gram_flop += (double)ntiles * 2.0 * TC_BM * TC_BN * (double)Kp;
-        k_tc_accum<false><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
-            F, s.tt_Gf.p, Fp, s.tt_sgd.p, req.average, s.tt_Cacc.p);
+        if (single)
+          k_tc_single<false><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
+              F, s.tt_Gf.p, Fp, sgdev, req.average, inv_npix, s.tt_Cq.p, Cout);
+        else
+          k_tc_accum<false><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
+              F, s.tt_Gf.p, Fp, sgdev, req.average, s.tt_Cacc.p);
         XG_CHECK_LAUNCH();
       } else {
         s.tt_Gi.reserve(nF2 + 1, st);
@@ -442,21 +489,20 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
                                                     s.row_ptr.p, s.row_len.p, s.ev_frame.p,
                                                     s.ev_val.p, s.tt_Gi.p, F);
         XG_CHECK_LAUNCH();
-        k_tc_accum<true><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
-            F, s.tt_Gi.p, F, s.tt_sgd.p, req.average, s.tt_Cacc.p);
+        if (single)
+          k_tc_single<true><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
+              F, s.tt_Gi.p, F, sgdev, req.average, inv_npix, s.tt_Cq.p, Cout);
+        else
+          k_tc_accum<true><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
+              F, s.tt_Gi.p, F, sgdev, req.average, s.tt_Cacc.p);
         XG_CHECK_LAUNCH();
       }
-      XG_CUDA(cudaStreamSynchronize(st));  // sgd is reused by the next group
-      if (tensor) {
-        float ms = 0.f;
-        XG_CUDA(cudaEventElapsedTime(&ms, g0, g1));
-        o.gram_ms += ms;
-      }
     }
-    const int32_t npix = lay.q_ptr[q + 1] - lay.q_ptr[q];
-    k_tc_final<<<(unsigned)(((size_t)F * F + 255) / 256), 256, 0, st>>>(
-        F, npix ? 1.0 / npix : 0.0, s.tt_Cacc.p, s.tt_Cq.p, s.tt_C.p + (size_t)q * F * F);
-    XG_CHECK_LAUNCH();
+    if (!single) {
+      k_tc_final<<<(unsigned)(((size_t)F * F + 255) / 256), 256, 0, st>>>(
+          F, inv_npix, s.tt_Cacc.p, s.tt_Cq.p, Cout);
+      XG_CHECK_LAUNCH();
+    }
     k_tc_diag<<<F, 256, 0, st>>>(Q, q, F, req.window, o.partials, s.tt_Cq.p, s.tt_full.p,
                                  s.tt_part.p);
     XG_CHECK_LAUNCH();
@@ -470,6 +516,11 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
   int32_t err = 0;
   XG_CUDA(cudaMemcpyAsync(&err, s.tt_err.p, sizeof(err), cudaMemcpyDeviceToHost, st));
   XG_CUDA(cudaStreamSynchronize(st));
+  for (size_t k = 0; k + 1 < gram_ev.size(); k += 2) {
+    float ms = 0.f;
+    XG_CUDA(cudaEventElapsedTime(&ms, gram_ev[k], gram_ev[k + 1]));
+    o.gram_ms += ms;
+  }
   if (err)  // a bounded wait of the tensor-core Gram expired
     throw Error(XPCS_ERR_CUDA, "tensor-core two-time: a pipeline wait timed out");
 }
