@@ -343,7 +343,9 @@ __device__ int compact_row(uint32_t *row, int m, int lastframe, int lane) {
 //   G2: per level, warp-cooperative compaction, then every lane takes the
 //     sources lane, lane+32, ... in one flat loop over (source, partner)
 //     visits into its own accumulators, summed over the warp at the end of
-//     the level.
+//     the level.  On sorted levels where a third of the bins hold an entry,
+//     the prefix-sum array (done with after IP/IF) holds the values by bin
+//     and a source finds each partner by one lookup.
 __global__ void __launch_bounds__(256)
 k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
           const int32_t *__restrict__ count_p, int32_t min_n, int32_t cap,
@@ -412,22 +414,42 @@ k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
       const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
       const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
       for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
-      int i = lane, j = lane + 1;
-      uint32_t wi = i < m ? row[i] : 0u;
-      uint32_t wj = j < m ? row[j] : 0u;
-      while (i < m) {
-        const int d = pk_t(wj) - pk_t(wi);
-        if (j < m && d <= thi) {
-          if (d >= tlo && (sorted || lower_bound_row(row, n0, pk_t(wj)) == j))
-            acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
-          j++;
-        } else {
-          i += 32;
-          if (i >= m) break;
-          wi = row[i];
-          j = i + 1;
+      const int lf = L.lastframe;
+      if (sorted && tlo >= 1 && lf <= cap && 3 * m >= lf) {
+        // at least a third of the level's bins hold an entry: the prefix sums
+        // S are done with, and S becomes the row's values by bin, so that each
+        // source finds its partner for every delay with one lookup (a missing
+        // bin reads 0, which adds nothing)
+        for (int bq = lane; bq < lf; bq += 32) S[bq] = 0;
+        __syncwarp();
+        for (int k = lane; k < m; k += 32) S[pk_t(row[k])] = pk_v(row[k]);
+        __syncwarp();
+        for (int i = lane; i < m; i += 32) {
+          const uint32_t wi = row[i];
+          const int ti = pk_t(wi), vi = pk_v(wi);
+          for (int k = 0; k < L.count; k++) {
+            const int tb = ti + tlo + k;
+            if (tb < lf) acc[k * 32] += vi * S[tb];
+          }
         }
-        wj = j < m ? row[j] : 0u;
+      } else {
+        int i = lane, j = lane + 1;
+        uint32_t wi = i < m ? row[i] : 0u;
+        uint32_t wj = j < m ? row[j] : 0u;
+        while (i < m) {
+          const int d = pk_t(wj) - pk_t(wi);
+          if (j < m && d <= thi) {
+            if (d >= tlo && (sorted || lower_bound_row(row, n0, pk_t(wj)) == j))
+              acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
+            j++;
+          } else {
+            i += 32;
+            if (i >= m) break;
+            wi = row[i];
+            j = i + 1;
+          }
+          wj = j < m ? row[j] : 0u;
+        }
       }
       int mine = 0;
       for (int k = 0; k < L.count; k++) {
