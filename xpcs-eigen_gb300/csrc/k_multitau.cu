@@ -343,7 +343,7 @@ __device__ int compact_row(uint32_t *row, int m, int lastframe, int lane) {
 //   G2: per level, warp-cooperative compaction, then every lane takes the
 //     sources lane, lane+32, ... in one flat loop over (source, partner)
 //     visits into its own accumulators, summed over the warp at the end of
-//     the level.  On sorted levels where a third of the bins hold an entry,
+//     the level.  On sorted levels where a fifth of the bins hold an entry,
 //     the prefix-sum array (done with after IP/IF) holds the values by bin
 //     and a source finds each partner by one lookup.
 __global__ void __launch_bounds__(256)
@@ -415,8 +415,8 @@ k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
       const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
       for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
       const int lf = L.lastframe;
-      if (sorted && tlo >= 1 && lf <= cap && 3 * m >= lf) {
-        // at least a third of the level's bins hold an entry: the prefix sums
+      if (sorted && tlo >= 1 && lf <= cap && 5 * m >= lf) {
+        // at least a fifth of the level's bins hold an entry: the prefix sums
         // S are done with, and S becomes the row's values by bin, so that each
         // source finds its partner for every delay with one lookup (a missing
         // bin reads 0, which adds nothing)
