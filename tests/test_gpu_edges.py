@@ -1,0 +1,76 @@
+"""Edge shapes through the C ABI against the oracle, bit for bit, in both modes:
+a two-pixel detector, detectors whose pixel count is not a multiple of a warp
+or a tile, fewer frames than delays per level, pixels with an event in every
+frame (rows past the 4096-event warp rows go to the float-row kernel), more
+than 65,536 frames (no packed integer rows), a fully masked detector and
+frames without events.  A one-pixel detector is refused: BuildQMap raises the
+static-partition total only from a bin's second pixel (quirk Q5), so the
+reference would index past its partition arrays."""
+import numpy as np
+import pytest
+
+import oracle
+import xpcs_gpu as xg
+from fixtures import same_bits, same_bits_nan
+
+pytestmark = pytest.mark.gpu
+
+
+def make(W, H, F, mean, seed, hot=(), mask_all=False, maxc=3, empty_every=0):
+    """Sparse frames with one static/dynamic bin over the detector: per frame
+    the pixels drawn with probability `mean` plus the `hot` pixels, counts in
+    [1, maxc]; every `empty_every`-th frame has no events."""
+    rng = np.random.default_rng(seed)
+    P = W * H
+    dq = np.full(P, 0 if mask_all else 1, np.int32)
+    sq = dq.copy()
+    nnz = np.zeros(F, np.uint32)
+    idx, val = [], []
+    for f in range(F):
+        sel = np.flatnonzero(rng.random(P) < mean)
+        sel = np.union1d(sel, np.asarray(hot, np.int64)).astype(np.int32)
+        if empty_every and f % empty_every == 0:
+            sel = sel[:0]
+        nnz[f] = sel.size
+        idx.append(sel)
+        val.append(rng.integers(1, maxc + 1, sel.size).astype(np.int16))
+    return (dq.reshape(H, W), sq.reshape(H, W), nnz, np.concatenate(idx).astype(np.int32),
+            np.concatenate(val).astype(np.int16))
+
+
+CASES = {
+    "two_pixels": dict(W=2, H=1, F=50, mean=0.5, seed=1),
+    "21_pixels_5_frames": dict(W=3, H=7, F=5, mean=0.3, seed=2),
+    "561_pixels_2_frames": dict(W=33, H=17, F=2, mean=0.2, seed=3),
+    "hot_rows_300": dict(W=40, H=40, F=300, mean=0.01, seed=4, hot=(5, 77, 1599)),
+    "hot_row_9000": dict(W=16, H=16, F=9000, mean=0.001, seed=5, hot=(100,)),
+    "70000_frames": dict(W=4, H=4, F=70000, mean=0.01, seed=6),
+    "empty_frames": dict(W=8, H=8, F=100, mean=0.1, seed=7, empty_every=3),
+    "masked": dict(W=8, H=8, F=60, mean=0.2, seed=8, mask_all=True),
+}
+
+
+@pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_edge_shapes_vs_oracle(name, mode):
+    c = dict(CASES[name])
+    W, H, F = c.pop("W"), c.pop("H"), c.pop("F")
+    dq, sq, nnz, idx, val = make(W, H, F, **c)
+    dpl = 4
+    with xg.Series(W, H, F, dpl, dq, sq) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, dpl, mode)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+    og, ose = oracle.normalize_f32(qm, oG2, oIP, oIF)
+    assert same_bits_nan(g32, og) and same_bits_nan(s32, ose)
+
+
+def test_one_pixel_detector_is_refused():
+    dq, sq, _, _, _ = make(1, 1, 10, 0.5, 9)
+    with pytest.raises(xg.XpcsError):
+        xg.Series(1, 1, 10, 4, dq, sq)
