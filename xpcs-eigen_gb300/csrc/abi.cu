@@ -91,7 +91,8 @@ void free_series(Series *s) {
                             &s->d_ppb};
     for (auto *b : i32) b->release(st);
     DBuf<float> *f32[] = {&s->vA, &s->vB, &s->ev_val, &s->pixels_sum, &s->sc_val, &s->G2,
-                          &s->IP, &s->IF, &s->n_ratio32, &s->n_g2f, &s->n_sef};
+                          &s->IP, &s->IF, &s->n_ratio32, &s->n_g2f, &s->n_sef, &s->n_tg,
+                          &s->n_ti, &s->n_tf, &s->n_tx};
     for (auto *b : f32) b->release(st);
     s->raw_val.release(st);
     s->raw_valf.release(st);

@@ -805,26 +805,6 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   }
 }
 
-// The float nearest to 1/b (ties to even) for an integer b in [1, 2^24]:
-// candidates around the double quotient compared by their exact residuals
-// (g*b has at most 48 significant bits, so 1 - g*b is exact in double).
-float recip_rn(int32_t b) {
-  const float f = (float)(1.0 / (double)b);
-  float best = f;
-  double be = std::fabs(1.0 - (double)f * b);
-  for (float g : {std::nextafter(f, 0.f), std::nextafter(f, 2.f * f)}) {
-    const double e = std::fabs(1.0 - (double)g * b);
-    uint32_t gb, bb;
-    std::memcpy(&gb, &g, 4);
-    std::memcpy(&bb, &best, 4);
-    if (e < be || (e == be && (gb & 1u) == 0 && (bb & 1u) != 0)) {
-      best = g;
-      be = e;
-    }
-  }
-  return best;
-}
-
 // Host-side plan: level groups of the delay schedule with the lastframe each
 // sees and whether the reference compacts before it (corr.cpp:341-391).
 std::vector<uint8_t> make_plan(const Series &s, int mode) {
@@ -909,6 +889,26 @@ size_t warp_smem(int D, int acc, int cap, int warps) {
 }
 
 }  // namespace
+
+// The float nearest to 1/b (ties to even) for an integer b in [1, 2^24]:
+// candidates around the double quotient compared by their exact residuals
+// (g*b has at most 48 significant bits, so 1 - g*b is exact in double).
+float recip_rn(int32_t b) {
+  const float f = (float)(1.0 / (double)b);
+  float best = f;
+  double be = std::fabs(1.0 - (double)f * b);
+  for (float g : {std::nextafter(f, 0.f), std::nextafter(f, 2.f * f)}) {
+    const double e = std::fabs(1.0 - (double)g * b);
+    uint32_t gb, bb;
+    std::memcpy(&gb, &g, 4);
+    std::memcpy(&bb, &best, 4);
+    if (e < be || (e == be && (gb & 1u) == 0 && (bb & 1u) != 0)) {
+      best = g;
+      be = e;
+    }
+  }
+  return best;
+}
 
 void run_multitau(Series &s, int mode) {
   cudaStream_t st = s.stream;

@@ -21,8 +21,14 @@
 //                  and the chunks' (n, mean, M2) merged in order with Chan's
 //                  pairwise update; stderr = sqrt(1/n) sqrt(M2/n) (:1043-1087).
 // float32 result (optional, bit-identical to the reference's float output):
-//   k_entry_f32 / k_q_f32 replay the reference's sequential float operations
-//   in its order, including the running-mean/M2 update of every pixel.
+//   k_f32_transpose / k_entry_f32 / k_q_f32 replay the reference's sequential
+//   float operations in its order, including the running-mean/M2 update of
+//   every pixel.
+#include <cuda_pipeline.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "xpcs_internal.h"
 
 namespace xg {
@@ -249,93 +255,193 @@ __global__ void k_norm_finish(int NQ, int D, const int32_t *__restrict__ qep,
 }
 
 // ------------------------------------------------ float32, reference order
+//
+// Every float sum below runs in the reference's order; what changes is where
+// its operands come from.  k_f32_transpose writes G2, IP, IF and the per-pixel
+// ratio x = G2 / (IP IF) (NaN -> 0) in q-ordered, pixel-major layout
+// [mapped pixel][tau], so the sequential sums of neighbouring taus (adjacent
+// threads) read adjacent words.  The running mean's division by the sample
+// count uses the correctly rounded reciprocal of the count (__frcp_rn) and
+// one FMA residual correction (Markstein; Muller et al., Handbook of
+// Floating-Point Arithmetic, ch. 4), which gives the IEEE quotient for every
+// float numerator and every integer count up to 65536 (checked exhaustively
+// against __fdiv_rn on the GPU); larger counts, zeros and non-finite
+// numerators use __fdiv_rn.
 
-__global__ void k_entry_f32(int NE, int D, int P, const int32_t *__restrict__ epp,
-                            const int32_t *__restrict__ pix, const float *__restrict__ G2,
-                            const float *__restrict__ IP, const float *__restrict__ IF,
-                            float *__restrict__ ratio) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= NE * D) return;
-  const int e = idx / D, t = idx - e * D;
-  const size_t o = (size_t)t * P;
-  float sg = 0.f, si = 0.f, sf = 0.f;
-  const int k0 = epp[e], k1 = epp[e + 1];
-  int k = k0;
-  for (; k + 8 <= k1; k += 8) {  // loads ahead of the three dependent sums
-    float g[8], a[8], b[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int p = pix[k + j];
-      g[j] = G2[o + p];
-      a[j] = IP[o + p];
-      b[j] = IF[o + p];
-    }
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      sg = __fadd_rn(sg, g[j]);
-      si = __fadd_rn(si, a[j]);
-      sf = __fadd_rn(sf, b[j]);
+constexpr int TR_K = 32, TR_T = 32;  // transpose tile: mapped pixels x taus
+
+__global__ void __launch_bounds__(256)
+k_f32_transpose(int NK, int D, int P, const int32_t *__restrict__ pix,
+                const float *__restrict__ G2, const float *__restrict__ IP,
+                const float *__restrict__ IF, float *__restrict__ Tg, float *__restrict__ Ti,
+                float *__restrict__ Tf, float *__restrict__ X) {
+  __shared__ float sg[TR_T][TR_K + 1], si[TR_T][TR_K + 1], sf[TR_T][TR_K + 1];
+  const int k0 = blockIdx.x * TR_K, t0 = blockIdx.y * TR_T;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  // read: lanes over mapped pixels (pixels of a ring run in raster order)
+  const int k = k0 + tx;
+  const int p = k < NK ? pix[k] : 0;
+  for (int r = ty; r < TR_T; r += 8) {
+    const int t = t0 + r;
+    if (k < NK && t < D) {
+      const size_t o = (size_t)t * P + p;
+      sg[r][tx] = G2[o];
+      si[r][tx] = IP[o];
+      sf[r][tx] = IF[o];
     }
   }
-  for (; k < k1; k++) {
-    const int p = pix[k];
-    sg = __fadd_rn(sg, G2[o + p]);
-    si = __fadd_rn(si, IP[o + p]);
-    sf = __fadd_rn(sf, IF[o + p]);
+  __syncthreads();
+  // write: lanes over taus
+  const int t = t0 + tx;
+  for (int r = ty; r < TR_K; r += 8) {
+    const int kk = k0 + r;
+    if (kk < NK && t < D) {
+      const float g = sg[tx][r], a = si[tx][r], b = sf[tx][r];
+      const size_t o = (size_t)kk * D + t;
+      Tg[o] = g;
+      Ti[o] = a;
+      Tf[o] = b;
+      const float x = __fdiv_rn(g, __fmul_rn(a, b));
+      X[o] = isnan(x) ? 0.f : x;
+    }
   }
-  const float c = (float)(k1 - k0);
-  sg = __fdiv_rn(sg, c);
-  si = __fdiv_rn(si, c);
-  sf = __fdiv_rn(sf, c);
-  ratio[(size_t)e * D + t] = __fdiv_rn(sg, __fmul_rn(si, sf));
 }
 
-__global__ void k_q_f32(int NQ, int D, int P, const int32_t *__restrict__ qep,
-                        const int32_t *__restrict__ qrow, const int32_t *__restrict__ epp,
-                        const int32_t *__restrict__ pix, const float *__restrict__ ratio,
-                        const float *__restrict__ G2, const float *__restrict__ IP,
-                        const float *__restrict__ IF, float *__restrict__ g2,
-                        float *__restrict__ se) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= NQ * D) return;
-  const int qi = idx / D, t = idx - qi * D;
-  const int row = qrow[qi];
-  const size_t o = (size_t)t * P;
-  float acc = 0.f, cnt = 0.f;
-  for (int e = qep[qi]; e < qep[qi + 1]; e++) {
-    float r = ratio[(size_t)e * D + t];
-    acc = __fadd_rn(acc, isnan(r) ? 0.f : r);
-    cnt = __fadd_rn(cnt, isnan(r) ? 0.f : 1.f);
+// a / n for the running mean: n is the (integer-valued) sample count and y
+// = __frcp_rn(n) its correctly rounded reciprocal, which depends on the count
+// only and so stays off the chain of dependent operations
+__device__ __forceinline__ float div_count(float a, float n, int ni, float y) {
+  if (ni > 65536 || a == 0.f || !isfinite(a) || fabsf(a) < 1e-30f) return __fdiv_rn(a, n);
+  const float q0 = __fmul_rn(a, y);
+  return __fmaf_rn(__fmaf_rn(-q0, n, a), y, q0);
+}
+
+// The replay kernels below run one block per q ring (or per entry) and one
+// thread per tau.  The rows [k][0..D) of the block's pixel range are streamed
+// into shared memory in chunks of `ch` rows (up to 32, fewer for long delay
+// lists) by asynchronous copies (two buffers: chunk c+1 is in flight while
+// the threads step through chunk c), so each thread's sequential chain reads
+// shared memory instead of waiting on global loads.
+constexpr int FR_SMEM = 200 * 1024;  // shared memory budget of a replay block
+
+// copies rows [r0, r0 + nrow) of the D-wide arrays into the shared buffers
+__device__ __forceinline__ void fr_issue(const float *const *src, float *const *dst, int narr,
+                                         int64_t r0, int nrow, int D) {
+  const int n = nrow * D;
+  for (int a = 0; a < narr; a++) {
+    const float *g = src[a] + (size_t)r0 * D;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) __pipeline_memcpy_async(dst[a] + i, g + i, 4);
   }
-  g2[(size_t)t * NQ + row] = __fdiv_rn(acc, cnt);
-  float avg = 0.f, sd = 0.f, samples = 0.f;
-  const int k0 = epp[qep[qi]], k1 = epp[qep[qi + 1]];
-  for (int k = k0; k < k1; k += 8) {
-    float xs[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {  // x of the next pixels ahead of the chain
-      xs[j] = 0.f;
-      if (k + j < k1) {
-        const int p = pix[k + j];
-        float x = __fdiv_rn(G2[o + p], __fmul_rn(IP[o + p], IF[o + p]));
-        xs[j] = isnan(x) ? 0.f : x;
+  __pipeline_commit();
+}
+
+// One block per entry, thread tau: the entry's sums of G2, IP, IF in pixel
+// order, / pixels, ratio (corr.cpp:966-1013).
+__global__ void k_entry_f32(int NE, int D, int FR_CH, const int32_t *__restrict__ epp,
+                            const float *__restrict__ Tg, const float *__restrict__ Ti,
+                            const float *__restrict__ Tf, float *__restrict__ ratio) {
+  extern __shared__ float fr_buf[];  // [2][3][FR_CH][D]
+  const int e = blockIdx.x, t = threadIdx.x;
+  const int k0 = epp[e], k1 = epp[e + 1];
+  const int n = k1 - k0, nch = (n + FR_CH - 1) / FR_CH;
+  const float *src[3] = {Tg, Ti, Tf};
+  float sg = 0.f, si = 0.f, sf = 0.f;
+  const size_t bw = (size_t)FR_CH * D;
+  if (nch > 0) {
+    float *d0[3] = {fr_buf, fr_buf + bw, fr_buf + 2 * bw};
+    fr_issue(src, d0, 3, k0, min(FR_CH, n), D);
+  }
+  for (int c = 0; c < nch; c++) {
+    if (c + 1 < nch) {
+      float *base = fr_buf + (size_t)((c + 1) & 1) * 3 * bw;
+      float *dn[3] = {base, base + bw, base + 2 * bw};
+      fr_issue(src, dn, 3, k0 + (int64_t)(c + 1) * FR_CH, min(FR_CH, n - (c + 1) * FR_CH), D);
+      __pipeline_wait_prior(1);
+    } else {
+      __pipeline_wait_prior(0);
+    }
+    __syncthreads();
+    if (t < D) {
+      const float *bg = fr_buf + (size_t)(c & 1) * 3 * bw, *bi = bg + bw, *bf = bg + 2 * bw;
+      const int rows = min(FR_CH, n - c * FR_CH);
+#pragma unroll 4
+      for (int r = 0; r < rows; r++) {
+        sg = __fadd_rn(sg, bg[r * D + t]);
+        si = __fadd_rn(si, bi[r * D + t]);
+        sf = __fadd_rn(sf, bf[r * D + t]);
       }
     }
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      if (k + j >= k1) break;
-      const float x = xs[j];
-      const float tmpAvg = avg;
-      samples = __fadd_rn(samples, 1.f);
-      float tmp00 = __fdiv_rn(__fsub_rn(x, tmpAvg), samples);
-      tmp00 = isnan(tmp00) ? 0.f : tmp00;
-      avg = __fadd_rn(avg, tmp00);
-      sd = __fadd_rn(sd, __fmul_rn(__fsub_rn(x, tmpAvg), __fsub_rn(x, avg)));
-    }
+    __syncthreads();
   }
-  const float stdNorm = __fdiv_rn(sd, samples);
-  const float inv = __fdiv_rn(1.f, samples);
-  se[(size_t)t * NQ + row] = __fmul_rn(__fsqrt_rn(inv), __fsqrt_rn(stdNorm));
+  if (t < D) {
+    const float cnt = (float)n;
+    sg = __fdiv_rn(sg, cnt);
+    si = __fdiv_rn(si, cnt);
+    sf = __fdiv_rn(sf, cnt);
+    ratio[(size_t)e * D + t] = __fdiv_rn(sg, __fmul_rn(si, sf));
+  }
+}
+
+// One block per q ring, thread tau: g2 = mean of the non-NaN entry ratios
+// (corr.cpp:1018-1040); stderr from the running mean / M2 over the ring's
+// pixels in order, NaN counted as 0 (corr.cpp:1043-1087).
+__global__ void k_q_f32(int NQ, int D, int FR_CH, const int32_t *__restrict__ qep,
+                        const int32_t *__restrict__ qrow, const int32_t *__restrict__ epp,
+                        const float *__restrict__ ratio, const float *__restrict__ X,
+                        float *__restrict__ g2, float *__restrict__ se) {
+  extern __shared__ float fr_buf[];  // [2][FR_CH][D]
+  const int qi = blockIdx.x, t = threadIdx.x;
+  const int row = qrow[qi];
+  if (t < D) {
+    float acc = 0.f, cnt = 0.f;
+    for (int e = qep[qi]; e < qep[qi + 1]; e++) {
+      float r = ratio[(size_t)e * D + t];
+      acc = __fadd_rn(acc, isnan(r) ? 0.f : r);
+      cnt = __fadd_rn(cnt, isnan(r) ? 0.f : 1.f);
+    }
+    g2[(size_t)t * NQ + row] = __fdiv_rn(acc, cnt);
+  }
+  float avg = 0.f, sd = 0.f, samples = 0.f;
+  int ns = 0;
+  const int k0 = epp[qep[qi]], k1 = epp[qep[qi + 1]];
+  const int n = k1 - k0, nch = (n + FR_CH - 1) / FR_CH;
+  const size_t bw = (size_t)FR_CH * D;
+  const float *src[1] = {X};
+  if (nch > 0) {
+    float *d0[1] = {fr_buf};
+    fr_issue(src, d0, 1, k0, min(FR_CH, n), D);
+  }
+  for (int c = 0; c < nch; c++) {
+    if (c + 1 < nch) {
+      float *dn[1] = {fr_buf + (size_t)((c + 1) & 1) * bw};
+      fr_issue(src, dn, 1, k0 + (int64_t)(c + 1) * FR_CH, min(FR_CH, n - (c + 1) * FR_CH), D);
+      __pipeline_wait_prior(1);
+    } else {
+      __pipeline_wait_prior(0);
+    }
+    __syncthreads();
+    if (t < D) {
+      const float *bx = fr_buf + (size_t)(c & 1) * bw;
+      const int rows = min(FR_CH, n - c * FR_CH);
+#pragma unroll 4
+      for (int r = 0; r < rows; r++) {
+        const float x = bx[r * D + t];
+        const float tmpAvg = avg;
+        samples = __fadd_rn(samples, 1.f);
+        ns++;
+        float tmp00 = div_count(__fsub_rn(x, tmpAvg), samples, ns, __frcp_rn(samples));
+        tmp00 = isnan(tmp00) ? 0.f : tmp00;
+        avg = __fadd_rn(avg, tmp00);
+        sd = __fadd_rn(sd, __fmul_rn(__fsub_rn(x, tmpAvg), __fsub_rn(x, avg)));
+      }
+    }
+    __syncthreads();
+  }
+  if (t < D) {
+    const float stdNorm = __fdiv_rn(sd, samples);
+    const float inv = __fdiv_rn(1.f, samples);
+    se[(size_t)t * NQ + row] = __fmul_rn(__fsqrt_rn(inv), __fsqrt_rn(stdNorm));
+  }
 }
 
 }  // namespace
@@ -384,18 +490,38 @@ void run_normalize(Series &s, bool want64, bool want32) {
     XG_CHECK_LAUNCH();
   }
   if (want32) {
+    const QMap &qm = s.qmap;
+    const int NK = qm.entry_pix_ptr.empty() ? 0 : qm.entry_pix_ptr.back();
     s.n_ratio32.reserve((size_t)(NE > 0 ? NE : 1) * D, st);
     s.n_g2f.reserve((size_t)NQ * D, st);
     s.n_sef.reserve((size_t)NQ * D, st);
-    const int bs = 32;
-    if (NE > 0) {
-      k_entry_f32<<<(NE * D + bs - 1) / bs, bs, 0, st>>>(NE, D, P, s.n_entry_pix_ptr.p, s.n_pix.p,
-                                                         s.G2.p, s.IP.p, s.IF.p, s.n_ratio32.p);
+    const size_t nt = (size_t)(NK > 0 ? NK : 1) * D;
+    s.n_tg.reserve(nt, st);
+    s.n_ti.reserve(nt, st);
+    s.n_tf.reserve(nt, st);
+    s.n_tx.reserve(nt, st);
+    if (NK > 0) {
+      k_f32_transpose<<<dim3((NK + TR_K - 1) / TR_K, (D + TR_T - 1) / TR_T), 256, 0, st>>>(
+          NK, D, P, s.n_pix.p, s.G2.p, s.IP.p, s.IF.p, s.n_tg.p, s.n_ti.p, s.n_tf.p, s.n_tx.p);
       XG_CHECK_LAUNCH();
     }
-    k_q_f32<<<(NQ * D + bs - 1) / bs, bs, 0, st>>>(NQ, D, P, s.n_q_entry_ptr.p, s.n_q_row.p,
-                                                  s.n_entry_pix_ptr.p, s.n_pix.p, s.n_ratio32.p,
-                                                  s.G2.p, s.IP.p, s.IF.p, s.n_g2f.p, s.n_sef.p);
+    if (D > 1024) throw Error(XPCS_ERR_INVALID_ARGUMENT, "more than 1024 delays");
+    const int bs = (D + 31) / 32 * 32;
+    const int ch_e = std::max(1, std::min(32, FR_SMEM / (24 * D)));
+    const int ch_q = std::max(1, std::min(32, FR_SMEM / (8 * D)));
+    const size_t sm_e = sizeof(float) * 2 * 3 * (size_t)ch_e * D;
+    const size_t sm_q = sizeof(float) * 2 * (size_t)ch_q * D;
+    XG_CUDA(cudaFuncSetAttribute(k_entry_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm_e));
+    XG_CUDA(cudaFuncSetAttribute(k_q_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm_q));
+    if (NE > 0) {
+      k_entry_f32<<<NE, bs, sm_e, st>>>(NE, D, ch_e, s.n_entry_pix_ptr.p, s.n_tg.p, s.n_ti.p,
+                                        s.n_tf.p, s.n_ratio32.p);
+      XG_CHECK_LAUNCH();
+    }
+    k_q_f32<<<NQ, bs, sm_q, st>>>(NQ, D, ch_q, s.n_q_entry_ptr.p, s.n_q_row.p, s.n_entry_pix_ptr.p,
+                                  s.n_ratio32.p, s.n_tx.p, s.n_g2f.p, s.n_sef.p);
     XG_CHECK_LAUNCH();
   }
 }

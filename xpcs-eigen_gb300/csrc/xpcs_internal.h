@@ -273,6 +273,7 @@ struct Series {
   // normalisation
   DBuf<int32_t> n_q_entry_ptr, n_entry_sbin, n_entry_pix_ptr, n_pix, n_q_row;
   DBuf<float> n_ratio32;
+  DBuf<float> n_tg, n_ti, n_tf, n_tx;  // float32 replay: G2/IP/IF and x, [mapped pixel][D]
   DBuf<int32_t> n_ch_k0, n_ch_k1, n_e_chunk_ptr;  // pixel chunks of every entry
   int32_t n_chunks = 0;
   DBuf<double> n_part;                            // [chunk][tau][5] partial sums
@@ -349,6 +350,8 @@ void run_filter_transpose(Series &s);                       // k_transpose.cu
 void run_multitau(Series &s, int mode);                      // k_multitau.cu
 void run_normalize(Series &s, bool want64, bool want32);     // k_normalize.cu
 void build_norm_chunks(Series &s);                           // k_normalize.cu
+// The float nearest to 1/b (ties to even) for an integer b in [1, 2^24].
+float recip_rn(int32_t b);                                   // k_multitau.cu
 
 // Stable radix sort of (key, a, b) by the low key_bits of key (k_transpose.cu);
 // returns true when the result is in the second set of arrays.
