@@ -264,9 +264,9 @@ __global__ void k_norm_finish(int NQ, int D, const int32_t *__restrict__ qep,
 // count uses the correctly rounded reciprocal of the count (__frcp_rn) and
 // one FMA residual correction (Markstein; Muller et al., Handbook of
 // Floating-Point Arithmetic, ch. 4), which gives the IEEE quotient for every
-// float numerator and every integer count up to 65536 (checked exhaustively
-// against __fdiv_rn on the GPU); larger counts, zeros and non-finite
-// numerators use __fdiv_rn.
+// float numerator and every integer count up to 2^20 (checked exhaustively
+// against __fdiv_rn on the GPU: every significand, every count); larger
+// counts, zeros and non-finite numerators use __fdiv_rn.
 
 constexpr int TR_K = 32, TR_T = 32;  // transpose tile: mapped pixels x taus
 
@@ -311,7 +311,7 @@ k_f32_transpose(int NK, int D, int P, const int32_t *__restrict__ pix,
 // = __frcp_rn(n) its correctly rounded reciprocal, which depends on the count
 // only and so stays off the chain of dependent operations
 __device__ __forceinline__ float div_count(float a, float n, int ni, float y) {
-  if (ni > 65536 || a == 0.f || !isfinite(a) || fabsf(a) < 1e-30f) return __fdiv_rn(a, n);
+  if (ni > (1 << 20) || a == 0.f || !isfinite(a) || fabsf(a) < 1e-30f) return __fdiv_rn(a, n);
   const float q0 = __fmul_rn(a, y);
   return __fmaf_rn(__fmaf_rn(-q0, n, a), y, q0);
 }
