@@ -420,6 +420,45 @@ def run_twotime_bench(args, dev):
                               "flop": gram_flop, "kernel_ms": gram_ms}}
 
 
+def run_corr(args, acq, dq, sq, nnz, idx, val):
+    """The drop-in `corr` driver on the same series: the IMM file and the
+    analysis container are written to a scratch directory, and `corr` reads
+    them, runs the GPU path and writes its datasets back (wall time of the
+    process, including CUDA start-up and file I/O)."""
+    import tempfile
+    sys.path.insert(0, str(ROOT / "tests"))
+    import refio  # the IMM / XH5C writers of the driver's tests
+    from build import build_corr
+
+    corr = build_corr()
+    with tempfile.TemporaryDirectory() as wd:
+        wd = Path(wd)
+        imm = wd / "series.imm"
+        refio.write_imm_sparse(imm, acq.height, acq.width, nnz, idx, val)
+        cfg = refio.config_entries(acq.width, acq.height, dq, sq, imm, first=1, last=acq.frames,
+                                   dpl=acq.dpl)
+        path = wd / "analysis.h5"
+        walls, log = [], ""
+        for _ in range(2):
+            refio.write_xh5c(path, cfg)
+            t0 = time.perf_counter()
+            r = subprocess.run([str(corr), str(path)], capture_output=True, text=True, cwd=wd)
+            walls.append(time.perf_counter() - t0)
+            if r.returncode != 0:
+                return {"error": r.stderr.strip()[-300:]}
+            log = r.stdout
+    stages = {}
+    for ln in log.splitlines():
+        for key, label in (("load_ms", "Loading data took"), ("multitau_ms", "Computing G2 MultiTau took"),
+                           ("normalize_ms", "Normalizing Data took"), ("total_ms", "Total took")):
+            if label in ln:
+                stages[key] = float(ln.split(label)[1].split()[0])
+    return {"workload": "the same series through the corr driver: IMM file + analysis container "
+                        "in, norm-0-g2 / norm-0-stderr (float32, bit-identical) and the side "
+                        "datasets written back",
+            "wall_s": min(walls), "stages_ms": stages}
+
+
 def run_dense(args, dev):
     """Dense CCD series: 960x960 x 20,000 int16 frames after 100 dark frames
     (dark ~ N(100, 8^2), read noise 4 ADU, 35 ADU/photon on the speckle
@@ -618,6 +657,8 @@ def run_gpu_arm(args, dist):
         result["twotime"] = run_twotime_bench(args, dev)
     if not args.no_dense:
         result["dense"] = run_dense(args, dev)
+    if not args.no_corr and dist.rank == 0:
+        result["corr"] = run_corr(args, acq, dq, sq, nnz, idx, val)
     if dist.rank == 0 and world == 1 and not args.no_cpu_baseline:
         frames = args.cpu_sample_frames
         t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
@@ -647,6 +688,7 @@ def main():
     ap.add_argument("--twotime-series", type=int, default=8)
     ap.add_argument("--twotime-frames", type=int, default=4096)
     ap.add_argument("--no-dense", action="store_true", help="skip the dense-frame measure")
+    ap.add_argument("--no-corr", action="store_true", help="skip the corr driver measure")
     ap.add_argument("--dense-frames", type=int, default=20000)
     ap.add_argument("--dense-steps", type=int, default=3)
     ap.add_argument("--dense-only", action="store_true",
