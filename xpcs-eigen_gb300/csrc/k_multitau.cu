@@ -180,32 +180,32 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
       acc[g * 32] = total - rsum;
     }
   }
-  // IP: thresholds t_ip strictly decreasing with the delay index
+  // IP and IF in one sweep over the delays, level group by level group: the
+  // IP thresholds t_ip decrease with the delay index (a pointer from the end
+  // of the row), the IF thresholds tau (in frames) increase (one from the
+  // start)
   {
-    int j = n0 - 1, rsum = 0;
-    for (int d = 0; d < D; d++) {
-      const int T = ar.t_ip[d];
-      while (j >= 0 && pk_t(row[j * 32]) >= T) {
-        rsum += pk_v(row[j * 32]);
-        j--;
+    int jp = n0 - 1, rsum = 0, jf = 0, ssum = 0;
+    for (int g = 0; g < nlev; g++) {
+      const McLevel L = pl->lv[g];
+      const int lvl = L.level, s_end = acc[g * 32];
+      for (int d = L.first; d < L.first + L.count; d++) {
+        const int Tp = ar.t_ip[d];
+        while (jp >= 0 && pk_t(row[jp * 32]) >= Tp) {
+          rsum += pk_v(row[jp * 32]);
+          jp--;
+        }
+        const int Tf = ar.tau_abs[d];
+        while (jf < n0 && pk_t(row[jf * 32]) < Tf) {
+          ssum += pk_v(row[jf * 32]);
+          jf++;
+        }
+        if (p < P) {
+          const float den = ar.denom[d], rc = ar.rcp[d];
+          IP[(size_t)d * P + p] = mine ? scaled_quotient(total - rsum, lvl, den, rc) : 0.f;
+          IF[(size_t)d * P + p] = mine ? scaled_quotient(s_end - ssum, lvl, den, rc) : 0.f;
+        }
       }
-      const int lvl = pl->lv[ar.gi[d]].level;
-      if (p < P) IP[(size_t)d * P + p] = mine ? scaled_quotient(total - rsum, lvl, ar.denom[d], ar.rcp[d]) : 0.f;
-    }
-  }
-  // IF: thresholds tau (in frames) increasing with the delay index
-  {
-    int j = 0, ssum = 0;
-    for (int d = 0; d < D; d++) {
-      const int T = ar.tau_abs[d];
-      while (j < n0 && pk_t(row[j * 32]) < T) {
-        ssum += pk_v(row[j * 32]);
-        j++;
-      }
-      const int g = ar.gi[d];
-      const int lvl = pl->lv[g].level;
-      if (p < P)
-        IF[(size_t)d * P + p] = mine ? scaled_quotient(acc[g * 32] - ssum, lvl, ar.denom[d], ar.rcp[d]) : 0.f;
     }
   }
 
