@@ -74,3 +74,51 @@ def test_one_pixel_detector_is_refused():
     dq, sq, _, _, _ = make(1, 1, 10, 0.5, 9)
     with pytest.raises(xg.XpcsError):
         xg.Series(1, 1, 10, 4, dq, sq)
+
+
+# ------------------------------------------------------------------ dense frames
+
+DENSE_CASES = {
+    # detector 5 x 3: rows are not a multiple of 8 pixels (no 16-byte loads)
+    "tiny_with_darks": dict(W=5, H=3, F=40, darks=6, lld=0.0, sigma=2.0, gain=(0.9, 1.1)),
+    "one_frame": dict(W=16, H=8, F=1, darks=4, lld=0.0, sigma=1.0, gain=(1.0, 1.0)),
+    "two_frames_no_darks_flat": dict(W=24, H=24, F=2, darks=0, lld=0.0, sigma=0.0,
+                                     gain=(0.8, 1.2)),
+    "no_darks_no_flat": dict(W=32, H=16, F=30, darks=0, lld=0.0, sigma=0.0, gain=(1.0, 1.0)),
+    # a threshold above every value: no pixel is kept
+    "nothing_kept": dict(W=16, H=16, F=20, darks=5, lld=30000.0, sigma=0.0, gain=(1.0, 1.0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(DENSE_CASES))
+def test_dense_edge_shapes_vs_oracle(name):
+    import xpcs_synth as xs
+
+    c = DENSE_CASES[name]
+    W, H, F, nd = c["W"], c["H"], c["F"], c["darks"]
+    acq = xs.Acquisition(width=W, height=H, frames=F, n_static=4, n_dynamic=2, mean=0.2,
+                         tau_min=3, tau_max=30, seed=60 + W + F, dpl=4, dense=True,
+                         dark_frames=nd, gain_min=c["gain"][0], gain_max=c["gain"][1])
+    dq, sq, flat, _ = xs.maps(acq)
+    use_flat = c["gain"] != (1.0, 1.0)
+    ds = xs.DenseStream(acq)
+    raw = ds.next(nd + F)
+    ds.close()
+    with xg.Series(W, H, F, 4, dq, sq, flatfield=flat if use_flat else None, dense=True,
+                   lld=c["lld"], sigma=c["sigma"]) as s:
+        if nd:
+            s.set_dark(raw[:nd])
+        s.ingest_dense(raw[nd:])
+        s.multitau()
+        G2, IP, IF = s.g2ipif()
+        info = s.info()
+    qm = oracle.QMap(dq, sq)
+    ones = np.ones(W * H)
+    da, dsd = (oracle.dark_image(raw[:nd], flat.ravel() if use_flat else ones) if nd
+               else (None, None))
+    rows, _ = oracle.dense_filter(qm, raw[nd:], F, da, dsd, c["lld"], c["sigma"],
+                                  flat=flat.ravel() if use_flat else None)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, 4, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+    if name == "nothing_kept":
+        assert info.events == 0
