@@ -104,3 +104,36 @@ def test_exact_twotime_large_tiles():
     for q in t["c2t"]:
         assert same_bits_nan(t["c2t"][q], c["c2t"][q]), q
     assert same_bits_nan(t["g2full"], c["g2full"])
+
+
+@pytest.mark.parametrize("frames", [5, 127, 128, 257])
+@pytest.mark.parametrize("static_map", [False, True])
+def test_twotime_frame_counts_around_the_tiles(frames, static_map):
+    """Frame counts below, at and just past the 128/256-frame Gram tiles
+    (padding rows and columns): REFERENCE mode against the oracle bit for bit,
+    EXACT mode on the tensor cores equal to the CUDA-core Gram, and within
+    float32 rounding of REFERENCE."""
+    acq = xs.Acquisition(width=24, height=20, frames=frames, n_static=8, n_dynamic=4, mean=0.1,
+                         tau_min=2, tau_max=50, seed=frames + (7 if static_map else 0), dpl=4)
+    dq, sq, _, _ = xs.maps(acq)
+    nnz, idx, val = xs.sparse_frames(acq)
+    qlist = [1, 3, 4]
+    window = min(4, frames)
+    res = {}
+    for mode in (xg.MODE_REFERENCE, xg.MODE_EXACT, xg.TWOTIME_EXACT_CUDA_CORES):
+        with xg.Series(acq.width, acq.height, frames, 4, dq, sq) as s:
+            s.ingest_sparse(nnz, idx, val)
+            res[mode] = s.twotime(qlist, static_map=static_map, average=False, window=window,
+                                  mode=mode)
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, frames)
+    o = oracle.twotime(qm, rows, frames, qlist, static_map, False, window)
+    r, t, c = res[xg.MODE_REFERENCE], res[xg.MODE_EXACT], res[xg.TWOTIME_EXACT_CUDA_CORES]
+    assert same_bits_nan(r["sg"], o["sg"])
+    for q, C in o["c2t"].items():
+        assert same_bits_nan(r["c2t"][q], C), q
+        assert same_bits_nan(t["c2t"][q], c["c2t"][q]), q
+        assert _max_rel(t["c2t"][q], C) <= 1e-4, q
+    assert same_bits_nan(r["g2full"], o["g2full"])
+    assert same_bits_nan(r["g2partials"], o["g2partials"])
+    assert same_bits_nan(t["g2full"], c["g2full"])
