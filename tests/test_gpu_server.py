@@ -114,3 +114,53 @@ def test_one_thread_per_acquisition():
         assert srv.stats()["series_finished"] == len(data)
     for r, ref in zip(results, refs):
         check(r, ref)
+
+
+def test_errors_and_edge_cases():
+    """Misuse is refused with an error and leaves the server usable: unknown
+    ids, frames after finish, finish twice, results before finish.  An
+    acquisition finished without frames gives the series' empty result; one
+    larger than the whole budget is admitted when nothing else is active; a
+    bad pixel index fails that acquisition only."""
+    acq, dq, sq, frames = make(0, *ACQS[0])
+    with xg.Server(memory_budget=256 << 20) as srv:
+        with pytest.raises(xg.XpcsError):
+            srv.state(12345)
+        with pytest.raises(xg.XpcsError):
+            srv.push(12345, *next(frame_slices(frames)))
+        # no frames at all
+        a = srv.submit(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, 0)
+        with pytest.raises(xg.XpcsError):
+            srv.result(a)  # finish not called
+        srv.finish(a)
+        with pytest.raises(xg.XpcsError):
+            srv.finish(a)
+        with pytest.raises(xg.XpcsError):
+            srv.push(a, *next(frame_slices(frames)))
+        empty = (np.zeros(0, np.uint32), np.zeros(0, np.int32), np.zeros(0, np.int16))
+        check(srv.result(a, g2ipif=True), alone(acq, dq, sq, empty))
+        srv.release(a)
+        # larger than the budget: admitted while nothing else is active
+        big, bdq, bsq, bframes = make(1, 256, 400, 0.05, 8, (2, 40))
+        b = srv.submit(big.width, big.height, big.frames, big.dpl, bdq, bsq,
+                       int(bframes[1].size))
+        for part in frame_slices(bframes):
+            srv.push(b, *part)
+        srv.finish(b)
+        check(srv.result(b, g2ipif=True), alone(big, bdq, bsq, bframes))
+        srv.release(b)
+        # a pixel index past the detector fails this acquisition only
+        c = srv.submit(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, 10)
+        d = srv.submit(acq.width, acq.height, acq.frames, acq.dpl, dq, sq,
+                       int(frames[1].size))
+        srv.push(c, np.array([1], np.uint32), np.array([acq.width * acq.height + 5], np.int32),
+                 np.array([1], np.int16))
+        for part in frame_slices(frames):
+            srv.push(d, *part)
+        srv.finish(c)
+        srv.finish(d)
+        with pytest.raises(xg.XpcsError):
+            srv.result(c)
+        check(srv.result(d, g2ipif=True), alone(acq, dq, sq, frames))
+        srv.release(c)
+        srv.release(d)
