@@ -122,3 +122,57 @@ def test_dense_edge_shapes_vs_oracle(name):
     assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
     if name == "nothing_kept":
         assert info.events == 0
+
+
+def test_series_call_order_and_kind_errors():
+    """Calls out of order, or for the other kind of frames, are refused with
+    an error and leave the handle usable: the results that follow match the
+    oracle."""
+    import xpcs_synth as xs
+
+    W, H, F = 12, 10, 200
+    dq, sq, nnz, idx, val = make(W, H, F, 0.05, 70)
+    with xg.Series(W, H, F, 4, dq, sq) as s:
+        for call in (s.g2ipif, s.normalize, lambda: s.side_stats(20),
+                     lambda: s.normalized(f64=True),
+                     lambda: xg.check(xg.lib().xpcs_get_twotime(s._h, *[None] * 5))):
+            with pytest.raises(xg.XpcsError):
+                call()
+        with pytest.raises(xg.XpcsError):
+            s.set_dark(np.zeros((2, W * H), np.int16))  # darks are for dense series
+        with pytest.raises(xg.XpcsError):
+            s.ingest_dense(np.zeros((3, W * H), np.int16))
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau()
+        with pytest.raises(xg.XpcsError):
+            s.normalized(f64=True)  # no normalisation has run yet
+        G2, IP, IF = s.g2ipif()
+        g64, s64, g32, s32 = s.normalize()
+        n64, e64, _, _ = s.normalized(f64=True)
+        assert same_bits_nan(n64, g64) and same_bits_nan(e64, s64)
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, 4, xg.MODE_REFERENCE)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+    acq = xs.Acquisition(width=8, height=8, frames=20, n_static=4, n_dynamic=2, mean=0.2,
+                         tau_min=3, tau_max=30, seed=71, dpl=4, dense=True, dark_frames=2)
+    dq, sq, _, _ = xs.maps(acq)
+    ds = xs.DenseStream(acq)
+    raw = ds.next(22)
+    ds.close()
+    with xg.Series(8, 8, 20, 4, dq, sq, dense=True, sigma=1.0) as s:
+        with pytest.raises(xg.XpcsError):
+            s.ingest_sparse(np.array([1], np.uint32), np.array([0], np.int32),
+                            np.array([1], np.int16))
+        s.set_dark(raw[:2])
+        s.ingest_dense(raw[2:])
+        with pytest.raises(xg.XpcsError):
+            s.set_dark(raw[:2])  # darks come before the frames
+        s.multitau()
+        G2, IP, IF = s.g2ipif()
+    qm = oracle.QMap(dq, sq)
+    da, dsd = oracle.dark_image(raw[:2], np.ones(64))
+    rows, _ = oracle.dense_filter(qm, raw[2:], 20, da, dsd, 0.0, 1.0, flat=None)
+    oG2, oIP, oIF = oracle.multitau2(rows, 20, 4, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
