@@ -115,6 +115,55 @@ __device__ __forceinline__ void copy_plan(uint8_t *dst, const uint8_t *src, size
 
 // ------------------------------------------------------ thread per pixel
 
+// Levels of at most MT_BIN_CAP bins: the thread keeps its row's occupied bins
+// as a bitmask in registers (4 x 64 bits).  Bins in a row's live prefix are
+// distinct and increasing, so the entry at bin b sits at position
+// popcount(bits below b): one 64-bit window of the mask after a source's bin
+// gives both the position of its first partner and which of the level's
+// delays have one.
+constexpr int MT_BIN_CAP = 256;
+
+__device__ __forceinline__ uint64_t bin_window(uint64_t b0, uint64_t b1, uint64_t b2,
+                                               uint64_t b3, int s) {
+  const int q = s >> 6, sh = s & 63;
+  const uint64_t lo = q == 0 ? b0 : q == 1 ? b1 : q == 2 ? b2 : q == 3 ? b3 : 0ull;
+  const uint64_t hi = q == 0 ? b1 : q == 1 ? b2 : q == 2 ? b3 : 0ull;
+  return sh ? (lo >> sh) | (hi << (64 - sh)) : lo;
+}
+
+// Pair products of one level from the bin mask, KM >= count accumulators in
+// registers; sources stop at the first bin whose first partner would be past
+// lastframe.
+template <int KM>
+__device__ __forceinline__ void bins_pairs(const uint32_t *row, int m, int lf, int tlo, int count,
+                                           uint64_t b0, uint64_t b1, uint64_t b2, uint64_t b3,
+                                           int32_t *acc) {
+  int a[KM];
+#pragma unroll
+  for (int k = 0; k < KM; k++) a[k] = 0;
+  const uint64_t gap = (1ull << (tlo - 1)) - 1ull;  // bins strictly between source and tau_lo
+  const uint32_t cmask = (1u << count) - 1u;
+  for (int i = 0; i < m; i++) {
+    const uint32_t wi = row[i * 32];
+    const int ti = pk_t(wi);
+    if (ti + tlo >= lf) break;
+    const uint64_t W = bin_window(b0, b1, b2, b3, ti + 1);
+    int j = i + 1 + __popcll(W & gap);
+    const uint32_t w = (uint32_t)(W >> (tlo - 1)) & cmask;
+    const int vi = pk_v(wi);
+#pragma unroll
+    for (int k = 0; k < KM; k++) {
+      if (w & (1u << k)) {
+        a[k] += vi * pk_v(row[j * 32]);
+        j++;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < KM; k++)
+    if (k < count) acc[k * 32] = a[k];
+}
+
 template <int CAP>
 __global__ void __launch_bounds__(MT_WARPS * 32)
 k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
@@ -122,16 +171,15 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
             const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
             float *__restrict__ G2, float *__restrict__ IP, float *__restrict__ IF) {
   extern __shared__ __align__(16) uint8_t smem[];
-  const int D = ((const McPlan *)plan_g)->D;
-  const size_t pb = mc_plan_bytes(D);
-  copy_plan(smem, plan_g, pb);
-  __syncthreads();
-  const McPlan *pl = (const McPlan *)smem;
-  const McArrays ar = mc_arrays(smem, D);
+  // the plan is read from global memory: every lane of a warp reads the same
+  // words (one L1-cached broadcast), and shared memory is left to the rows
+  const McPlan *pl = (const McPlan *)plan_g;
+  const int D = pl->D;
+  const McArrays ar = mc_arrays(plan_g, D);
   const int P = pl->P, nlev = pl->nlev, mode = pl->mode;
   const int scr = max(pl->acc, nlev);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *wbase = (uint32_t *)(smem + pb) + (size_t)warp * (CAP + scr) * 32;
+  uint32_t *wbase = (uint32_t *)smem + (size_t)warp * (CAP + scr) * 32;
   uint32_t *row = wbase + lane;
   int32_t *acc = (int32_t *)(row + CAP * 32);  // scratch, also S(t_end) per level
 
@@ -235,9 +283,26 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
       m = m2;
     }
     const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
-    for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
     const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
-    if (sorted) {
+    // warp-uniform: every lane of the warp sees the same level
+    const bool bins = L.lastframe <= MT_BIN_CAP && tlo >= 1 && thi <= 64 && L.count <= 16;
+    if (bins && sorted) {
+      uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+      for (int i = 0; i < m; i++) {
+        const int t = pk_t(row[i * 32]);
+        const uint64_t bit = 1ull << (t & 63);
+        const int q = t >> 6;
+        b0 |= q == 0 ? bit : 0ull;
+        b1 |= q == 1 ? bit : 0ull;
+        b2 |= q == 2 ? bit : 0ull;
+        b3 |= q == 3 ? bit : 0ull;
+      }
+      if (L.count <= 8)
+        bins_pairs<8>(row, m, L.lastframe, tlo, L.count, b0, b1, b2, b3, acc);
+      else
+        bins_pairs<16>(row, m, L.lastframe, tlo, L.count, b0, b1, b2, b3, acc);
+    } else if (sorted) {
+      for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
       // one flat loop, one visit per iteration, so that the lanes of a warp
       // stay together however their pairs are spread: either the partner
       // pointer j takes the next word (a pair when its distance is in
@@ -265,6 +330,7 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
     } else {
       // the buffer is not globally sorted: a pair counts only when the
       // reference's lower_bound over the whole buffer lands on the partner
+      for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
       for (int i = 0; i < m; i++) {
         const uint32_t wi = row[i * 32];
         const int ti = pk_t(wi);
@@ -867,8 +933,8 @@ std::vector<uint8_t> make_plan(const Series &s, int mode) {
   return buf;
 }
 
-size_t thread_smem(int D, int scr, int cap) {
-  return mc_plan_bytes(D) + (size_t)MT_WARPS * (cap + scr) * 32 * sizeof(uint32_t);
+size_t thread_smem(int scr, int cap) {
+  return (size_t)MT_WARPS * (cap + scr) * 32 * sizeof(uint32_t);
 }
 
 using ThreadKernel = void (*)(const uint8_t *, const int64_t *, const int32_t *, const uint8_t *,
@@ -930,7 +996,7 @@ void run_multitau(Series &s, int mode) {
   if (D == 0 || P == 0) return;
   const int scr = std::max(hp->acc, hp->nlev);
   const ThreadKernel ktt = thread_kernel(s.thread_cap);
-  const size_t smt = thread_smem(D, scr, s.thread_cap), smw = warp_smem(D, scr, MT_WARP_CAP, WP_WARPS);
+  const size_t smt = thread_smem(scr, s.thread_cap), smw = warp_smem(D, scr, MT_WARP_CAP, WP_WARPS);
   const size_t smm = warp_smem(D, scr, MT_MID_CAP, MID_WARPS);
   const size_t sml = warp_smem(D, scr, MT_LONG_CAP, LONG_WARPS);
   if (smt > 227 * 1024 || smw > 227 * 1024 || smm > 227 * 1024 || sml > 227 * 1024)
