@@ -165,7 +165,7 @@ __device__ __forceinline__ void bins_pairs(const uint32_t *row, int m, int lf, i
 }
 
 template <int CAP>
-__global__ void __launch_bounds__(MT_WARPS * 32)
+__global__ void __launch_bounds__(MT_WARPS * 32, 8)
 k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
             const int32_t *__restrict__ row_len, const uint8_t *__restrict__ pclass,
             const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
@@ -190,26 +190,42 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
   const int n0 = mine ? row_len[p] : 0;
 
   // cooperative, coalesced load of the warp's rows (consecutive pixels have
-  // consecutive rows), scattered to the owning lane's slots
-  {
+  // consecutive rows), scattered to the owning lane's slots; four chunks of
+  // 32 events in flight per lane.  Positions are relative to the warp's first
+  // event: when a lane owns a packed row every frame is below 65536, so the
+  // 32 rows span fewer than 2^21 events.
+  if (__any_sync(0xffffffffu, n0 > 0)) {
+    const unsigned FULL = 0xffffffffu;
     const int plast = min(p0 + 32, P);
-    const int64_t e0 = row_ptr[p0], e1 = row_ptr[plast];
-    const int64_t my_b = p < P ? row_ptr[p] : e1;
-    for (int64_t base = e0; base < e1; base += 32) {
-      const int64_t e = base + lane;
-      int owner = 0;  // last lane whose row starts at or before e
+    const int64_t e0 = row_ptr[p0];
+    const int nw = (int)(row_ptr[plast] - e0);
+    const int my_b = p < P ? (int)(row_ptr[p] - e0) : nw;
+    const int lo = __reduce_min_sync(FULL, n0 > 0 ? my_b : INT_MAX);
+    const int hi = __reduce_max_sync(FULL, n0 > 0 ? my_b + n0 : 0);
+    for (int base = lo; base < hi; base += 128) {
+      int dst[4], fr[4];
+      float vl[4];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const int cand = owner + o;
-        const int64_t cb = __shfl_sync(0xffffffffu, my_b, cand & 31);
-        if (cand < 32 && cb <= e) owner = cand;
+      for (int u = 0; u < 4; u++) {
+        const int e = base + u * 32 + lane;
+        int owner = 0;  // last lane whose row starts at or before e
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const int cand = owner + o;
+          const int cb = __shfl_sync(FULL, my_b, cand & 31);
+          if (cand < 32 && cb <= e) owner = cand;
+        }
+        const int slot = e - __shfl_sync(FULL, my_b, owner);
+        const int olen = __shfl_sync(FULL, n0, owner);
+        dst[u] = (e < hi && slot < olen) ? slot * 32 + owner : -1;
+        if (dst[u] >= 0) {
+          fr[u] = ev_frame[e0 + e];
+          vl[u] = ev_val[e0 + e];
+        }
       }
-      const int64_t ob = __shfl_sync(0xffffffffu, my_b, owner);
-      const int olen = __shfl_sync(0xffffffffu, n0, owner);
-      if (e < e1) {
-        const int slot = (int)(e - ob);
-        if (slot < olen) wbase[slot * 32 + owner] = pk(ev_frame[e], __float2int_rn(ev_val[e]));
-      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (dst[u] >= 0) wbase[dst[u]] = pk(fr[u], __float2int_rn(vl[u]));
     }
   }
   __syncwarp();
@@ -231,27 +247,45 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
   // IP and IF in one sweep over the delays, level group by level group: the
   // IP thresholds t_ip decrease with the delay index (a pointer from the end
   // of the row), the IF thresholds tau (in frames) increase (one from the
-  // start)
+  // start).  Lane k loads the thresholds and divisor of the chunk's k-th
+  // delay, and they are broadcast by shuffle.
   {
+    const unsigned FULL = 0xffffffffu;
     int jp = n0 - 1, rsum = 0, jf = 0, ssum = 0;
+    uint32_t wp = n0 > 0 ? row[(n0 - 1) * 32] : 0u;  // word at jp
+    uint32_t wf = n0 > 0 ? row[0] : 0u;              // word at jf
     for (int g = 0; g < nlev; g++) {
       const McLevel L = pl->lv[g];
       const int lvl = L.level, s_end = acc[g * 32];
-      for (int d = L.first; d < L.first + L.count; d++) {
-        const int Tp = ar.t_ip[d];
-        while (jp >= 0 && pk_t(row[jp * 32]) >= Tp) {
-          rsum += pk_v(row[jp * 32]);
-          jp--;
+      for (int d0 = L.first; d0 < L.first + L.count; d0 += 32) {
+        const int nd = min(32, L.first + L.count - d0);
+        int tp_l = 0, tf_l = 0;
+        float den_l = 0.f, rc_l = 0.f;
+        if (lane < nd) {
+          tp_l = ar.t_ip[d0 + lane];
+          tf_l = ar.tau_abs[d0 + lane];
+          den_l = ar.denom[d0 + lane];
+          rc_l = ar.rcp[d0 + lane];
         }
-        const int Tf = ar.tau_abs[d];
-        while (jf < n0 && pk_t(row[jf * 32]) < Tf) {
-          ssum += pk_v(row[jf * 32]);
-          jf++;
-        }
-        if (p < P) {
-          const float den = ar.denom[d], rc = ar.rcp[d];
-          IP[(size_t)d * P + p] = mine ? scaled_quotient(total - rsum, lvl, den, rc) : 0.f;
-          IF[(size_t)d * P + p] = mine ? scaled_quotient(s_end - ssum, lvl, den, rc) : 0.f;
+        for (int k = 0; k < nd; k++) {
+          const int Tp = __shfl_sync(FULL, tp_l, k), Tf = __shfl_sync(FULL, tf_l, k);
+          const float den = __shfl_sync(FULL, den_l, k), rc = __shfl_sync(FULL, rc_l, k);
+          while (jp >= 0 && pk_t(wp) >= Tp) {
+            rsum += pk_v(wp);
+            jp--;
+            wp = jp >= 0 ? row[jp * 32] : 0u;
+          }
+          while (jf < n0 && pk_t(wf) < Tf) {
+            ssum += pk_v(wf);
+            jf++;
+            wf = jf < n0 ? row[jf * 32] : 0u;
+          }
+          // lanes without a row of this kernel have n0 = 0: both numerators are 0
+          if (p < P) {
+            const size_t o = (size_t)(d0 + k) * P + p;
+            IP[o] = scaled_quotient(total - rsum, lvl, den, rc);
+            IF[o] = scaled_quotient(s_end - ssum, lvl, den, rc);
+          }
         }
       }
     }
