@@ -115,39 +115,34 @@ __device__ __forceinline__ void copy_plan(uint8_t *dst, const uint8_t *src, size
 
 // ------------------------------------------------------ thread per pixel
 
-// Levels of at most MT_BIN_CAP bins: the thread keeps its row's occupied bins
-// as a bitmask in registers (4 x 64 bits).  Bins in a row's live prefix are
-// distinct and increasing, so the entry at bin b sits at position
-// popcount(bits below b): one 64-bit window of the mask after a source's bin
-// gives both the position of its first partner and which of the level's
-// delays have one.
-constexpr int MT_BIN_CAP = 256;
-
-__device__ __forceinline__ uint64_t bin_window(uint64_t b0, uint64_t b1, uint64_t b2,
-                                               uint64_t b3, int s) {
-  const int q = s >> 6, sh = s & 63;
-  const uint64_t lo = q == 0 ? b0 : q == 1 ? b1 : q == 2 ? b2 : q == 3 ? b3 : 0ull;
-  const uint64_t hi = q == 0 ? b1 : q == 1 ? b2 : q == 2 ? b3 : 0ull;
-  return sh ? (lo >> sh) | (hi << (64 - sh)) : lo;
-}
-
-// Pair products of one level from the bin mask, KM >= count accumulators in
-// registers; sources stop at the first bin whose first partner would be past
-// lastframe.
+// Levels of at most 32 x (scratch words) bins: the thread keeps its row's
+// occupied bins as a bitmask in its scratch words (lane-interleaved, one
+// 32-bit word per 32 bins).  Bins in a row's live prefix are distinct and
+// increasing, so the entry at bin b sits at position popcount(bits below b):
+// one 64-bit window of the mask after a source's bin gives both the position
+// of its first partner and which of the level's delays have one.  The KM >=
+// count accumulators stay in registers and overwrite the mask once the
+// sources are done; sources stop at the first bin whose first partner would
+// be past lastframe.
 template <int KM>
-__device__ __forceinline__ void bins_pairs(const uint32_t *row, int m, int lf, int tlo, int count,
-                                           uint64_t b0, uint64_t b1, uint64_t b2, uint64_t b3,
-                                           int32_t *acc) {
+__device__ __forceinline__ void bins_pairs(const uint32_t *row, int m, int lf, int tlo,
+                                                int count, int32_t *acc) {
+  const uint32_t *mk = (const uint32_t *)acc;
+  const int nw = (lf + 31) >> 5;
   int a[KM];
 #pragma unroll
   for (int k = 0; k < KM; k++) a[k] = 0;
-  const uint64_t gap = (1ull << (tlo - 1)) - 1ull;  // bins strictly between source and tau_lo
+  const uint64_t gap = (1ull << (tlo - 1)) - 1ull;
   const uint32_t cmask = (1u << count) - 1u;
   for (int i = 0; i < m; i++) {
     const uint32_t wi = row[i * 32];
     const int ti = pk_t(wi);
     if (ti + tlo >= lf) break;
-    const uint64_t W = bin_window(b0, b1, b2, b3, ti + 1);
+    const int s = ti + 1, q = s >> 5, sh = s & 31;  // s < lf: word q exists
+    const uint32_t m0 = mk[q * 32];
+    const uint32_t m1 = q + 1 < nw ? mk[(q + 1) * 32] : 0u;
+    const uint32_t m2 = q + 2 < nw ? mk[(q + 2) * 32] : 0u;
+    const uint64_t W = ((uint64_t)__funnelshift_r(m1, m2, sh) << 32) | __funnelshift_r(m0, m1, sh);
     int j = i + 1 + __popcll(W & gap);
     const uint32_t w = (uint32_t)(W >> (tlo - 1)) & cmask;
     const int vi = pk_v(wi);
@@ -319,22 +314,28 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
     const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
     const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
     // warp-uniform: every lane of the warp sees the same level
-    const bool bins = L.lastframe <= MT_BIN_CAP && tlo >= 1 && thi <= 64 && L.count <= 16;
+    const bool bins = tlo >= 1 && thi <= 64 && L.count <= 16 && L.lastframe <= 32 * scr;
     if (bins && sorted) {
-      uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+      // mask words in the scratch: zeroed, then one store per word that holds
+      // an entry (the bins increase along the prefix)
+      const int nw = (L.lastframe + 31) >> 5;
+      for (int q = 0; q < nw; q++) acc[q * 32] = 0;
+      int cq = -1;
+      uint32_t cb = 0u;
       for (int i = 0; i < m; i++) {
         const int t = pk_t(row[i * 32]);
-        const uint64_t bit = 1ull << (t & 63);
-        const int q = t >> 6;
-        b0 |= q == 0 ? bit : 0ull;
-        b1 |= q == 1 ? bit : 0ull;
-        b2 |= q == 2 ? bit : 0ull;
-        b3 |= q == 3 ? bit : 0ull;
+        if ((t >> 5) != cq) {
+          if (cq >= 0) acc[cq * 32] = (int32_t)cb;
+          cq = t >> 5;
+          cb = 0u;
+        }
+        cb |= 1u << (t & 31);
       }
+      if (cq >= 0) acc[cq * 32] = (int32_t)cb;
       if (L.count <= 8)
-        bins_pairs<8>(row, m, L.lastframe, tlo, L.count, b0, b1, b2, b3, acc);
+        bins_pairs<8>(row, m, L.lastframe, tlo, L.count, acc);
       else
-        bins_pairs<16>(row, m, L.lastframe, tlo, L.count, b0, b1, b2, b3, acc);
+        bins_pairs<16>(row, m, L.lastframe, tlo, L.count, acc);
     } else if (sorted) {
       for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
       // one flat loop, one visit per iteration, so that the lanes of a warp
@@ -377,10 +378,20 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
         }
       }
     }
-    if (p < P) {
-      for (int k = 0; k < L.count; k++) {
-        const int d = L.first + k;
-        G2[(size_t)d * P + p] = mine ? scaled_quotient(acc[k * 32], 2 * L.level, ar.denom[d], ar.rcp[d]) : 0.f;
+    // divisors broadcast by shuffle as in the IP/IF sweep; lanes without a
+    // row of this kernel have zero sums
+    for (int d0 = L.first; d0 < L.first + L.count; d0 += 32) {
+      const int nd = min(32, L.first + L.count - d0);
+      float den_l = 0.f, rc_l = 0.f;
+      if (lane < nd) {
+        den_l = ar.denom[d0 + lane];
+        rc_l = ar.rcp[d0 + lane];
+      }
+      for (int k = 0; k < nd; k++) {
+        const float den = __shfl_sync(0xffffffffu, den_l, k), rc = __shfl_sync(0xffffffffu, rc_l, k);
+        if (p < P)
+          G2[(size_t)(d0 + k) * P + p] =
+              scaled_quotient(acc[(d0 - L.first + k) * 32], 2 * L.level, den, rc);
       }
     }
   }
