@@ -265,15 +265,31 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
         for (int k = 0; k < nd; k++) {
           const int Tp = __shfl_sync(FULL, tp_l, k), Tf = __shfl_sync(FULL, tf_l, k);
           const float den = __shfl_sync(FULL, den_l, k), rc = __shfl_sync(FULL, rc_l, k);
-          while (jp >= 0 && pk_t(wp) >= Tp) {
-            rsum += pk_v(wp);
-            jp--;
-            wp = jp >= 0 ? row[jp * 32] : 0u;
+          // one step of each pointer without a branch (lanes step at different
+          // delays), then a loop for the lanes that need more
+          bool ap = jp >= 0 && pk_t(wp) >= Tp, af = jf < n0 && pk_t(wf) < Tf;
+          {
+            const uint32_t np = row[max(jp - 1, 0) * 32], nf = row[min(jf + 1, CAP - 1) * 32];
+            rsum += ap ? pk_v(wp) : 0;
+            ssum += af ? pk_v(wf) : 0;
+            jp -= ap ? 1 : 0;
+            jf += af ? 1 : 0;
+            wp = ap ? (jp >= 0 ? np : 0u) : wp;
+            wf = af ? (jf < n0 ? nf : 0u) : wf;
           }
-          while (jf < n0 && pk_t(wf) < Tf) {
-            ssum += pk_v(wf);
-            jf++;
-            wf = jf < n0 ? row[jf * 32] : 0u;
+          ap = jp >= 0 && pk_t(wp) >= Tp;
+          af = jf < n0 && pk_t(wf) < Tf;
+          if (__any_sync(FULL, ap || af)) {
+            while (jp >= 0 && pk_t(wp) >= Tp) {
+              rsum += pk_v(wp);
+              jp--;
+              wp = jp >= 0 ? row[jp * 32] : 0u;
+            }
+            while (jf < n0 && pk_t(wf) < Tf) {
+              ssum += pk_v(wf);
+              jf++;
+              wf = jf < n0 ? row[jf * 32] : 0u;
+            }
           }
           // lanes without a row of this kernel have n0 = 0: both numerators are 0
           if (p < P) {
@@ -294,8 +310,10 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
     if (L.compact && m > 0) {
       const int lf = L.lastframe;
       int index = -1, prev = INT_MIN;
+      uint32_t wnext = row[0];
       for (int i = 0; i < m; i++) {
-        const uint32_t w = row[i * 32];
+        const uint32_t w = wnext;
+        wnext = row[min(i + 1, CAP - 1) * 32];  // ahead of the writes (index <= i)
         const int t = pk_t(w) >> 1;
         if (t >= lf) break;
         if (t == prev) {
@@ -343,24 +361,27 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
       // pointer j takes the next word (a pair when its distance is in
       // [tlo, thi]; closer words can pair with no later source, so jlo moves
       // past them) or the source i moves on and j restarts at jlo.
-      int i = 0, j = 1, jlo = 1;
+      // per source the next two entries are checked without a branch (lanes
+      // stay together); a loop runs only while the second one is still short
+      // of the window's end
       uint32_t wi = m > 0 ? row[0] : 0u;
-      uint32_t wj = m > 1 ? row[32] : 0u;
-      while (i < m - 1) {
-        const int ti = pk_t(wi);
-        const int d = pk_t(wj) - ti;
-        if (j < m && d <= thi) {
-          if (d >= tlo)
-            acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
-          else
-            jlo = j + 1;
-          j++;
-        } else {
-          i++;
-          wi = row[i * 32];
-          j = max(jlo, i + 1);
+      uint32_t w1 = m > 1 ? row[32] : 0u;
+      for (int i = 0; i < m - 1; i++) {
+        const uint32_t w2 = i + 2 < m ? row[(i + 2) * 32] : 0xffff0000u;  // frame 65535, value 0
+        const int ti = pk_t(wi), vi = pk_v(wi);
+        const int d1 = pk_t(w1) - ti, d2 = pk_t(w2) - ti;
+        if (d1 >= tlo && d1 <= thi) acc[(d1 - tlo) * 32] += vi * pk_v(w1);
+        if (d2 >= tlo && d2 <= thi) acc[(d2 - tlo) * 32] += vi * pk_v(w2);
+        if (d2 < thi && i + 3 < m) {
+          for (int j = i + 3; j < m; j++) {
+            const uint32_t wj = row[j * 32];
+            const int d = pk_t(wj) - ti;
+            if (d > thi) break;
+            if (d >= tlo) acc[(d - tlo) * 32] += vi * pk_v(wj);
+          }
         }
-        wj = j < m ? row[j * 32] : 0u;
+        wi = w1;
+        w1 = w2;
       }
     } else {
       // the buffer is not globally sorted: a pair counts only when the
