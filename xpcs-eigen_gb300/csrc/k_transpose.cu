@@ -85,9 +85,9 @@ __device__ __forceinline__ void raw_load(const RawCfg &c, int64_t i, int32_t &p,
 // in registers so that the common case (no frame boundary crossed) loads
 // nothing.  Masked pixels keep their own key here; their rows are emptied by
 // the merge, which reads the mask once per pixel instead of once per event.
-__device__ __forceinline__ void raw_key(const RawCfg &c, int64_t i, int32_t &r, int64_t &nb,
-                                        int32_t &k, int32_t p, float &v, uint32_t &key,
-                                        int32_t &frame) {
+__device__ __forceinline__ bool raw_frame_key(const RawCfg &c, int64_t i, int32_t &r, int64_t &nb,
+                                              int32_t &k, int32_t p, uint32_t &key,
+                                              int32_t &frame) {
   while (nb <= i) {
     r++;
     nb = c.frame_off[r + 1];
@@ -97,16 +97,34 @@ __device__ __forceinline__ void raw_key(const RawCfg &c, int64_t i, int32_t &r, 
   if (p < 0 || p >= c.P) {
     c.stats->error |= DEVERR_PIXEL_INDEX;
     key = (uint32_t)c.P;
+    return false;
+  }
+  key = k >= 0 ? (uint32_t)p : (uint32_t)c.P;
+  return true;
+}
+
+// (float)((double)v * g) as the reference forms a flat-fielded value,
+// exactly, in integer arithmetic (f64emu.cuh)
+__device__ __forceinline__ float flat_value(float v, double g) {
+  float w;
+  return f32_mul_f64(v, g, w) ? w : __double2float_rn(__dmul_rn((double)v, g));
+}
+
+__device__ __forceinline__ void raw_key(const RawCfg &c, int64_t i, int32_t &r, int64_t &nb,
+                                        int32_t &k, int32_t p, float &v, uint32_t &key,
+                                        int32_t &frame) {
+  if (!raw_frame_key(c, i, r, nb, k, p, key, frame)) {
     v = 0.f;
     return;
   }
-  key = k >= 0 ? (uint32_t)p : (uint32_t)c.P;
-  if (!c.valf && c.flat) {
-    // (float)((double)v * flat), exactly, in integer arithmetic (f64emu.cuh)
-    const double g = c.flat[p];
-    float w;
-    v = f32_mul_f64(v, g, w) ? w : __double2float_rn(__dmul_rn((double)v, g));
-  }
+  if (!c.valf && c.flat) v = flat_value(v, c.flat[p]);
+}
+
+// Packed items (sparse series with fewer than 65,536 filter frames): filter
+// frame in the high half, the raw int16 value in the low half.  The flatfield
+// is applied when the last pass writes the events out.
+__device__ __forceinline__ int32_t pack_item(int32_t frame, float raw) {
+  return (int32_t)(((uint32_t)frame << 16) | ((uint32_t)(int32_t)raw & 0xffffu));
 }
 
 // Item i of a tile in warp-striped order: warp w owns [w*32*IPT, (w+1)*32*IPT),
@@ -170,22 +188,22 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
 
 // Shared memory of the downsweep: per-warp digit counters, the tile's global
 // and local digit offsets, and the tile staged in digit order.
-template <int IPT>
+template <int IPT, bool PK>
 struct DsSmem {
   uint32_t wcnt[RS_WARPS][RS_DIGITS];
   uint32_t toff[RS_DIGITS];
   uint32_t tstart[RS_DIGITS];
   uint32_t wtot[RS_THREADS / 32];
   uint32_t key[RS_THREADS * IPT];
-  int32_t fr[RS_THREADS * IPT];
-  float v[RS_THREADS * IPT];
+  int32_t fr[RS_THREADS * IPT];      // frame, or the packed item
+  float v[PK ? 1 : RS_THREADS * IPT];
 };
 
-template <int IPT, bool FIRST, bool LAST>
+template <int IPT, bool FIRST, bool LAST, bool PK>
 __global__ void __launch_bounds__(RS_THREADS)
 k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   extern __shared__ __align__(16) uint8_t ds_raw[];
-  DsSmem<IPT> &sm = *reinterpret_cast<DsSmem<IPT> *>(ds_raw);
+  DsSmem<IPT, PK> &sm = *reinterpret_cast<DsSmem<IPT, PK> *>(ds_raw);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
   for (int d = lane; d < RS_DIGITS; d += 32) sm.wcnt[w][d] = 0;
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
@@ -216,7 +234,14 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
       const int64_t i = item_index<IPT>(tile, w, k, lane);
       key[k] = 0xffffffffu;
       fr[k] = 0;
-      if (i < pc.n) raw_key(rc, i, r, nb, kf, pix[k], v[k], key[k], fr[k]);
+      if (i < pc.n) {
+        if (PK) {
+          raw_frame_key(rc, i, r, nb, kf, pix[k], key[k], fr[k]);
+          fr[k] = pack_item(fr[k], v[k]);
+        } else {
+          raw_key(rc, i, r, nb, kf, pix[k], v[k], key[k], fr[k]);
+        }
+      }
     }
   } else {
 #pragma unroll
@@ -228,7 +253,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
       if (i < pc.n) {
         key[k] = pc.key_in[i];
         fr[k] = pc.fr_in[i];
-        v[k] = pc.v_in[i];
+        if (!PK) v[k] = pc.v_in[i];
       }
     }
   }
@@ -279,7 +304,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
     const uint32_t q = sm.tstart[d] + sm.wcnt[w][d] + rank[k];
     sm.key[q] = key[k];
     sm.fr[q] = fr[k];
-    sm.v[q] = v[k];
+    if (!PK) sm.v[q] = v[k];
   }
   __syncthreads();
   // write out: consecutive staged elements of a digit go to consecutive addresses
@@ -292,8 +317,15 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
     const uint32_t d = (kq >> pc.shift) & (RS_DIGITS - 1);
     const uint32_t pos = sm.toff[d] + (q - sm.tstart[d]);
     if (!LAST) pc.key_out[pos] = kq;
-    pc.fr_out[pos] = sm.fr[q];
-    pc.v_out[pos] = sm.v[q];
+    if (PK && LAST) {
+      const uint32_t it = (uint32_t)sm.fr[q];
+      const float raw = (float)(int16_t)(it & 0xffffu);
+      pc.fr_out[pos] = (int32_t)(it >> 16);
+      pc.v_out[pos] = rc.flat ? flat_value(raw, rc.flat[kq]) : raw;
+    } else {
+      pc.fr_out[pos] = sm.fr[q];
+      if (!PK) pc.v_out[pos] = sm.v[q];
+    }
   }
 }
 
@@ -452,18 +484,18 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
   record_class_warp(has, p, c, out, pclass, cl, stats);
 }
 
-template <int IPT, bool FIRST, bool LAST>
+template <int IPT, bool FIRST, bool LAST, bool PK>
 void launch_downsweep(int ntiles, cudaStream_t st, const RawCfg &rc, const PassCfg &pc,
                       const uint32_t *offsets) {
-  const size_t smem = sizeof(DsSmem<IPT>);
-  XG_CUDA(cudaFuncSetAttribute(k_downsweep<IPT, FIRST, LAST>,
+  const size_t smem = sizeof(DsSmem<IPT, PK>);
+  XG_CUDA(cudaFuncSetAttribute(k_downsweep<IPT, FIRST, LAST, PK>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_downsweep<IPT, FIRST, LAST><<<ntiles, RS_THREADS, smem, st>>>(rc, pc, offsets);
+  k_downsweep<IPT, FIRST, LAST, PK><<<ntiles, RS_THREADS, smem, st>>>(rc, pc, offsets);
 }
 
 // One radix pass: tile histograms, digit-major scan, stable scatter.
 template <int IPT>
-void radix_pass(Series &s, bool first, bool last, int ntiles, const RawCfg &rc,
+void radix_pass(Series &s, bool first, bool last, bool packed, int ntiles, const RawCfg &rc,
                 const PassCfg &pc) {
   cudaStream_t st = s.stream;
   if (first)
@@ -472,14 +504,25 @@ void radix_pass(Series &s, bool first, bool last, int ntiles, const RawCfg &rc,
     k_upsweep<IPT, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
   XG_CHECK_LAUNCH();
   exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
-  if (first && last)
-    launch_downsweep<IPT, true, true>(ntiles, st, rc, pc, s.hist_scan.p);
-  else if (first)
-    launch_downsweep<IPT, true, false>(ntiles, st, rc, pc, s.hist_scan.p);
-  else if (last)
-    launch_downsweep<IPT, false, true>(ntiles, st, rc, pc, s.hist_scan.p);
-  else
-    launch_downsweep<IPT, false, false>(ntiles, st, rc, pc, s.hist_scan.p);
+  if (packed) {
+    if (first && last)
+      launch_downsweep<IPT, true, true, true>(ntiles, st, rc, pc, s.hist_scan.p);
+    else if (first)
+      launch_downsweep<IPT, true, false, true>(ntiles, st, rc, pc, s.hist_scan.p);
+    else if (last)
+      launch_downsweep<IPT, false, true, true>(ntiles, st, rc, pc, s.hist_scan.p);
+    else
+      launch_downsweep<IPT, false, false, true>(ntiles, st, rc, pc, s.hist_scan.p);
+  } else {
+    if (first && last)
+      launch_downsweep<IPT, true, true, false>(ntiles, st, rc, pc, s.hist_scan.p);
+    else if (first)
+      launch_downsweep<IPT, true, false, false>(ntiles, st, rc, pc, s.hist_scan.p);
+    else if (last)
+      launch_downsweep<IPT, false, true, false>(ntiles, st, rc, pc, s.hist_scan.p);
+    else
+      launch_downsweep<IPT, false, false, false>(ntiles, st, rc, pc, s.hist_scan.p);
+  }
   XG_CHECK_LAUNCH();
 }
 
@@ -517,9 +560,9 @@ bool radix_sort_triples(Series &s, uint32_t *key, int32_t *a, float *b, uint32_t
     pc.fr_out = ab[(pass + 1) & 1];
     pc.v_out = bb[(pass + 1) & 1];
     if (ipt == 16)
-      radix_pass<16>(s, false, false, ntiles, rc, pc);
+      radix_pass<16>(s, false, false, false, ntiles, rc, pc);
     else
-      radix_pass<8>(s, false, false, ntiles, rc, pc);
+      radix_pass<8>(s, false, false, false, ntiles, rc, pc);
   }
   return (passes & 1) != 0;
 }
@@ -569,17 +612,20 @@ void run_filter_transpose(Series &s) {
     size_t ws = scan_workspace_bytes((int64_t)RS_DIGITS * ntiles);
     size_t ws2 = scan_workspace_bytes(P);
     s.scan_tmp.reserve(ws > ws2 ? ws : ws2, st);
+    // sparse series below 65,536 filter frames carry one packed word per item
+    // (frame, raw value) through the passes instead of a frame and a value
+    const bool dense = s.desc.dense != 0;
+    const bool packed = !dense && s.F <= 65536;
     if (passes > 1) {
       s.keyA.reserve(n, st);
       s.frA.reserve(n, st);
-      s.vA.reserve(n, st);
+      if (!packed) s.vA.reserve(n, st);
     }
     if (passes > 2) {
       s.keyB.reserve(n, st);
       s.frB.reserve(n, st);
-      s.vB.reserve(n, st);
+      if (!packed) s.vB.reserve(n, st);
     }
-    const bool dense = s.desc.dense != 0;
     const int chunk = 32 * ipt;
     const int64_t nch = (n + chunk - 1) / chunk;
     s.d_chunk_frame.reserve((size_t)nch, st);
@@ -614,9 +660,9 @@ void run_filter_transpose(Series &s) {
         pc.v_out = vbuf[pass & 1];
       }
       if (ipt == 16)
-        radix_pass<16>(s, first, last, ntiles, rc, pc);
+        radix_pass<16>(s, first, last, packed, ntiles, rc, pc);
       else
-        radix_pass<8>(s, first, last, ntiles, rc, pc);
+        radix_pass<8>(s, first, last, packed, ntiles, rc, pc);
     }
   } else {
     s.scan_tmp.reserve(scan_workspace_bytes(P), st);
