@@ -176,3 +176,89 @@ def test_series_call_order_and_kind_errors():
     rows, _ = oracle.dense_filter(qm, raw[2:], 20, da, dsd, 0.0, 1.0, flat=None)
     oG2, oIP, oIF = oracle.multitau2(rows, 20, 4, 0)
     assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
+@pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
+@pytest.mark.parametrize("dpl", [1, 2, 3, 16])
+def test_delays_per_level_vs_oracle(dpl, mode):
+    """The delays per level decide which levels of the thread-per-pixel kernel
+    take the bitmask pair search (at most 16 delays and 32 bins per scratch
+    word) and which take the sparse search: dpl 1-3 give few scratch words,
+    dpl 16 gives 32 delays at level 0.  Hot pixels put rows on the warp
+    kernels too."""
+    F = 3000
+    dq, sq, nnz, idx, val = make(24, 20, F, 0.01, 80 + dpl, hot=(7, 300), maxc=3)
+    with xg.Series(24, 20, F, dpl, dq, sq) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(mode)
+        G2, IP, IF = s.g2ipif()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, dpl, mode)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
+def _signed_frames(F, P, mean, seed, big_pixel=None):
+    """Sparse frames whose values are signed int16 (quirk Q3: counts above
+    32767 read back negative); `big_pixel` gets values near the int16 limits."""
+    rng = np.random.default_rng(seed)
+    nnz = np.zeros(F, np.uint32)
+    idx, val = [], []
+    for f in range(F):
+        sel = np.flatnonzero(rng.random(P) < mean).astype(np.int32)
+        v = rng.choice(np.array([-3, -2, -1, 1, 2, 3], np.int16), sel.size)
+        if big_pixel is not None and rng.random() < 0.01:
+            sel = np.union1d(sel, [big_pixel]).astype(np.int32)
+            v = rng.choice(np.array([-3, -2, -1, 1, 2, 3], np.int16), sel.size)
+            v[np.searchsorted(sel, big_pixel)] = rng.choice(np.array([-32768, -30000, 32767],
+                                                                     np.int16))
+        nnz[f] = sel.size
+        idx.append(sel)
+        val.append(v.astype(np.int16))
+    return nnz, np.concatenate(idx).astype(np.int32), np.concatenate(val).astype(np.int16)
+
+
+@pytest.mark.parametrize("flat", [False, True])
+def test_65536_frames_signed_values_vs_oracle(flat):
+    """65,536 frames is the longest series whose radix items are packed
+    (frame 65535 in the high half, the signed raw value in the low half); the
+    flatfield is then applied as the events are written out."""
+    F, W, H = 65536, 4, 4
+    P = W * H
+    nnz, idx, val = _signed_frames(F - 1, P, 0.0008, 90 + flat, big_pixel=5)
+    # the last frame (65535) holds an event of every pixel
+    extra_idx = np.arange(P, dtype=np.int32)
+    extra_val = np.full(P, 2, np.int16)
+    nnz = np.append(nnz, np.uint32(P))
+    idx = np.concatenate([idx, extra_idx])
+    val = np.concatenate([val, extra_val])
+    dq = np.ones((H, W), np.int32)
+    sq = dq.copy()
+    g = np.random.default_rng(7).uniform(0.9, 1.1, (H, W)) if flat else None
+    with xg.Series(W, H, F, 4, dq, sq, flatfield=g) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(xg.MODE_REFERENCE)
+        G2, IP, IF = s.g2ipif()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F,
+                                   flat=g.ravel() if flat else None)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, 4, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
+def test_stride_past_65536_raw_frames_vs_oracle():
+    """Stride 2 over 40,000 filter frames reads 80,000 raw frames: the packed
+    radix items carry the filter frame, which stays below 65,536."""
+    F, W, H, stride = 40000, 6, 5, 2
+    P = W * H
+    nnz, idx, val = _signed_frames(F * stride, P, 0.002, 95)
+    dq = np.ones((H, W), np.int32)
+    sq = dq.copy()
+    with xg.Series(W, H, F, 4, dq, sq, stride=stride) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(xg.MODE_REFERENCE)
+        G2, IP, IF = s.g2ipif()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F, stride=stride)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, 4, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
