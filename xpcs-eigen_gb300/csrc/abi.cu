@@ -83,7 +83,7 @@ void free_series(Series *s) {
     DeviceGuard g(s->device);
     cudaStream_t st = s->stream;
     cudaStreamSynchronize(st);
-    DBuf<int32_t> *i32[] = {&s->raw_idx, &s->frA, &s->frB, &s->cnt, &s->row_len,
+    DBuf<int32_t> *i32[] = {&s->raw_idx, &s->frA, &s->frB, &s->row_len,
                             &s->flist, &s->wlist, &s->llist, &s->ev_frame, &s->sc_frame,
                             &s->n_q_entry_ptr,
                             &s->n_entry_sbin, &s->n_entry_pix_ptr, &s->n_pix, &s->n_q_row,

@@ -14,8 +14,8 @@
 //            does (sparse_filter.cpp:149-153).
 //   pass k   8-bit digit k of the pixel index: tile histograms -> digit-major
 //            exclusive scan -> stable scatter.  Ranking inside a tile uses
-//            warp match_any + per-warp digit counters, so equal digits keep
-//            stream order (tile, warp, round, lane).
+//            per-bit warp ballots + per-warp digit counters, so equal digits
+//            keep stream order (tile, warp, round, lane).
 //   merge    one warp per 32 pixels: events of the same filter frame are
 //            summed in stream order and divided by avg (sparse_filter.cpp:
 //            160-172), pixelSum is accumulated in frame order, pixels outside
@@ -136,7 +136,7 @@ __device__ __forceinline__ int64_t item_index(int tile, int w, int k, int lane) 
 
 template <int IPT, bool FIRST>
 __global__ void __launch_bounds__(RS_THREADS)
-k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restrict__ cnt) {
+k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist) {
   __shared__ uint32_t h[RS_DIGITS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, tile = blockIdx.x;
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS) h[d] = 0;
@@ -175,11 +175,16 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist, int32_t *__restric
       key[k] = i < pc.n ? pc.key_in[i] : 0xffffffffu;
     }
   }
+  int dropped = 0;  // items that sort last: their count gives the kept total
 #pragma unroll
   for (int k = 0; k < IPT; k++) {
     if (key[k] == 0xffffffffu) continue;
-    if (FIRST && key[k] != pc.sentinel) atomicAdd(&cnt[key[k]], 1);
+    if (FIRST && key[k] == pc.sentinel) dropped++;
     atomicAdd(&h[(key[k] >> pc.shift) & (RS_DIGITS - 1)], 1u);
+  }
+  if (FIRST) {
+    dropped = __reduce_add_sync(0xffffffffu, dropped);
+    if (lane == 0 && dropped) atomicAdd(&rc.stats->dropped, (unsigned long long)dropped);
   }
   __syncthreads();
   for (int d = threadIdx.x; d < RS_DIGITS; d += RS_THREADS)
@@ -262,7 +267,15 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   for (int k = 0; k < IPT; k++) {
     const bool ok = key[k] != 0xffffffffu;
     uint32_t d = ok ? ((key[k] >> pc.shift) & (RS_DIGITS - 1)) : RS_DIGITS;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
+    // lanes with the same digit (9 bits with the invalid marker), one ballot
+    // per bit: cheaper here than match_any
+    unsigned peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 9; b++) {
+      const bool bit = (d >> b) & 1u;
+      const unsigned bal = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? bal : ~bal;
+    }
     int leader = __ffs(peers) - 1;
     uint32_t base = 0;
     if (ok && lane == leader) {
@@ -316,7 +329,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
     if (LAST && kq == pc.sentinel) continue;
     const uint32_t d = (kq >> pc.shift) & (RS_DIGITS - 1);
     const uint32_t pos = sm.toff[d] + (q - sm.tstart[d]);
-    if (!LAST) pc.key_out[pos] = kq;
+    if (!LAST || pc.key_out) pc.key_out[pos] = kq;
     if (PK && LAST) {
       const uint32_t it = (uint32_t)sm.fr[q];
       const float raw = (float)(int16_t)(it & 0xffffu);
@@ -327,6 +340,28 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
       if (!PK) pc.v_out[pos] = sm.v[q];
     }
   }
+}
+
+// Row pointers from the sorted keys: row_ptr[p] = first position whose key
+// is >= p (std::lower_bound over the kept items), row_ptr[P] = the kept total.
+// One thread per pixel; neighbouring pixels share the upper search steps.
+__global__ void k_row_ptr(const uint32_t *__restrict__ keys, int64_t n,
+                          const DevStats *__restrict__ stats, int32_t P,
+                          int64_t *__restrict__ row_ptr) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > P) return;
+  const int64_t nv = n - (int64_t)stats->dropped;
+  int64_t first = 0, len = nv;
+  while (len > 0) {
+    const int64_t half = len >> 1;
+    if ((int64_t)keys[first + half] < p) {
+      first += half + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  row_ptr[p] = first;
 }
 
 // Work lists of the multi-tau kernels (pixel indices per class).
@@ -408,7 +443,6 @@ __device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *
 // outside the mask get empty rows.
 __global__ void __launch_bounds__(256)
 k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_float,
-                 const int32_t *__restrict__ cnt,
                  const int64_t *__restrict__ row_ptr, const uint8_t *__restrict__ mask,
                  int32_t *__restrict__ fr, float *__restrict__ val, int32_t *__restrict__ row_len,
                  uint8_t *__restrict__ pclass, ClassLists cl, float *__restrict__ pixels_sum,
@@ -424,7 +458,7 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
   const int plast = min(p0 + 32, P);
   const int64_t e0 = row_ptr[p0], e1 = row_ptr[plast];
   const int64_t my_b = has ? row_ptr[p] : e1;
-  const int32_t my_n = has ? cnt[p] : 0;
+  const int32_t my_n = has ? (int32_t)(row_ptr[p + 1] - my_b) : 0;
   const bool keep = has && mask[p] != 0;
   s_total[w][lane] = 0;
   s_sum[w][lane] = 0;
@@ -499,9 +533,9 @@ void radix_pass(Series &s, bool first, bool last, bool packed, int ntiles, const
                 const PassCfg &pc) {
   cudaStream_t st = s.stream;
   if (first)
-    k_upsweep<IPT, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+    k_upsweep<IPT, true><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p);
   else
-    k_upsweep<IPT, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p, s.cnt.p);
+    k_upsweep<IPT, false><<<ntiles, RS_THREADS, 0, st>>>(rc, pc, s.hist.p);
   XG_CHECK_LAUNCH();
   exclusive_scan_u32(s.hist.p, s.hist_scan.p, (int64_t)RS_DIGITS * ntiles, s.scan_tmp.p, st);
   if (packed) {
@@ -571,7 +605,6 @@ void run_filter_transpose(Series &s) {
   cudaStream_t st = s.stream;
   const int64_t n = s.raw_events;
   const int32_t P = s.P;
-  s.cnt.reserve(P, st);
   s.row_ptr.reserve((size_t)P + 1, st);
   s.row_len.reserve(P, st);
   s.pclass.reserve(P, st);
@@ -580,7 +613,6 @@ void run_filter_transpose(Series &s) {
   s.llist.reserve(P, st);
   s.pixels_sum.reserve(P, st);
   s.stats.reserve(1, st);
-  XG_CUDA(cudaMemsetAsync(s.cnt.p, 0, sizeof(int32_t) * P, st));
   XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
   size_t nalloc = n > 0 ? (size_t)n : 1;
   s.ev_frame.reserve(nalloc, st);
@@ -616,13 +648,14 @@ void run_filter_transpose(Series &s) {
     // (frame, raw value) through the passes instead of a frame and a value
     const bool dense = s.desc.dense != 0;
     const bool packed = !dense && s.F <= 65536;
+    // the last pass also writes the kept items' keys, for the row pointers
+    s.keyA.reserve(n, st);
     if (passes > 1) {
-      s.keyA.reserve(n, st);
+      s.keyB.reserve(n, st);
       s.frA.reserve(n, st);
       if (!packed) s.vA.reserve(n, st);
     }
     if (passes > 2) {
-      s.keyB.reserve(n, st);
       s.frB.reserve(n, st);
       if (!packed) s.vB.reserve(n, st);
     }
@@ -651,7 +684,7 @@ void run_filter_transpose(Series &s) {
         pc.v_in = vbuf[(pass - 1) & 1];
       }
       if (last) {
-        pc.key_out = nullptr;
+        pc.key_out = kbuf[pass & 1];  // not the pass's input
         pc.fr_out = s.ev_frame.p;
         pc.v_out = s.ev_val.p;
       } else {
@@ -667,11 +700,19 @@ void run_filter_transpose(Series &s) {
   } else {
     s.scan_tmp.reserve(scan_workspace_bytes(P), st);
   }
-  exclusive_scan_i32_i64(s.cnt.p, s.row_ptr.p, P, s.scan_tmp.p, st);
+  if (n > 0) {
+    const uint32_t *keys = s.keyA.p;  // written by the last pass
+    const int passes = (32 - __builtin_clz((unsigned)P) + 7) / 8;
+    if (passes % 2 == 0) keys = s.keyB.p;
+    k_row_ptr<<<(unsigned)(((int64_t)P + 1 + 255) / 256), 256, 0, st>>>(keys, n, s.stats.p, P,
+                                                                        s.row_ptr.p);
+    XG_CHECK_LAUNCH();
+  } else {
+    XG_CUDA(cudaMemsetAsync(s.row_ptr.p, 0, sizeof(int64_t) * ((size_t)P + 1), st));
+  }
   const int pix_per_block = 256;
   k_merge_classify<<<(P + pix_per_block - 1) / pix_per_block, 256, 0, st>>>(
-      P, s.F, s.desc.avg_frames, s.thread_cap, s.desc.normalize_by_framesum, s.cnt.p,
-      s.row_ptr.p, s.d_mask.p, s.ev_frame.p,
+      P, s.F, s.desc.avg_frames, s.thread_cap, s.desc.normalize_by_framesum, s.row_ptr.p, s.d_mask.p, s.ev_frame.p,
       s.ev_val.p,
       s.row_len.p, s.pclass.p, ClassLists{s.wlist.p, s.llist.p, s.flist.p}, s.pixels_sum.p,
       s.stats.p);

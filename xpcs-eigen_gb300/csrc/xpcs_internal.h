@@ -175,6 +175,7 @@ struct DevStats {
   int32_t nlong;
   int32_t fnext;  // next float-path pixel to hand out (k_mt_fwarp)
   unsigned long long events;
+  unsigned long long dropped;  // K-a items sorted last (unused frames, bad pixel indices)
 };
 
 // -------------------------------------------------------------- two-time
@@ -240,7 +241,6 @@ struct Series {
   DBuf<int32_t> frA, frB;
   DBuf<float> vA, vB;
   DBuf<uint32_t> hist, hist_scan;
-  DBuf<int32_t> cnt;        // raw events per pixel
   DBuf<int64_t> row_ptr;    // [P+1]
   DBuf<int32_t> row_len;    // events per pixel after merging duplicates
   DBuf<uint8_t> pclass;
