@@ -102,6 +102,21 @@ __device__ __forceinline__ float scaled_quotient(int num, int shift, float den, 
   return __fmaf_rn(__fmaf_rn(-q0, den, x), rcp, q0);
 }
 
+// The same without branches, for divisors prepared by div_prep: num = 0 gives
+// +0 through the correction steps, and a delay without division carries
+// (den, rcp) = (1, 1), for which the steps return x unchanged.
+__device__ __forceinline__ float scaled_quotient_nb(int num, int shift, float den, float rcp) {
+  const float x = __fmul_rn((float)num, pow2_neg(shift));
+  const float q0 = __fmul_rn(x, rcp);
+  return __fmaf_rn(__fmaf_rn(-q0, den, x), rcp, q0);
+}
+__device__ __forceinline__ void div_prep(float &den, float &rcp) {
+  if (!(den > 0.f)) {
+    den = 1.f;
+    rcp = 1.f;
+  }
+}
+
 __device__ __forceinline__ int32_t pk_t(uint32_t w) { return (int32_t)(w >> 16); }
 __device__ __forceinline__ int32_t pk_v(uint32_t w) { return (int32_t)(int16_t)(w & 0xffffu); }
 __device__ __forceinline__ uint32_t pk(int32_t t, int32_t v) {
@@ -261,6 +276,7 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
           tf_l = ar.tau_abs[d0 + lane];
           den_l = ar.denom[d0 + lane];
           rc_l = ar.rcp[d0 + lane];
+          div_prep(den_l, rc_l);
         }
         for (int k = 0; k < nd; k++) {
           const int Tp = __shfl_sync(FULL, tp_l, k), Tf = __shfl_sync(FULL, tf_l, k);
@@ -294,8 +310,8 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
           // lanes without a row of this kernel have n0 = 0: both numerators are 0
           if (p < P) {
             const size_t o = (size_t)(d0 + k) * P + p;
-            IP[o] = scaled_quotient(total - rsum, lvl, den, rc);
-            IF[o] = scaled_quotient(s_end - ssum, lvl, den, rc);
+            IP[o] = scaled_quotient_nb(total - rsum, lvl, den, rc);
+            IF[o] = scaled_quotient_nb(s_end - ssum, lvl, den, rc);
           }
         }
       }
@@ -407,12 +423,13 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
       if (lane < nd) {
         den_l = ar.denom[d0 + lane];
         rc_l = ar.rcp[d0 + lane];
+        div_prep(den_l, rc_l);
       }
       for (int k = 0; k < nd; k++) {
         const float den = __shfl_sync(0xffffffffu, den_l, k), rc = __shfl_sync(0xffffffffu, rc_l, k);
         if (p < P)
           G2[(size_t)(d0 + k) * P + p] =
-              scaled_quotient(acc[(d0 - L.first + k) * 32], 2 * L.level, den, rc);
+              scaled_quotient_nb(acc[(d0 - L.first + k) * 32], 2 * L.level, den, rc);
       }
     }
   }
