@@ -372,11 +372,6 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
         bins_pairs<16>(row, m, L.lastframe, tlo, L.count, acc);
     } else if (sorted) {
       for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
-      // one flat loop, one visit per iteration, so that the lanes of a warp
-      // stay together however their pairs are spread: either the partner
-      // pointer j takes the next word (a pair when its distance is in
-      // [tlo, thi]; closer words can pair with no later source, so jlo moves
-      // past them) or the source i moves on and j restarts at jlo.
       // per source the next two entries are checked without a branch (lanes
       // stay together); a loop runs only while the second one is still short
       // of the window's end
