@@ -441,7 +441,7 @@ __device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *
 // 2^24 every float partial sum of pixelSum is exact, so pixelSum = (float)sum v;
 // otherwise each lane merges its own row / sums it in frame order.  Pixels
 // outside the mask get empty rows.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
 k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_float,
                  const int64_t *__restrict__ row_ptr, const uint8_t *__restrict__ mask,
                  int32_t *__restrict__ fr, float *__restrict__ val, int32_t *__restrict__ row_len,
@@ -482,7 +482,15 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
     if (lane == 0 && in && e > e0) fprev = fr[e - 1];
     if (in && e > ob && f == fprev) dup = true;
     const bool nonint = in && !(x == truncf(x) && fabsf(x) < 16777216.f);
-    const unsigned peers = __match_any_sync(0xffffffffu, in ? owner : 32);
+    // a row's lanes are one run (owners do not decrease across the lanes)
+    const int ow = in ? owner : 32;
+    const int oprev = __shfl_up_sync(0xffffffffu, ow, 1);
+    const unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || ow != oprev);
+    const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+    const int rs = 31 - __clz(starts & upto);
+    const unsigned after = starts & ~upto;
+    const unsigned peers =
+        (after ? ((1u << (__ffs(after) - 1)) - 1u) : 0xffffffffu) & ~((1u << rs) - 1u);
     const unsigned a = in ? (unsigned)fminf(fabsf(x), 16777216.f) : 0u;
     const int xi = (in && !nonint) ? (int)x : 0;
     const unsigned sum = __reduce_add_sync(peers, a);
