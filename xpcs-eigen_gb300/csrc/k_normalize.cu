@@ -93,30 +93,10 @@ __device__ __forceinline__ dw dw_from_double(double x) {
 }
 __device__ __forceinline__ double to_double(dw x) { return (double)x.h + (double)x.l; }
 
-// Sums N doubles over the block at once (one pair of barriers).
-template <int N>
-__device__ __forceinline__ void block_sum_n(double (&x)[N], double *sh) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < N; k++)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_down_sync(0xffffffffu, x[k], o);
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < N; k++) sh[k * (NB / 32) + w] = x[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < N; k++) {
-    double r = 0.0;
-#pragma unroll
-    for (int ww = 0; ww < NB / 32; ww++) r += sh[k * (NB / 32) + ww];
-    x[k] = r;
-  }
-  __syncthreads();
-}
-
 // Block sum of N double-word values: warp reduction in double-word arithmetic
-// on the FP32 pipes, FP64 only for the per-warp partials.
+// on the FP32 pipes, FP64 only for the per-warp partials, which thread 0 adds
+// up: out is valid in thread 0 only (FP64 runs at a small fraction of the FP32
+// rate here, so the other threads do not repeat those additions).
 template <int N>
 __device__ __forceinline__ void block_sum_dw(dw (&x)[N], double (&out)[N], double *sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -131,33 +111,16 @@ __device__ __forceinline__ void block_sum_dw(dw (&x)[N], double (&out)[N], doubl
 #pragma unroll
     for (int k = 0; k < N; k++) sh[k * (NB / 32) + w] = to_double(x[k]);
   __syncthreads();
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int k = 0; k < N; k++) {
-    double r = 0.0;
+    for (int k = 0; k < N; k++) {
+      double r = 0.0;
 #pragma unroll
-    for (int ww = 0; ww < NB / 32; ww++) r += sh[k * (NB / 32) + ww];
-    out[k] = r;
+      for (int ww = 0; ww < NB / 32; ww++) r += sh[k * (NB / 32) + ww];
+      out[k] = r;
+    }
   }
   __syncthreads();
-}
-
-__device__ __forceinline__ double block_sum(double x, double *sh) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if (lane == 0) sh[w] = x;
-  __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x < 32) {
-    r = threadIdx.x < NB / 32 ? sh[threadIdx.x] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-    if (threadIdx.x == 0) sh[NB / 32] = r;
-  }
-  __syncthreads();
-  r = sh[NB / 32];
-  __syncthreads();
-  return r;
 }
 
 // part layout: [chunk][tau][5] = sum G2, sum IP, sum IF, sum x, M2 about the chunk mean
@@ -166,6 +129,7 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
              const int32_t *__restrict__ pix, const float *__restrict__ G2,
              const float *__restrict__ IP, const float *__restrict__ IF, double *__restrict__ part) {
   __shared__ double sh[4 * (NB / 32) + 1];
+  __shared__ float s_mean[2];
   __shared__ float xh[NCH], xl[NCH];
   const int c = blockIdx.x, t = blockIdx.y;
   const int k0 = ch_k0[c], k1 = ch_k1[c];
@@ -190,9 +154,14 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
   const double n = (double)(k1 - k0);
   dw parts[4] = {sg, si, sf, sx};
   double sums[4];
-  block_sum_dw<4>(parts, sums, sh);
-  const double Sg = sums[0], Si = sums[1], Sf = sums[2], Sx = sums[3];
-  const dw mean = dw_from_double(Sx / n);
+  block_sum_dw<4>(parts, sums, sh);  // thread 0 holds the sums
+  if (threadIdx.x == 0) {
+    const dw mu = dw_from_double(sums[3] / n);
+    s_mean[0] = mu.h;
+    s_mean[1] = mu.l;
+  }
+  __syncthreads();
+  const dw mean{s_mean[0], s_mean[1]};
   const dw nmean{-mean.h, -mean.l};
   dw m2{0.f, 0.f};
 #pragma unroll
@@ -206,14 +175,13 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
   dw mparts[1] = {m2};
   double msum[1];
   block_sum_dw<1>(mparts, msum, sh);
-  const double M2 = msum[0];
   if (threadIdx.x == 0) {
     double *q = part + ((size_t)c * D + t) * 5;
-    q[0] = Sg;
-    q[1] = Si;
-    q[2] = Sf;
-    q[3] = Sx;
-    q[4] = M2;
+    q[0] = sums[0];
+    q[1] = sums[1];
+    q[2] = sums[2];
+    q[3] = sums[3];
+    q[4] = msum[0];
   }
 }
 
