@@ -262,3 +262,37 @@ def test_stride_past_65536_raw_frames_vs_oracle():
     rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F, stride=stride)
     oG2, oIP, oIF = oracle.multitau2(rows, F, 4, 0)
     assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+
+
+@pytest.mark.parametrize("odd_only", [True, False])
+def test_stride_drops_events_vs_oracle(odd_only):
+    """Stride 2 reads every other raw frame.  With events only in the skipped
+    frames every event sorts last and the rows come out empty; otherwise the
+    kept events interleave with dropped ones."""
+    F, W, H, stride = 50, 6, 4, 2
+    rng = np.random.default_rng(97)
+    P = W * H
+    nnz = np.zeros(F * stride, np.uint32)
+    idx, val = [], []
+    for r in range(F * stride):
+        if odd_only and r % 2 == 0:
+            continue
+        sel = np.flatnonzero(rng.random(P) < 0.3).astype(np.int32)
+        nnz[r] = sel.size
+        idx.append(sel)
+        val.append(rng.integers(1, 4, sel.size).astype(np.int16))
+    idx = np.concatenate(idx).astype(np.int32)
+    val = np.concatenate(val).astype(np.int16)
+    dq = np.ones((H, W), np.int32)
+    sq = dq.copy()
+    with xg.Series(W, H, F, 4, dq, sq, stride=stride) as s:
+        s.ingest_sparse(nnz, idx, val)
+        s.multitau(xg.MODE_REFERENCE)
+        G2, IP, IF = s.g2ipif()
+        info = s.info()
+    qm = oracle.QMap(dq, sq)
+    rows, _ = oracle.sparse_filter(qm, nnz, idx, val, F, stride=stride)
+    oG2, oIP, oIF = oracle.multitau2(rows, F, 4, 0)
+    assert same_bits(G2, oG2) and same_bits(IP, oIP) and same_bits(IF, oIF)
+    if odd_only:
+        assert info.events == 0 and not G2.any() and not IP.any()
