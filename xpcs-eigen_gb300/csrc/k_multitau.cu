@@ -22,18 +22,18 @@
 //     and the (monotone) per-delay thresholds give all of them.
 //   * G2 needs the compacted rows: per level the row is compacted in place
 //     (the same buffer the reference keeps, stale tail included) and the
-//     pairs whose bin distance lies in the level's delay window are scanned
-//     with a second pointer, in one flat loop per level (one visit per
-//     iteration) so that the lanes of a warp do not wait on each other's
-//     inner loops.  In REFERENCE mode a pair counts only when
-//     lower_bound over the whole buffer lands on the partner; that always
-//     holds while the buffer is globally sorted, which is tracked per level
-//     from the junction between the new prefix and the stale tail.
+//     pairs whose bin distance lies in the level's delay window are summed.
+//     In REFERENCE mode a pair counts only when lower_bound over the whole
+//     buffer lands on the partner; that always holds while the buffer is
+//     globally sorted, which is tracked per level from the junction between
+//     the new prefix and the stale tail.
 // k_mt_thread: one thread per pixel, rows packed (frame << 16 | int16 value)
 //   in shared memory with a lane-interleaved layout (conflict-free), outputs
 //   written straight to [D][P] (32 consecutive pixels per warp = coalesced).
-//   Pixels of other classes get zeros here and are rewritten by the kernels
-//   below.
+//   Levels of few bins find pairs from an occupancy bitmask of the row in the
+//   thread's scratch words; sparse levels check each source's next two
+//   entries without branching.  Pixels of other classes get zeros here and
+//   are rewritten by the kernels below.
 // k_mt_warp:   one warp per pixel, rows packed in shared memory: rows of up
 //   to 256 events (8 warps per block), up to 1024 (4 warps per block) and up
 //   to 4096 (2 warps per block).
