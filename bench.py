@@ -182,25 +182,27 @@ def cpu_cores():
 def run_reference_arm(args, dist):
     if dist.rank != 0:
         return
-    acq, dq, sq, nnz, idx, val = make_series_data()
+    # the same series as the GPU arm (--width / --frames select a reduced one)
+    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames)
     # size the per-step sample so the whole run stays within ~2-3 minutes
-    probe_frames = 200
+    probe_frames = min(200, acq.frames)
     t_probe = cpu_pipeline(acq, dq, sq, nnz, idx, val, probe_frames)
     budget = 150.0 / max(args.steps + args.warmup, 1)
-    frames = int(max(200, min(acq.frames, probe_frames * budget / max(t_probe, 1e-3))))
+    frames = int(max(probe_frames, min(acq.frames, probe_frames * budget / max(t_probe, 1e-3))))
     for _ in range(args.warmup):
         cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
     times = [cpu_pipeline(acq, dq, sq, nnz, idx, val, frames) for _ in range(args.steps)]
     t = sum(times) / len(times)
     v = frames / t
-    sample = (f"first {frames} of the {acq.frames} frames of the 1024x1024 series, full detector; "
+    sample = (f"first {frames} of the {acq.frames} frames of the {acq.width}x{acq.height} series, "
+              "full detector; "
               "sparse filter and normalisation serial, multi-tau OpenMP over all host threads")
     print(json.dumps({
         "impl": "reference", "metric": "multitau_frames_per_s", "value": v, "unit": "frames/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD_DESC, "frames_sampled": frames},
+        "config": {"workload": workload_desc(acq), "frames_sampled": frames},
         "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
