@@ -662,7 +662,7 @@ def run_gpu_arm(args, dist):
     if not args.no_corr and dist.rank == 0:
         result["corr"] = run_corr(args, acq, dq, sq, nnz, idx, val)
     if dist.rank == 0 and world == 1 and not args.no_cpu_baseline:
-        frames = args.cpu_sample_frames
+        frames = min(args.cpu_sample_frames, F)
         t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
         result["cpu_baseline"] = {
             "value": frames / t_cpu, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
