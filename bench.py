@@ -11,8 +11,8 @@ the library's stream).  `e2e`: the same step through the C ABI from pinned
 host frames, host-to-device copies and the g2/stderr readback inside the
 timed region (wall clock).  Every step reads/writes > 1 GB, far above L2.
 `--impl reference` times the CPU restatement of the reference's path (the
-oracle port; the reference's own binary is built for this container's x86
-host only) on a bounded sample of the same series.
+oracle port; the reference's own sources are not present where the GPU runs)
+on the same whole series, every step.
 
 Multi-GPU: each rank runs an independent replica of the series (the path has
 no cross-series exchange); value = frames of all ranks / max time over ranks.
@@ -48,6 +48,17 @@ def workload_desc(acq) -> str:
         return WORKLOAD_DESC
     return (f"{acq.width}x{acq.height} detector, {acq.frames} sparse IMM frames, otherwise as the "
             "1024x1024 10000-frame series (a reduced case for profiling)")
+
+
+def bench_config(acq, delays: int, qbins: int, raw_events: int, world: int) -> dict:
+    """The `config` object of both arms: the workload and what the timed step
+    reads, identical for the GPU arm and the reference arm."""
+    return {"workload": workload_desc(acq), "detector": f"{acq.width}x{acq.height}",
+            "frames": acq.frames, "delays": delays, "qbins": qbins, "raw_events": raw_events,
+            "mode": "reference",
+            "l2": (f"no flush: every step reads {raw_events * 6 >> 20} MB of raw events, "
+                   "above the 126 MB L2"),
+            "parallelism": f"replicas x{world}"}
 
 
 def rank_env():
@@ -180,29 +191,31 @@ def cpu_cores():
 
 
 def run_reference_arm(args, dist):
+    """The reference's CPU path (the oracle restatement of SparseFilter::Apply,
+    Corr::multiTau2 and Corr::normalizeG2s) on the whole series the GPU arm
+    runs: every step is the full --frames series, filter and normalisation
+    serial as in the reference, multi-tau OpenMP over every host thread."""
     if dist.rank != 0:
         return
-    # the same series as the GPU arm (--width / --frames select a reduced one)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
     acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames)
-    # size the per-step sample so the whole run stays within ~2-3 minutes
-    probe_frames = min(200, acq.frames)
-    t_probe = cpu_pipeline(acq, dq, sq, nnz, idx, val, probe_frames)
-    budget = 150.0 / max(args.steps + args.warmup, 1)
-    frames = int(max(probe_frames, min(acq.frames, probe_frames * budget / max(t_probe, 1e-3))))
+    qm = oracle.QMap(dq, sq)
+    lv, _ = oracle.delays(acq.frames, acq.dpl)
     for _ in range(args.warmup):
-        cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
-    times = [cpu_pipeline(acq, dq, sq, nnz, idx, val, frames) for _ in range(args.steps)]
+        cpu_pipeline(acq, dq, sq, nnz, idx, val, acq.frames)
+    times = [cpu_pipeline(acq, dq, sq, nnz, idx, val, acq.frames) for _ in range(args.steps)]
     t = sum(times) / len(times)
-    v = frames / t
-    sample = (f"first {frames} of the {acq.frames} frames of the {acq.width}x{acq.height} series, "
-              "full detector; "
-              "sparse filter and normalisation serial, multi-tau OpenMP over all host threads")
+    v = acq.frames / t
+    sample = (f"the whole {acq.frames}-frame {acq.width}x{acq.height} series every step "
+              "(no sampling); sparse filter and normalisation serial, multi-tau OpenMP over "
+              "all host threads")
     print(json.dumps({
         "impl": "reference", "metric": "multitau_frames_per_s", "value": v, "unit": "frames/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_desc(acq), "frames_sampled": frames},
+        "config": bench_config(acq, int(lv.size), int(qm.nq), int(idx.size), dist.world),
         "cpu_baseline": {"value": v, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -629,13 +642,9 @@ def run_gpu_arm(args, dist):
         "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32/f32 (bit-exact multi-tau), f64 normalisation",
         "data": "synthetic",
-        "config": {"workload": workload_desc(acq), "detector": f"{acq.width}x{acq.height}",
-                   "frames": F, "delays": D,
-                   "qbins": Q, "raw_events": int(info.raw_events), "events": int(info.events),
-                   "float_path_pixels": int(info.float_path_pixels), "mode": "reference",
-                   "l2": f"no flush: every step reads {idx.nbytes + val.nbytes >> 20} MB of raw "
-                         f"events and writes {12 * D * P >> 20} MB of G2/IP/IF, above the 126 MB L2",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(acq, D, Q, int(info.raw_events), world),
+        "series": {"events": int(info.events), "float_path_pixels": int(info.float_path_pixels),
+                   "g2ipif_written": True},
         "pixel_frames_per_s": value * P,
         "stages_ms": med,
         "normalize_f32_replay_ms": f32_ms,
@@ -662,12 +671,11 @@ def run_gpu_arm(args, dist):
     if not args.no_corr and dist.rank == 0:
         result["corr"] = run_corr(args, acq, dq, sq, nnz, idx, val)
     if dist.rank == 0 and world == 1 and not args.no_cpu_baseline:
-        frames = min(args.cpu_sample_frames, F)
-        t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, frames)
+        t_cpu = cpu_pipeline(acq, dq, sq, nnz, idx, val, F)
         result["cpu_baseline"] = {
-            "value": frames / t_cpu, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
-            "sample": f"first {frames} of {F} frames, full {acq.width}x{acq.height} detector "
-                      "(oracle restatement of SparseFilter + multiTau2 + normalizeG2s)"}
+            "value": F / t_cpu, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
+            "sample": f"the whole {F}-frame {acq.width}x{acq.height} series, once (oracle "
+                      "restatement of SparseFilter + multiTau2 + normalizeG2s)"}
     s.close()
     s2.close()
     xg.unpin(idx)
@@ -682,7 +690,6 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-sample-frames", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-series batch measure")
     ap.add_argument("--no-serving", action="store_true", help="skip the streaming measure")

@@ -207,6 +207,17 @@ int xpcs_synchronize(xpcs_series *s);
 
 int xpcs_get_stage_times(xpcs_series *s, xpcs_stage_times *t);
 
+/* Device-memory limit (no reference counterpart; the reference holds its rows
+ * in host memory).  Every device allocation the library makes on `device` is
+ * counted; with a non-zero limit, a call whose allocations would take the
+ * library's total on that device past `bytes` fails with
+ * XPCS_ERR_OUT_OF_MEMORY (message naming the limit) before CUDA is asked, and
+ * the handle stays usable: destroy or reset it, or raise the limit and call
+ * again.  0 = no limit (the default).  xpcs_get_device_memory reports the
+ * bytes the library holds on the device and the limit. */
+int xpcs_set_device_memory_limit(int32_t device, uint64_t bytes);
+int xpcs_get_device_memory(int32_t device, uint64_t *used, uint64_t *limit);
+
 /* Page-lock (cudaHostRegister) / release a caller buffer so that ingest copies
  * from it run at full host-to-device bandwidth.  No reference counterpart: the
  * reference reads frames from disk into pageable memory (imm.cpp:70-118). */
@@ -235,16 +246,27 @@ int xpcs_multitau2(const int64_t *row_ptr, const int32_t *frame, const float *va
  * one fixed static device array of 16 KiB + 8 bytes x XPCS_NOALLOC_MAX_EVENTS
  * (about 32 MiB), which every GPU that loads this library holds until the
  * process exits.
- *  - events > XPCS_NOALLOC_MAX_EVENTS is rejected with XPCS_ERR_INVALID_ARGUMENT.
+ *  - events > XPCS_NOALLOC_MAX_EVENTS, or a delay schedule (frames,
+ *    delays_per_level) of more than XPCS_NOALLOC_MAX_DELAYS delays, is
+ *    rejected with XPCS_ERR_INVALID_ARGUMENT.
  *  - Runs on the calling thread's current device, on `stream` (a cudaStream_t;
  *    NULL = the default stream), and waits for its own work to finish.
- *  - The first call on a device looks up the scratch's device address
- *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - The first call on a device is the set-up: it looks up the scratch's
+ *    device address (cudaGetSymbolAddress).  With CUDA's lazy module loading
+ *    (the default) that lookup is also when the driver loads this library's
+ *    device code and reserves the array on that device, so make the first
+ *    call at initialisation, with device memory to spare and before any
+ *    stream capture, or run with CUDA_MODULE_LOADING=EAGER.  A failed set-up
+ *    returns XPCS_ERR_OUT_OF_MEMORY or XPCS_ERR_CUDA with a message saying so.
+ *  - The address is kept per device for the life of the process; after a
+ *    cudaDeviceReset of that device it is stale, so do not call this entry
+ *    point on a device after resetting it.
  *  - All calls on a device share the one scratch array, so calls that overlap
  *    on the GPU (other host threads, other streams) race: serialise them.
  *  - Rows whose row_ptr lies outside [0, events] get zero outputs and the call
  *    returns XPCS_ERR_INPUT. */
 #define XPCS_NOALLOC_MAX_EVENTS 4194304
+#define XPCS_NOALLOC_MAX_DELAYS 512
 int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *frame, const float *value,
                            int32_t pixels, int64_t events, int32_t frames,
                            int32_t delays_per_level, int32_t mode, float *G2, float *IP,

@@ -36,12 +36,25 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
-def build_reference(ref_root: str = "/root/reference", jobs: int = 8) -> Path | None:
-    """Build the upstream `corr` from its own sources into oracle/_ref (when present)."""
-    if not Path(ref_root, "src", "xpcs", "corr.cpp").exists():
+def reference_root() -> Path:
+    """The upstream checkout the reference build reads: $XPCS_REFERENCE_SRC, or
+    the default the build recipe (ref_build/Makefile) names."""
+    env = os.environ.get("XPCS_REFERENCE_SRC")
+    if env:
+        return Path(env)
+    out = subprocess.run(["make", "-s", "-C", str(HERE / "ref_build"), "print-ref"],
+                         capture_output=True, text=True)
+    return Path(out.stdout.strip()) if out.returncode == 0 and out.stdout.strip() else Path()
+
+
+def build_reference(ref_root: str | None = None, jobs: int = 8) -> Path | None:
+    """Build the upstream `corr` from its own sources into oracle/_ref, when
+    the upstream checkout is present (None otherwise)."""
+    root = Path(ref_root) if ref_root else reference_root()
+    if not (root / "src" / "xpcs" / "corr.cpp").exists():
         return None
     subprocess.check_call(
-        ["make", "-s", "-C", str(HERE / "ref_build"), f"REF={ref_root}", f"-j{jobs}"]
+        ["make", "-s", "-C", str(HERE / "ref_build"), f"REF={root}", f"-j{jobs}"]
     )
     return REF_CORR
 

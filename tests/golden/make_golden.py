@@ -5,7 +5,10 @@ config), runs xpcs-eigen's own `corr --g2out` (built from its unmodified
 sources by oracle/ref_build) and stores inputs and every /exchange dataset in
 <case>.npz.  Run where the upstream checkout is mounted:
 
-    python tests/golden/make_golden.py [--ref /root/reference] [--only CASE]
+    python tests/golden/make_golden.py [--ref CHECKOUT] [--only CASE]
+
+CHECKOUT defaults to $XPCS_REFERENCE_SRC, else to the checkout the reference
+build recipe (oracle/ref_build/Makefile) reads.
 
 The fixtures pin the oracle (tests/test_oracle_golden.py) and the GPU path
 (tests/test_gpu_parity.py) to the reference's outputs.
@@ -248,12 +251,13 @@ def make_twotime(name, corr: Path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
-    corr = oracle.build_reference(a.ref)
+    ref = a.ref or str(oracle.reference_root())
+    corr = oracle.build_reference(ref)
     if corr is None:
-        sys.exit("reference sources not found at " + a.ref)
+        sys.exit("reference sources not found at " + ref)
     for name in CASES:
         if a.only and name != a.only:
             continue

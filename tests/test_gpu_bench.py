@@ -15,7 +15,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def test_gpu_arm_json_line():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--steps", "2", "--warmup", "3",
-                        "--width", "128", "--frames", "1000", "--cpu-sample-frames", "5000",
+                        "--width", "128", "--frames", "1000",
                         "--no-batch", "--no-serving", "--no-twotime", "--no-dense", "--no-corr"],
                        cwd=str(ROOT), capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -39,4 +39,11 @@ def test_gpu_arm_json_line():
     assert d["gpu_launches"] > 0
     cb = d["cpu_baseline"]
     assert cb["value"] > 0 and cb["kind"] == "port" and cb["cores"] >= 1
-    assert "first 1000 of 1000 frames" in cb["sample"]
+    assert "whole 1000-frame" in cb["sample"]
+    # the reference arm reports the identical config object for the same series
+    ref = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "0", "--width", "128", "--frames", "1000"],
+                         cwd=str(ROOT), capture_output=True, text=True, timeout=600)
+    assert ref.returncode == 0, ref.stderr[-2000:]
+    rd = json.loads([l for l in ref.stdout.splitlines() if l.startswith("{")][0])
+    assert rd["config"] == d["config"]

@@ -164,3 +164,25 @@ def test_errors_and_edge_cases():
         check(srv.result(d, g2ipif=True), alone(acq, dq, sq, frames))
         srv.release(c)
         srv.release(d)
+
+
+def test_close_after_finish_without_result():
+    """Closing the server while acquisitions are finishing (finish called,
+    result never read) waits for their work and frees them instead of
+    deadlocking on the completion callback."""
+    data = [make(i, *a) for i, a in enumerate(ACQS[:3])]
+    srv = xg.Server(memory_budget=8 << 30)
+    for acq, dq, sq, fr in data:
+        i = srv.submit(acq.width, acq.height, acq.frames, acq.dpl, dq, sq,
+                       expected_events=fr[1].size)
+        srv.push(i, *fr)
+        srv.finish(i)
+    srv.close()  # returns: nothing waits on a lock the callbacks need
+    # and a new server on the same device still works
+    acq, dq, sq, fr = data[0]
+    with xg.Server(memory_budget=8 << 30) as srv2:
+        i = srv2.submit(acq.width, acq.height, acq.frames, acq.dpl, dq, sq,
+                        expected_events=fr[1].size)
+        srv2.push(i, *fr)
+        srv2.finish(i)
+        check(srv2.result(i, g2ipif=True), alone(acq, dq, sq, fr))

@@ -1,6 +1,7 @@
 // C ABI of libxpcs_gpu (include/xpcs_gpu.h): series lifecycle, ingest,
 // multi-tau, normalisation, results and the per-stage CUDA-event tracer.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 
@@ -15,6 +16,45 @@ thread_local std::string g_last_error;
 namespace xg {
 thread_local int64_t tl_launches = 0;
 void xpcs_set_last_error(const char *msg) { g_last_error.assign(msg); }
+
+namespace {
+constexpr int ACCT_DEVICES = 64;
+std::atomic<uint64_t> g_dev_used[ACCT_DEVICES];
+std::atomic<uint64_t> g_dev_limit[ACCT_DEVICES];  // 0: no limit
+
+int acct_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= ACCT_DEVICES) return 0;
+  return dev;
+}
+}  // namespace
+
+void *dev_alloc(size_t bytes, cudaStream_t st) {
+  const int dev = acct_device();
+  const uint64_t lim = g_dev_limit[dev].load();
+  const uint64_t was = g_dev_used[dev].fetch_add(bytes);
+  if (lim && was + bytes > lim) {
+    g_dev_used[dev].fetch_sub(bytes);
+    throw Error(XPCS_ERR_OUT_OF_MEMORY,
+                "device memory limit reached: " + std::to_string(was + bytes) + " bytes asked, " +
+                    std::to_string(lim) + " allowed on device " + std::to_string(dev));
+  }
+  void *q = nullptr;
+  const cudaError_t e = cudaMallocAsync(&q, bytes, st);
+  if (e != cudaSuccess) {
+    g_dev_used[dev].fetch_sub(bytes);
+    cudaGetLastError();
+    throw Error(e == cudaErrorMemoryAllocation ? XPCS_ERR_OUT_OF_MEMORY : XPCS_ERR_CUDA,
+                std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+  }
+  return q;
+}
+
+void dev_free(void *p, size_t bytes, cudaStream_t st) {
+  if (!p) return;
+  cudaFreeAsync(p, st);
+  g_dev_used[acct_device()].fetch_sub(bytes);
+}
 }
 
 namespace {
@@ -661,6 +701,21 @@ int xpcs_get_stage_times(xpcs_series *h, xpcs_stage_times *t) {
     t->d2h_ms = el(8, 11);
     t->step_ms = el(2, 11);
     t->launches = s.launches;
+  });
+}
+
+int xpcs_set_device_memory_limit(int32_t device, uint64_t bytes) {
+  return guarded([&] {
+    need(device >= 0 && device < ACCT_DEVICES, "device ordinal out of range");
+    g_dev_limit[device].store(bytes);
+  });
+}
+
+int xpcs_get_device_memory(int32_t device, uint64_t *used, uint64_t *limit) {
+  return guarded([&] {
+    need(device >= 0 && device < ACCT_DEVICES, "device ordinal out of range");
+    if (used) *used = g_dev_used[device].load();
+    if (limit) *limit = g_dev_limit[device].load();
   });
 }
 

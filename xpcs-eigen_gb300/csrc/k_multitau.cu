@@ -44,6 +44,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "mt_replay.cuh"
 #include "xpcs_internal.h"
 
 namespace xg {
@@ -55,22 +56,8 @@ constexpr int MT_MID_CAP = 1024;  // long rows up to this length: 4 warps per bl
 constexpr int MID_WARPS = 4;
 constexpr int LONG_WARPS = 2;  // warps per block for rows of up to MT_LONG_CAP events
 
-// std::lower_bound as libstdc++ implements it (halving the remaining length).
-__device__ __forceinline__ int lower_bound_i32(const int32_t *a, int n, int32_t x) {
-  int first = 0, len = n;
-  while (len > 0) {
-    int half = len >> 1;
-    if (a[first + half] < x) {
-      first += half + 1;
-      len -= half + 1;
-    } else {
-      len = half;
-    }
-  }
-  return first;
-}
-
-// The same search over lane-interleaved packed words (frame in the high half).
+// std::lower_bound as libstdc++ implements it (halving the remaining length),
+// over lane-interleaved packed words (frame in the high half).
 __device__ __forceinline__ int lower_bound_packed(const uint32_t *row, int n, int32_t x) {
   int first = 0, len = n;
   while (len > 0) {
@@ -619,7 +606,7 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
            int32_t *__restrict__ sc_frame, float *__restrict__ sc_val, float *__restrict__ G2,
            float *__restrict__ IP, float *__restrict__ IF) {
   const McPlan *pl = (const McPlan *)plan_g;
-  const int D = pl->D, P = pl->P, mode = pl->mode;
+  const int D = pl->D, P = pl->P;
   const McArrays ar = mc_arrays(plan_g, D);
   const int nf = stats->nfloat;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nf; q += gridDim.x * blockDim.x) {
@@ -633,58 +620,7 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
       // normalize_by_framesum: v / (frameSum[f] / mean) (main.cpp:330-333)
       val[i] = fscale ? __fdiv_rn(ev_val[b + i], fscale[idx[i]]) : ev_val[b + i];
     }
-    int lastIndex = n0;
-    for (int gi = 0; gi < pl->nlev; gi++) {
-      const McLevel L = pl->lv[gi];
-      const int lastframe = L.lastframe;
-      if (L.compact) {
-        int index = 0, cnt = 0;
-        int i0 = idx[0] / 2, i1;  // (int)(idx / 2.0): truncation toward zero
-        if (lastIndex > 0 && i0 < lastframe) {
-          idx[index] = i0;
-          cnt = 1;
-        }
-        while (cnt < lastIndex) {
-          i1 = idx[cnt] / 2;
-          if (i1 >= lastframe) break;
-          if (i1 == i0) {
-            val[index] = __fadd_rn(val[index], val[cnt]);
-          } else {
-            idx[++index] = i1;
-            val[index] = val[cnt];
-          }
-          i0 = i1;
-          cnt++;
-        }
-        lastIndex = index + 1;
-        for (int r = 0; r < lastIndex; r++) val[r] = __fdiv_rn(val[r], 2.0f);
-      }
-      const int sn = mode == XPCS_MODE_REFERENCE ? n0 : lastIndex;
-      for (int k = 0; k < L.count; k++) {
-        const int d = L.first + k;
-        const int tau = ar.tau_lvl[d];
-        float g2 = 0.f, ip = 0.f, iff = 0.f;
-        for (int r = 0; r < lastIndex; r++) {
-          const int src = idx[r];
-          if (src < lastframe - tau) {
-            ip = __fadd_rn(ip, val[r]);
-            const int pos = lower_bound_i32(idx, sn, src + tau);
-            if (pos != sn && pos < lastIndex && idx[pos] == src + tau)
-              g2 = __fadd_rn(g2, __fmul_rn(val[r], val[pos]));
-          }
-          if (src >= tau && src < lastframe) iff = __fadd_rn(iff, val[r]);
-        }
-        const float den = ar.denom[d];
-        if (den > 0.f) {
-          g2 = __fdiv_rn(g2, den);
-          ip = __fdiv_rn(ip, den);
-          iff = __fdiv_rn(iff, den);
-        }
-        G2[(size_t)d * P + p] = g2;
-        IP[(size_t)d * P + p] = ip;
-        IF[(size_t)d * P + p] = iff;
-      }
-    }
+    replay_pixel(pl, ar, P, p, idx, val, n0, G2, IP, IF);
   }
 }
 

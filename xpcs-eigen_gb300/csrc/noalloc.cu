@@ -18,12 +18,16 @@
 #include <cstring>
 #include <mutex>
 
+#include "mt_replay.cuh"
 #include "xpcs_internal.h"
 
 namespace xg {
 namespace {
 
 constexpr size_t NA_PLAN_BYTES = 16384;
+static_assert(sizeof(McPlan) + (size_t)XPCS_NOALLOC_MAX_DELAYS * 6 * sizeof(int32_t) <=
+                  NA_PLAN_BYTES,
+              "the plan of the largest accepted delay schedule fits its scratch slot");
 constexpr size_t NA_STATUS_BYTES = 256;
 constexpr int64_t NA_MAX_EVENTS = XPCS_NOALLOC_MAX_EVENTS;
 constexpr size_t NA_SCRATCH_BYTES =
@@ -52,20 +56,6 @@ __host__ __device__ inline NaView na_view(unsigned char *base) {
                           (size_t)NA_MAX_EVENTS * sizeof(int32_t))};
 }
 
-__device__ __forceinline__ int na_lower_bound(const int32_t *a, int n, int32_t x) {
-  int first = 0, len = n;
-  while (len > 0) {
-    int half = len >> 1;
-    if (a[first + half] < x) {
-      first += half + 1;
-      len -= half + 1;
-    } else {
-      len = half;
-    }
-  }
-  return first;
-}
-
 __global__ void __launch_bounds__(128)
 k_mt_float_noalloc(unsigned char *scratch, const int64_t *__restrict__ row_ptr,
                    const int32_t *__restrict__ frame, const float *__restrict__ value,
@@ -73,7 +63,7 @@ k_mt_float_noalloc(unsigned char *scratch, const int64_t *__restrict__ row_ptr,
                    float *__restrict__ IF) {
   const NaView v = na_view(scratch);
   const McPlan *pl = (const McPlan *)v.plan;
-  const int D = pl->D, mode = pl->mode;
+  const int D = pl->D;
   const McArrays ar = mc_arrays(v.plan, D);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
     const int64_t b = row_ptr[p];
@@ -94,58 +84,7 @@ k_mt_float_noalloc(unsigned char *scratch, const int64_t *__restrict__ row_ptr,
       idx[i] = frame[b + i];
       val[i] = value[b + i];
     }
-    int lastIndex = n0;
-    for (int gi = 0; gi < pl->nlev; gi++) {
-      const McLevel L = pl->lv[gi];
-      const int lastframe = L.lastframe;
-      if (L.compact && n0 > 0) {
-        int index = 0, cnt = 0;
-        int i0 = idx[0] / 2, i1;  // (int)(idx / 2.0): truncation toward zero
-        if (lastIndex > 0 && i0 < lastframe) {
-          idx[index] = i0;
-          cnt = 1;
-        }
-        while (cnt < lastIndex) {
-          i1 = idx[cnt] / 2;
-          if (i1 >= lastframe) break;
-          if (i1 == i0) {
-            val[index] = __fadd_rn(val[index], val[cnt]);
-          } else {
-            idx[++index] = i1;
-            val[index] = val[cnt];
-          }
-          i0 = i1;
-          cnt++;
-        }
-        lastIndex = index + 1;
-        for (int r = 0; r < lastIndex; r++) val[r] = __fdiv_rn(val[r], 2.0f);
-      }
-      const int sn = mode == XPCS_MODE_REFERENCE ? n0 : lastIndex;
-      for (int k = 0; k < L.count; k++) {
-        const int d = L.first + k;
-        const int tau = ar.tau_lvl[d];
-        float g2 = 0.f, ip = 0.f, iff = 0.f;
-        for (int r = 0; r < lastIndex; r++) {
-          const int src = idx[r];
-          if (src < lastframe - tau) {
-            ip = __fadd_rn(ip, val[r]);
-            const int pos = na_lower_bound(idx, sn, src + tau);
-            if (pos != sn && pos < lastIndex && idx[pos] == src + tau)
-              g2 = __fadd_rn(g2, __fmul_rn(val[r], val[pos]));
-          }
-          if (src >= tau && src < lastframe) iff = __fadd_rn(iff, val[r]);
-        }
-        const float den = ar.denom[d];
-        if (den > 0.f) {
-          g2 = __fdiv_rn(g2, den);
-          ip = __fdiv_rn(ip, den);
-          iff = __fdiv_rn(iff, den);
-        }
-        G2[(size_t)d * P + p] = g2;
-        IP[(size_t)d * P + p] = ip;
-        IF[(size_t)d * P + p] = iff;
-      }
-    }
+    replay_pixel(pl, ar, P, p, idx, val, n0, G2, IP, IF);
   }
 }
 
@@ -174,7 +113,7 @@ int na_build_plan(int32_t P, int32_t F, int32_t dpl, int32_t mode, uint8_t *buf,
       }
     }
   }
-  if (head + (size_t)D * 5 * sizeof(int32_t) > cap) return -1;
+  if (D > XPCS_NOALLOC_MAX_DELAYS || head + (size_t)D * 6 * sizeof(int32_t) > cap) return -1;
   int32_t *base = (int32_t *)(buf + head);
   int32_t *tau_lvl = base;
   float *denom = (float *)(base + D);
@@ -257,9 +196,16 @@ extern "C" int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *fra
     std::lock_guard<std::mutex> lock(g_na_mutex);
     if (!g_na_ptr[dev]) {
       void *ptr = nullptr;
+      // under lazy module loading this first lookup also loads the module,
+      // which is when the driver reserves the array on this device
       cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-      if (e != cudaSuccess || !ptr)
-        return fail(XPCS_ERR_CUDA, "xpcs_multitau2_noalloc: cudaGetSymbolAddress failed");
+      if (e != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? XPCS_ERR_OUT_OF_MEMORY : XPCS_ERR_CUDA,
+                    "xpcs_multitau2_noalloc: the fixed scratch array could not be set up on this "
+                    "device (its first call loads the library's device code and reserves the "
+                    "array; make that call at initialisation, with device memory to spare)");
+      }
       g_na_ptr[dev] = (unsigned char *)ptr;
     }
     scratch = g_na_ptr[dev];
@@ -267,7 +213,9 @@ extern "C" int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *fra
   alignas(16) uint8_t plan[NA_PLAN_BYTES];
   const int D = na_build_plan(pixels, frames, delays_per_level, mode, plan, sizeof(plan));
   if (D < 0)
-    return fail(XPCS_ERR_INVALID_ARGUMENT, "xpcs_multitau2_noalloc: delay schedule too large");
+    return fail(XPCS_ERR_INVALID_ARGUMENT,
+                "xpcs_multitau2_noalloc: more delays than the fixed scratch holds "
+                "(XPCS_NOALLOC_MAX_DELAYS)");
   cudaStream_t st = (cudaStream_t)stream;
   const NaView v = na_view(scratch);
   if (cudaMemsetAsync(v.status, 0, sizeof(int32_t), st) != cudaSuccess ||

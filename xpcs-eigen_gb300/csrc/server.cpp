@@ -242,11 +242,20 @@ void server_destroy(void *h) {
     for (auto &kv : srv->slots) all.push_back(kv.second);
   }
   for (auto &sl : all) {
-    std::lock_guard<std::mutex> g(sl->mu);
-    if (sl->s) {
-      xpcs_synchronize(sl->s);
-      xpcs_series_destroy(sl->s);
+    // A finishing slot still has on_final queued on its stream, and on_final
+    // takes sl->mu: wait for it (as server_release does) and take the series
+    // out under the lock, then synchronise and destroy it without the lock.
+    xpcs_series *s = nullptr;
+    {
+      std::unique_lock<std::mutex> g(sl->mu);
+      if (sl->state == Slot::FINISHING)
+        sl->cv.wait(g, [&] { return sl->state == Slot::DONE || sl->state == Slot::FAILED; });
+      s = sl->s;
       sl->s = nullptr;
+    }
+    if (s) {
+      xpcs_synchronize(s);
+      xpcs_series_destroy(s);
     }
   }
   delete srv;

@@ -41,6 +41,13 @@ enum : int32_t { DEVERR_PIXEL_INDEX = 1 };
 
 // ------------------------------------------------------------ device buffers
 
+// Stream-ordered device allocation through the library's accounting: every
+// byte the library holds on a device is counted, and an allocation that would
+// take the device past its limit (xpcs_set_device_memory_limit) fails with
+// XPCS_ERR_OUT_OF_MEMORY before CUDA is asked (abi.cu).
+void *dev_alloc(size_t bytes, cudaStream_t st);
+void dev_free(void *p, size_t bytes, cudaStream_t st);
+
 // A stream-ordered device allocation that grows on demand.
 template <class T>
 struct DBuf {
@@ -48,9 +55,8 @@ struct DBuf {
   size_t cap = 0;
   void reserve(size_t n, cudaStream_t st) {
     if (n <= cap) return;
-    T *q = nullptr;
-    XG_CUDA(cudaMallocAsync((void **)&q, sizeof(T) * n, st));
-    if (p) XG_CUDA(cudaFreeAsync(p, st));
+    T *q = (T *)dev_alloc(sizeof(T) * n, st);
+    if (p) dev_free(p, sizeof(T) * cap, st);
     p = q;
     cap = n;
   }
@@ -59,15 +65,21 @@ struct DBuf {
     if (n <= cap) return;
     size_t c = cap ? cap : 1;
     while (c < n) c *= 2;
-    T *q = nullptr;
-    XG_CUDA(cudaMallocAsync((void **)&q, sizeof(T) * c, st));
-    if (p && keep) XG_CUDA(cudaMemcpyAsync(q, p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, st));
-    if (p) XG_CUDA(cudaFreeAsync(p, st));
+    T *q = (T *)dev_alloc(sizeof(T) * c, st);
+    if (p && keep) {
+      const cudaError_t e =
+          cudaMemcpyAsync(q, p, sizeof(T) * keep, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) {
+        dev_free(q, sizeof(T) * c, st);
+        XG_CUDA(e);
+      }
+    }
+    if (p) dev_free(p, sizeof(T) * cap, st);
     p = q;
     cap = c;
   }
   void release(cudaStream_t st) {
-    if (p) cudaFreeAsync(p, st);
+    if (p) dev_free(p, sizeof(T) * cap, st);
     p = nullptr;
     cap = 0;
   }

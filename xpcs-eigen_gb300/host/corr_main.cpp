@@ -12,7 +12,12 @@
 // The analysis file is read and written in the XH5C container format
 // (xh5c.h).  Extra flags: --mode=exact (lookup over the live prefix only),
 // --fp64 (write the float64 normalisation), --device=N, --block=N (frames
-// per ingest call).
+// per ingest call), --dry-run (read and check the configuration and every
+// frame the analysis would use, report, and stop before any GPU work).
+// Input errors the reference lets through -- a frame whose dlen exceeds the
+// detector (sparse) or differs from it (dense), a pixel index outside the
+// detector, a file that ends before the configured frames -- stop the run
+// with a message and exit status 1.
 #include <algorithm>
 #include <cctype>
 #include <chrono>
@@ -31,7 +36,7 @@
 namespace {
 
 struct Flags {
-  bool g2out = false, darkout = false, fp64 = false, frame_threading = false;
+  bool g2out = false, darkout = false, fp64 = false, frame_threading = false, dry_run = false;
   int frameout = 0, device = 0, block = 512;
   std::string imm, inpath, outpath, exchange, entry, mode = "reference";
   std::vector<std::string> positional;
@@ -66,6 +71,7 @@ bool parse(int argc, char **argv, Flags &f, std::string &err) {
     else if (k == "entry") f.entry = v;
     else if (k == "mode") f.mode = v;
     else if (k == "frame_threading") boolean(f.frame_threading);
+    else if (k == "dry-run" || k == "dry_run") boolean(f.dry_run);
     else if (k == "ufxc" || k == "rigaku" || k == "hdf5" || k == "transposed") {
       err = "--" + k + " selects a reader or analysis outside the multi-tau IMM path";
       return false;
@@ -232,8 +238,51 @@ int main(int argc, char **argv) {
       fprintf(stderr, "corr: cannot open IMM file %s\n", imm_path.c_str());
       return 1;
     }
+    rd.set_frame_pixels((int64_t)W * H);
     printf("[corr] %s: %dx%d, %d frames (stride %d, average %d), %s frames\n", imm_path.c_str(),
            W, H, F, stride, avg, rd.compressed() ? "sparse" : "dense");
+    if (dq.size() != (size_t)W * H || sq.size() != (size_t)W * H)
+      throw std::runtime_error("dqmap/sqmap size differs from the detector's x_dimension * "
+                               "y_dimension");
+    if (flat_on && flat.size() != (size_t)W * H)
+      throw std::runtime_error("flatfield size differs from the detector's pixel count");
+    if (fl.dry_run) {
+      // every frame the analysis would read, checked on the host; no GPU work
+      imm::Block blk;
+      int64_t r = 0, events = 0, bad = 0;
+      if (!rd.compressed() && darks > 0) {
+        const int n = rd.next(darks, blk);
+        if (n < 0) throw std::runtime_error(rd.error());
+        if (n != darks) throw std::runtime_error("short IMM file (darks)");
+        r += darks;
+      }
+      if (frame_from > 0 && r < frame_from) {
+        const int n = rd.skip((int)(frame_from - r));
+        if (n < 0) throw std::runtime_error(rd.error());
+        r += n;
+      }
+      const int64_t want = (int64_t)F * read_in;
+      int64_t got = 0;
+      while (got < want) {
+        const int n = rd.next((int)std::min<int64_t>(fl.block, want - got), blk);
+        if (n < 0) throw std::runtime_error(rd.error());
+        if (n == 0) break;
+        for (int32_t p : blk.idx) bad += (p < 0 || (int64_t)p >= (int64_t)W * H);
+        events += (int64_t)blk.val.size();
+        got += n;
+      }
+      if (got < want)
+        throw std::runtime_error("IMM file ends after " + std::to_string(got) + " of " +
+                                 std::to_string(want) + " frames");
+      if (bad)
+        throw std::runtime_error(std::to_string(bad) +
+                                 " pixel indices lie outside the detector");
+      int32_t nd = 0;
+      CHECK(xpcs_delay_schedule(F, dpl, nullptr, nullptr, 0, &nd));
+      printf("[corr] dry run: %d frames, %lld events, %d delays: input is valid\n", F,
+             (long long)events, nd);
+      return 0;
+    }
     xpcs_series_desc d{};
     d.width = W;
     d.height = H;
@@ -262,16 +311,23 @@ int main(int argc, char **argv) {
       imm::Block blk;
       int r = 0;
       if (!rd.compressed() && darks > 0) {  // the first frames of the file (main.cpp:227-239)
-        if (rd.next(darks, blk) != darks) throw std::runtime_error("short IMM file (darks)");
+        const int n = rd.next(darks, blk);
+        if (n < 0) throw std::runtime_error(rd.error());
+        if (n != darks) throw std::runtime_error("short IMM file (darks)");
         CHECK(xpcs_set_dark(s, blk.val.data(), darks));
         r += darks;
       }
-      if (frame_from > 0 && r < frame_from) r += rd.skip(frame_from - r);
+      if (frame_from > 0 && r < frame_from) {
+        const int n = rd.skip(frame_from - r);
+        if (n < 0) throw std::runtime_error(rd.error());
+        r += n;
+      }
       const int want = F * read_in;
       int got = 0;
       while (got < want) {
         int n = rd.next(std::min(fl.block, want - got), blk);
-        if (n <= 0) break;
+        if (n < 0) throw std::runtime_error(rd.error());
+        if (n == 0) break;
         if (rd.compressed())
           CHECK(xpcs_ingest_sparse(s, blk.idx.data(), blk.val.data(), blk.nnz.data(), n));
         else
@@ -285,7 +341,9 @@ int main(int argc, char **argv) {
         }
         got += n;
       }
-      if (got < want) fprintf(stderr, "corr: warning: IMM file ends after %d of %d frames\n", got, want);
+      if (got < want)
+        throw std::runtime_error("IMM file ends after " + std::to_string(got) + " of " +
+                                 std::to_string(want) + " frames");
     }
     const std::string g = output + "/";
     if (twotime) {

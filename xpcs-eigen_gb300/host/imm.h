@@ -6,6 +6,11 @@
 // (int32 @620, the frame's tick).  Sparse frames carry int32 pixel indices
 // then int16 values; dense frames carry int16 values only.  Values are read as
 // signed 16-bit, as the reference reads them (imm.cpp:87-99).
+//
+// Unlike the reference (which trusts dlen and goes on after a short read,
+// imm.cpp:70-118), the reader refuses a frame whose dlen exceeds the
+// detector's pixel count (sparse) or differs from it (dense), and a file that
+// ends inside a frame; next() and skip() then return -1 and error() says why.
 #pragma once
 
 #include <cstdint>
@@ -27,14 +32,24 @@ class Reader {
   ~Reader();
   bool open(const std::string &path);
   bool compressed() const { return compressed_; }
-  // Reads up to `count` frames; returns the number read (0 at end of file).
+  // The detector's pixel count (width * height): the bound on dlen.
+  void set_frame_pixels(int64_t pixels) { pixels_ = pixels; }
+  // Reads up to `count` frames; returns the number read (fewer only at the
+  // end of the file), or -1 for a corrupt or truncated frame.
   int next(int count, Block &out);
-  // Skips `count` frames (Imm::SkipFrames, imm.cpp:120-129).
+  // Skips `count` frames (Imm::SkipFrames, imm.cpp:120-129); same returns.
   int skip(int count);
+  // Frames read or skipped so far.
+  int64_t position() const { return frame_; }
+  const std::string &error() const { return error_; }
 
  private:
+  bool check_dlen(uint32_t n);
   FILE *f_ = nullptr;
   bool compressed_ = false;
+  int64_t pixels_ = -1;  // unknown: no bound
+  int64_t frame_ = 0;
+  std::string error_;
 };
 
 }  // namespace imm

@@ -38,6 +38,7 @@ EXPORTS = [
     "xpcs_autotune", "xpcs_server_create", "xpcs_server_destroy", "xpcs_server_submit",
     "xpcs_server_push_sparse", "xpcs_server_finish", "xpcs_server_state", "xpcs_server_result",
     "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
+    "xpcs_set_device_memory_limit", "xpcs_get_device_memory",
 ]
 
 BATCH_F64 = 1
@@ -46,6 +47,7 @@ BATCH_AUTOTUNE = 4
 TWOTIME_EXACT_CUDA_CORES = 2
 
 NOALLOC_MAX_EVENTS = 4194304
+NOALLOC_MAX_DELAYS = 512
 
 
 class TwoTimeDesc(C.Structure):
@@ -160,6 +162,9 @@ def lib() -> C.CDLL:
         L.xpcs_multitau2_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                              C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.xpcs_set_device_memory_limit.argtypes = [C.c_int32, C.c_uint64]
+        L.xpcs_get_device_memory.argtypes = [C.c_int32, C.POINTER(C.c_uint64),
+                                             C.POINTER(C.c_uint64)]
         L.xpcs_pin_host.argtypes = [C.c_void_p, C.c_uint64]
         L.xpcs_unpin_host.argtypes = [C.c_void_p]
         L.xpcs_multitau2.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
@@ -471,6 +476,18 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def set_device_memory_limit(device: int, nbytes: int) -> None:
+    """Cap the device memory the library may hold on `device` (0: no cap)."""
+    check(lib().xpcs_set_device_memory_limit(device, int(nbytes)))
+
+
+def device_memory(device: int = 0) -> tuple[int, int]:
+    """(bytes the library holds on `device`, its limit; 0 = none)."""
+    used, limit = C.c_uint64(0), C.c_uint64(0)
+    check(lib().xpcs_get_device_memory(device, C.byref(used), C.byref(limit)))
+    return used.value, limit.value
 
 
 def pin(a: np.ndarray) -> np.ndarray:
