@@ -264,7 +264,9 @@ int xpcs_multitau2(const int64_t *row_ptr, const int32_t *frame, const float *va
  *  - All calls on a device share the one scratch array, so calls that overlap
  *    on the GPU (other host threads, other streams) race: serialise them.
  *  - Rows whose row_ptr lies outside [0, events] get zero outputs and the call
- *    returns XPCS_ERR_INPUT. */
+ *    returns XPCS_ERR_INPUT.  A decreasing row_ptr entry makes the rows around
+ *    it overlap; the outputs of overlapping rows are then unspecified (every
+ *    access still stays inside [0, events)). */
 #define XPCS_NOALLOC_MAX_EVENTS 4194304
 #define XPCS_NOALLOC_MAX_DELAYS 512
 int xpcs_multitau2_noalloc(const int64_t *row_ptr, const int32_t *frame, const float *value,

@@ -115,8 +115,13 @@ def test_noalloc_row_pointers_outside_the_events_give_input_error_and_zero_rows(
             b.free()
     for p in bad:
         assert not got[:, :, p].any()
-    good = [p for p in range(P) if p not in bad and rp[p + 1] - rp[p] == rows.row_ptr[p + 1] -
-            rows.row_ptr[p]]
+    # the descending entry also makes row 6 start inside row 4: rows that share
+    # scratch words with another row give unspecified values; the rest are exact
+    lo6, hi6 = rp[6], rp[7]
+    good = [p for p in range(P) if p not in bad and p != 6
+            and rp[p] == rows.row_ptr[p] and rp[p + 1] == rows.row_ptr[p + 1]
+            and (rp[p + 1] <= lo6 or rp[p] >= hi6)]
+    assert len(good) > P - 10
     for k in range(3):
         assert same_bits(got[k][:, good], want[k][:, good])
 
