@@ -127,6 +127,19 @@ int xpcs_series_reset(xpcs_series *s);
 
 int xpcs_series_get_info(xpcs_series *s, xpcs_series_info *info);
 
+/* Incremental transposes (no reference counterpart: SparseFilter::Apply pushes
+ * each frame onto per-pixel rows as it is read, sparse_filter.cpp:115-193, and
+ * this keeps that property on the GPU).  With block_frames > 0, every time
+ * block_frames complete filter frames (block_frames * stride * avg raw frames)
+ * have been ingested, they are filtered and transposed on the handle's stream
+ * into pixel-major rows that stay on the device; xpcs_multitau then
+ * transposes only the last, partial block and joins the blocks' rows in frame
+ * order.  The event lists, and every result, are bit-identical to those of one
+ * transpose of all frames.  0 (the default) transposes everything at
+ * xpcs_multitau.  Set it before ingesting frames (XPCS_ERR_STATE otherwise).
+ * Such a handle cannot join a batch. */
+int xpcs_series_set_block_frames(xpcs_series *s, int32_t block_frames);
+
 /* Imm::NextFrames + SparseFilter::Apply input (imm.cpp:70-118,
  * sparse_filter.cpp:115-193): append `nframes` raw sparse frames.  Frame r has
  * nnz[r] events idx[..] (int32 pixel index) and val[..] (int16 value, read as
@@ -311,6 +324,8 @@ typedef struct {
   int32_t sg_rows, sg_cols;
   float gram_ms;            /* EXACT mode: device time of the tensor-core Gram kernels */
   double gram_flop;         /* EXACT mode: their multiply-add work, 2 x M x N x K per tile */
+  double gram_flop_algorithmic; /* EXACT mode: the upper triangle's own work,
+                                   2 x rows x F (F + 1) / 2 per smoothing group */
 } xpcs_twotime_info;
 int xpcs_twotime(xpcs_series *s, const xpcs_twotime_desc *d, int32_t mode,
                  xpcs_twotime_info *info);
@@ -353,13 +368,16 @@ void xpcs_batch_destroy(xpcs_batch *b);
 /* Serving (no reference counterpart): several acquisitions streamed at once.
  * An acquisition is submitted with its series description and expected event
  * count; it is admitted -- its series created on the GPU -- as soon as its
- * estimated device footprint (raw events and work buffers, ~46 B per event,
- * plus 12 B per pixel and delay for G2/IP/IF) fits `memory_budget`, in
- * submission order (an acquisition larger than the budget is admitted when
- * nothing else is active).  Frames pushed before admission wait in host
- * memory.  push copies frames into the acquisition's resident buffers on its
- * own stream and returns; finish enqueues filter/transpose, multi-tau and the
- * float64 normalisation and returns; result waits and reads g2/stderr [D][Q]
+ * estimated device footprint (raw events, resident rows and work buffers,
+ * ~54 B per event, plus 12 B per pixel and delay for G2/IP/IF) fits
+ * `memory_budget`, in submission order (an acquisition larger than the budget
+ * is admitted when nothing else is active).  Frames pushed before admission
+ * wait in host memory.  push copies frames into the acquisition's resident
+ * buffers on its own stream and returns; every 512 frames the acquisition's
+ * new frames are transposed on its stream into pixel-major rows that stay
+ * resident (xpcs_series_set_block_frames); finish enqueues the last block's
+ * transpose, the join of the rows, multi-tau and the float64 normalisation
+ * and returns; result waits and reads g2/stderr [D][Q]
  * (and G2/IP/IF [D][P]; any pointer may be NULL); release frees the series and
  * admits waiting acquisitions.  Results equal those of the series run alone.
  * Different acquisitions may be driven from different threads; calls for one

@@ -176,6 +176,13 @@ void free_series(Series *s) {
     s->keyB.release(st);
     s->hist.release(st);
     s->hist_scan.release(st);
+    s->d_blk_base.release(st);
+    s->blk_fr.release(st);
+    s->blk_val.release(st);
+    s->blk_off.release(st);
+    s->blk_len.release(st);
+    s->blk_rp.release(st);
+    s->blk_tot.release(st);
     s->stats.release(st);
     cudaStreamSynchronize(st);
     for (auto &e : s->ev)
@@ -276,6 +283,7 @@ int xpcs_series_reset(xpcs_series *h) {
     DeviceGuard g(s.device);
     XG_CUDA(cudaStreamSynchronize(s.stream));
     s.frame_off.assign(1, 0);
+    reset_blocks(s);
     s.raw_events = 0;
     s.rmin_ready = s.rmin_ready && s.has_dark;
     s.raw_frames = 0;
@@ -286,6 +294,17 @@ int xpcs_series_reset(xpcs_series *h) {
     s.timed_h2d = false;
     s.h2d_ms_acc = 0.f;
     s.generation++;
+  });
+}
+
+int xpcs_series_set_block_frames(xpcs_series *h, int32_t block_frames) {
+  return guarded([&] {
+    need(h, "null handle");
+    need(block_frames >= 0, "block_frames must be non-negative");
+    Series &s = *(Series *)h;
+    if (s.raw_frames > 0)
+      throw Error(XPCS_ERR_STATE, "set the block size before ingesting frames");
+    s.block_frames = block_frames;
   });
 }
 
@@ -343,6 +362,7 @@ static void ingest_common(Series &s, const int32_t *idx, const int16_t *val, con
   s.have_multitau = false;
   s.tt.ready = false;
   s.generation++;
+  transpose_ready_blocks(s);
 }
 
 int xpcs_ingest_sparse(xpcs_series *h, const int32_t *idx, const int16_t *val,
@@ -391,6 +411,7 @@ static int ingest_dense_common(xpcs_series *h, const int16_t *frames, int32_t nf
     s.generation++;
     s.have_multitau = false;
     s.tt.ready = false;
+    transpose_ready_blocks(s);
     XG_CUDA(cudaEventRecord(s.ev[1], s.stream));
   });
 }
@@ -537,6 +558,7 @@ int xpcs_twotime(xpcs_series *h, const xpcs_twotime_desc *d, int32_t mode,
       info->sg_cols = s.tt.sg_cols;
       info->gram_ms = s.tt.gram_ms;
       info->gram_flop = s.tt.gram_flop;
+      info->gram_flop_algorithmic = s.tt.gram_flop_alg;
     }
   });
 }

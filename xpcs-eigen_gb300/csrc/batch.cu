@@ -45,6 +45,10 @@ Batch *batch_create(Series *const *ss, int32_t n) {
     if (ss[i]->desc.normalize_by_framesum)
       throw Error(XPCS_ERR_INVALID_ARGUMENT,
                   "normalize_by_framesum reads frame sums back to the host: not in a batch");
+    if (ss[i]->block_frames > 0)
+      throw Error(XPCS_ERR_INVALID_ARGUMENT,
+                  "series with incremental transposes finish from host-held block tables: "
+                  "not in a batch");
   }
   Batch *b = new Batch();
   try {

@@ -21,6 +21,9 @@
 //            160-172), pixelSum is accumulated in frame order, pixels outside
 //            the mask (sparse_filter.cpp:147) get empty rows, and every pixel
 //            is classified for the multi-tau kernels.
+#include <algorithm>
+#include <cstddef>
+
 #include "f64emu.cuh"
 #include "xpcs_internal.h"
 
@@ -35,6 +38,10 @@ constexpr int64_t RS_BIG_N = (int64_t)1 << 27;
 constexpr int RS_DIGITS = 256;
 static_assert(RS_THREADS == RS_DIGITS, "one digit per thread in the downsweep scan");
 
+// The raw frames [r0, r0 + nframes) of a series: idx/val/valf start at their
+// first event e0, frame_off/frame_map at r0, and frame_off holds absolute
+// event offsets, so an event's index relative to e0 is compared with
+// frame_off[r] - e0.
 struct RawCfg {
   const int32_t *idx;
   const int16_t *val;   // sparse series: raw values (flatfield applied here)
@@ -43,6 +50,7 @@ struct RawCfg {
   const int32_t *frame_map;  // [nframes]: filter frame of a raw frame, -1 if unused
   const int32_t *chunk_frame;  // [ceil(n / chunk)]: raw frame of item chunk * c
   int32_t nframes;
+  int64_t e0;
   int64_t n;
   int32_t P, F, R_in, stride;
   const double *flat;  // may be null
@@ -63,13 +71,14 @@ struct PassCfg {
 };
 
 // Raw frame of the first item of every chunk of 32 * IPT items (one warp's
-// share of a tile): chunk c starts in frame r when off[r] <= chunk c < off[r + 1].
-__global__ void k_chunk_frames(int32_t nframes, const int64_t *__restrict__ off, int64_t nchunks,
-                               int32_t chunk, int32_t *__restrict__ chunk_frame) {
+// share of a tile): chunk c starts in frame r when off[r] - e0 <= chunk c <
+// off[r + 1] - e0.
+__global__ void k_chunk_frames(int32_t nframes, const int64_t *__restrict__ off, int64_t e0,
+                               int64_t nchunks, int32_t chunk, int32_t *__restrict__ chunk_frame) {
   const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nframes) return;
-  const int64_t c0 = (off[r] + chunk - 1) / chunk;
-  const int64_t c1 = min((off[r + 1] + chunk - 1) / chunk, nchunks);
+  const int64_t c0 = (off[r] - e0 + chunk - 1) / chunk;
+  const int64_t c1 = min((off[r + 1] - e0 + chunk - 1) / chunk, nchunks);
   for (int64_t c = c0; c < c1; c++) chunk_frame[c] = r;
 }
 
@@ -90,7 +99,7 @@ __device__ __forceinline__ bool raw_frame_key(const RawCfg &c, int64_t i, int32_
                                               int32_t &frame) {
   while (nb <= i) {
     r++;
-    nb = c.frame_off[r + 1];
+    nb = c.frame_off[r + 1] - c.e0;
     k = c.frame_map[r];
   }
   frame = k;
@@ -146,7 +155,7 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist) {
   if (FIRST) {
     const int64_t nch = (rc.n + 32 * IPT - 1) / (32 * IPT);
     int32_t r = rc.chunk_frame[min((int64_t)tile * RS_WARPS + w, nch - 1)];
-    int64_t nb = rc.frame_off[r + 1];
+    int64_t nb = rc.frame_off[r + 1] - rc.e0;
     int32_t kf = rc.frame_map[r];
     int32_t pix[IPT];
 #pragma unroll
@@ -161,7 +170,7 @@ k_upsweep(RawCfg rc, PassCfg pc, uint32_t *__restrict__ hist) {
       if (i < pc.n) {
         while (nb <= i) {
           r++;
-          nb = rc.frame_off[r + 1];
+          nb = rc.frame_off[r + 1] - rc.e0;
           kf = rc.frame_map[r];
         }
         const int32_t p = pix[k];
@@ -224,7 +233,7 @@ k_downsweep(RawCfg rc, PassCfg pc, const uint32_t *__restrict__ offsets) {
   if (FIRST) {
     const int64_t nch = (rc.n + 32 * IPT - 1) / (32 * IPT);
     int32_t r = rc.chunk_frame[min((int64_t)tile * RS_WARPS + w, nch - 1)];
-    int64_t nb = rc.frame_off[r + 1];
+    int64_t nb = rc.frame_off[r + 1] - rc.e0;
     int32_t kf = rc.frame_map[r];
     int32_t pix[IPT];
 #pragma unroll
@@ -609,9 +618,114 @@ bool radix_sort_triples(Series &s, uint32_t *key, int32_t *a, float *b, uint32_t
   return (passes & 1) != 0;
 }
 
-void run_filter_transpose(Series &s) {
+namespace {
+
+// Device copies of the per-raw-frame tables (event offsets, filter frame of
+// every raw frame) after frames were ingested.
+void upload_frame_tables(Series &s) {
   cudaStream_t st = s.stream;
-  const int64_t n = s.raw_events;
+  if (!s.frame_off_dirty) return;
+  s.d_frame_off.reserve(s.frame_off.size(), st);
+  XG_CUDA(cudaMemcpyAsync(s.d_frame_off.p, s.frame_off.data(),
+                          sizeof(int64_t) * s.frame_off.size(), cudaMemcpyHostToDevice, st));
+  s.frame_map.resize(s.raw_frames);
+  for (int32_t r = 0; r < s.raw_frames; r++) {  // stride*avg raw frames per filter frame
+    const int32_t k = r / s.R_in;
+    s.frame_map[r] = (k < s.F && ((r - k * s.R_in) % s.desc.stride_frames) == 0) ? k : -1;
+  }
+  s.d_frame_map.reserve(s.frame_map.size() ? s.frame_map.size() : 1, st);
+  if (!s.frame_map.empty())
+    XG_CUDA(cudaMemcpyAsync(s.d_frame_map.p, s.frame_map.data(),
+                            sizeof(int32_t) * s.frame_map.size(), cudaMemcpyHostToDevice, st));
+  s.frame_off_dirty = false;
+}
+
+// Filter and stable radix transpose of the raw frames [r0, r1): pixel-major
+// events into ev_fr / ev_val and their row pointers (relative to ev_fr) into
+// row_ptr [P+1].  Needs the frame tables on the device.
+void transpose_range(Series &s, int32_t r0, int32_t r1, int32_t *ev_fr, float *ev_val,
+                     int64_t *row_ptr) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P;
+  const int64_t e0 = s.frame_off[r0], n = s.frame_off[r1] - e0;
+  s.scan_tmp.reserve(scan_workspace_bytes(P), st);
+  if (n <= 0) {
+    XG_CUDA(cudaMemsetAsync(row_ptr, 0, sizeof(int64_t) * ((size_t)P + 1), st));
+    return;
+  }
+  // the count of items sorted last, read by the row pointers, is per range
+  XG_CUDA(cudaMemsetAsync(&s.stats.p->dropped, 0, sizeof(unsigned long long), st));
+  const int nbits = 32 - __builtin_clz((unsigned)P);  // bits to hold P (the drop key)
+  const int passes = (nbits + 7) / 8;
+  const int ipt = items_per_lane(n);
+  const int ntiles = (int)((n + RS_THREADS * ipt - 1) / (RS_THREADS * ipt));
+  s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
+  s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);
+  const size_t ws = scan_workspace_bytes((int64_t)RS_DIGITS * ntiles);
+  s.scan_tmp.reserve(std::max(ws, scan_workspace_bytes(P)), st);
+  // sparse series below 65,536 filter frames carry one packed word per item
+  // (frame, raw value) through the passes instead of a frame and a value
+  const bool dense = s.desc.dense != 0;
+  const bool packed = !dense && s.F <= 65536;
+  // the last pass also writes the kept items' keys, for the row pointers
+  s.keyA.reserve(n, st);
+  if (passes > 1) {
+    s.keyB.reserve(n, st);
+    s.frA.reserve(n, st);
+    if (!packed) s.vA.reserve(n, st);
+  }
+  if (passes > 2) {
+    s.frB.reserve(n, st);
+    if (!packed) s.vB.reserve(n, st);
+  }
+  const int chunk = 32 * ipt;
+  const int64_t nch = (n + chunk - 1) / chunk;
+  const int32_t nfr = r1 - r0;
+  s.d_chunk_frame.reserve((size_t)nch, st);
+  k_chunk_frames<<<(nfr + 255) / 256, 256, 0, st>>>(nfr, s.d_frame_off.p + r0, e0, nch, chunk,
+                                                     s.d_chunk_frame.p);
+  XG_CHECK_LAUNCH();
+  RawCfg rc{s.raw_idx.p + e0, dense ? nullptr : s.raw_val.p + e0,
+            dense ? s.raw_valf.p + e0 : nullptr, s.d_frame_off.p + r0, s.d_frame_map.p + r0,
+            s.d_chunk_frame.p, nfr, e0, n, P, s.F, s.R_in, s.desc.stride_frames,
+            s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
+  uint32_t *kbuf[2] = {s.keyA.p, s.keyB.p};
+  int32_t *fbuf[2] = {s.frA.p, s.frB.p};
+  float *vbuf[2] = {s.vA.p, s.vB.p};
+  for (int pass = 0; pass < passes; pass++) {
+    bool first = pass == 0, last = pass == passes - 1;
+    PassCfg pc{};
+    pc.n = n;
+    pc.shift = 8 * pass;
+    pc.ntiles = ntiles;
+    pc.sentinel = (uint32_t)P;
+    if (!first) {
+      pc.key_in = kbuf[(pass - 1) & 1];
+      pc.fr_in = fbuf[(pass - 1) & 1];
+      pc.v_in = vbuf[(pass - 1) & 1];
+    }
+    if (last) {
+      pc.key_out = kbuf[pass & 1];  // not the pass's input
+      pc.fr_out = ev_fr;
+      pc.v_out = ev_val;
+    } else {
+      pc.key_out = kbuf[pass & 1];
+      pc.fr_out = fbuf[pass & 1];
+      pc.v_out = vbuf[pass & 1];
+    }
+    if (ipt == 16)
+      radix_pass<16>(s, first, last, packed, ntiles, rc, pc);
+    else
+      radix_pass<8>(s, first, last, packed, ntiles, rc, pc);
+  }
+  const uint32_t *keys = (passes % 2 == 0) ? s.keyB.p : s.keyA.p;  // written by the last pass
+  k_row_ptr<<<(unsigned)(((int64_t)P + 1 + 255) / 256), 256, 0, st>>>(keys, n, s.stats.p, P,
+                                                                      row_ptr);
+  XG_CHECK_LAUNCH();
+}
+
+void reserve_lists(Series &s) {
+  cudaStream_t st = s.stream;
   const int32_t P = s.P;
   s.row_ptr.reserve((size_t)P + 1, st);
   s.row_len.reserve(P, st);
@@ -621,110 +735,192 @@ void run_filter_transpose(Series &s) {
   s.llist.reserve(P, st);
   s.pixels_sum.reserve(P, st);
   s.stats.reserve(1, st);
-  XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
-  size_t nalloc = n > 0 ? (size_t)n : 1;
+}
+
+void merge_classify(Series &s, int32_t avg) {
+  const int pix_per_block = 256;
+  k_merge_classify<<<(s.P + pix_per_block - 1) / pix_per_block, 256, 0, s.stream>>>(
+      s.P, s.F, avg, s.thread_cap, s.desc.normalize_by_framesum, s.row_ptr.p, s.d_mask.p,
+      s.ev_frame.p, s.ev_val.p, s.row_len.p, s.pclass.p,
+      ClassLists{s.wlist.p, s.llist.p, s.flist.p}, s.pixels_sum.p, s.stats.p);
+  XG_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+// ----------------------------------------------------- incremental transposes
+//
+// With a block size set (xpcs_series_set_block_frames), the frames are
+// transposed as they are ingested, block by block (block_frames filter frames
+// = block_frames * stride * avg raw frames, so that a filter frame's raw
+// frames never straddle two blocks), into a store of block-local pixel-major
+// rows that stays on the device.  Each block's rows are merged (events of one
+// filter frame summed in stream order, then / avg; masked pixels emptied) as
+// the whole-series merge does.  Finishing the series transposes the last,
+// partial block and gathers every pixel's segments in block order -- blocks
+// follow each other in time, so a row's segments concatenate in frame order --
+// into the series' event lists, which are then classified as usual.  The
+// result is the same event lists, bit for bit, as one transpose of every frame.
+
+namespace {
+
+// Block merge: one warp per 32 pixels; each lane merges its pixel's row of the
+// block in place (when the block's rows hold a repeated frame or avg > 1) and
+// records the row's start in the block and its merged length.
+__global__ void __launch_bounds__(256)
+k_merge_block(int32_t P, int32_t avg, const int64_t *__restrict__ row_ptr,
+              const uint8_t *__restrict__ mask, int32_t *__restrict__ fr,
+              float *__restrict__ val, int32_t *__restrict__ blk_off,
+              int32_t *__restrict__ blk_len) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p - (int)(threadIdx.x & 31) >= P) return;  // whole warp past the end
+  const bool has = p < P;
+  const int64_t b = has ? row_ptr[p] : 0;
+  const int32_t n = has ? (int32_t)(row_ptr[p + 1] - b) : 0;
+  int32_t out = 0;
+  if (has && mask[p]) {
+    bool dup = false;
+    for (int32_t i = 1; i < n && !dup; i++) dup = fr[b + i] == fr[b + i - 1];
+    if (dup || avg != 1) {
+      const float favg = (float)avg;
+      int32_t i = 0;
+      while (i < n) {
+        const int32_t f = fr[b + i];
+        float acc = 0.f;
+        do {
+          acc = __fadd_rn(acc, val[b + i]);
+          i++;
+        } while (i < n && fr[b + i] == f);
+        fr[b + out] = f;
+        val[b + out] = __fdiv_rn(acc, favg);
+        out++;
+      }
+    } else {
+      out = n;
+    }
+  }
+  if (has) {
+    blk_off[p] = (int32_t)b;
+    blk_len[p] = out;
+  }
+}
+
+// Merged row lengths of every block summed per pixel.
+__global__ void k_block_totals(int32_t P, int32_t nblk, const int32_t *__restrict__ blk_len,
+                               int32_t *__restrict__ tot) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  int32_t t = 0;
+  for (int32_t k = 0; k < nblk; k++) t += blk_len[(size_t)k * P + p];
+  tot[p] = t;
+}
+
+// Each pixel's block segments, in block order, copied to its row of the
+// series' event lists.
+__global__ void k_gather_blocks(int32_t P, int32_t nblk, const int64_t *__restrict__ blk_base,
+                                const int32_t *__restrict__ blk_off,
+                                const int32_t *__restrict__ blk_len,
+                                const int32_t *__restrict__ bfr, const float *__restrict__ bval,
+                                const int64_t *__restrict__ row_ptr, int32_t *__restrict__ fr,
+                                float *__restrict__ val) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  int64_t d = row_ptr[p];
+  for (int32_t k = 0; k < nblk; k++) {
+    const int32_t n = blk_len[(size_t)k * P + p];
+    const int64_t src = blk_base[k] + blk_off[(size_t)k * P + p];
+    for (int32_t i = 0; i < n; i++) {
+      fr[d + i] = bfr[src + i];
+      val[d + i] = bval[src + i];
+    }
+    d += n;
+  }
+}
+
+// Transposes the next block, ending at raw frame r1, into the block store.
+void transpose_block(Series &s, int32_t r1) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P, r0 = s.blk_raw_done;
+  const int64_t n = s.frame_off[r1] - s.frame_off[r0];
+  const int64_t base = s.blk_events;
+  s.blk_fr.grow((size_t)(base + std::max<int64_t>(n, 1)), (size_t)base, st);
+  s.blk_val.grow((size_t)(base + std::max<int64_t>(n, 1)), (size_t)base, st);
+  const size_t k = s.blk_base.size();
+  s.blk_off.grow((k + 1) * (size_t)P, k * (size_t)P, st);
+  s.blk_len.grow((k + 1) * (size_t)P, k * (size_t)P, st);
+  s.blk_rp.reserve((size_t)P + 1, st);
+  transpose_range(s, r0, r1, s.blk_fr.p + base, s.blk_val.p + base, s.blk_rp.p);
+  k_merge_block<<<(P + 255) / 256, 256, 0, st>>>(P, s.desc.avg_frames, s.blk_rp.p, s.d_mask.p,
+                                                  s.blk_fr.p + base, s.blk_val.p + base,
+                                                  s.blk_off.p + k * (size_t)P,
+                                                  s.blk_len.p + k * (size_t)P);
+  XG_CHECK_LAUNCH();
+  s.blk_base.push_back(base);
+  s.blk_events = base + n;
+  s.blk_raw_done = r1;
+}
+
+}  // namespace
+
+void transpose_ready_blocks(Series &s) {
+  if (s.block_frames <= 0) return;
+  const int32_t step = s.block_frames * s.R_in;
+  // raw frames past the series' last filter frame are never used
+  const int32_t limit = std::min<int64_t>(s.raw_frames, (int64_t)s.F * s.R_in);
+  if (s.blk_raw_done + step > limit) return;
+  s.stats.reserve(1, s.stream);
+  if (s.blk_base.empty())  // the first block of the series: a clean error word
+    XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), s.stream));
+  upload_frame_tables(s);
+  while (s.blk_raw_done + step <= limit) transpose_block(s, s.blk_raw_done + step);
+}
+
+void reset_blocks(Series &s) {
+  s.blk_base.clear();
+  s.blk_events = 0;
+  s.blk_raw_done = 0;
+}
+
+void run_filter_transpose(Series &s) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P;
+  reserve_lists(s);
+  const size_t nalloc = s.raw_events > 0 ? (size_t)s.raw_events : 1;
   s.ev_frame.reserve(nalloc, st);
   s.ev_val.reserve(nalloc, st);
-
-  if (s.frame_off_dirty) {
-    s.d_frame_off.reserve(s.frame_off.size(), st);
-    XG_CUDA(cudaMemcpyAsync(s.d_frame_off.p, s.frame_off.data(),
-                            sizeof(int64_t) * s.frame_off.size(), cudaMemcpyHostToDevice, st));
-    s.frame_map.resize(s.raw_frames);
-    for (int32_t r = 0; r < s.raw_frames; r++) {  // stride*avg raw frames per filter frame
-      const int32_t k = r / s.R_in;
-      s.frame_map[r] = (k < s.F && ((r - k * s.R_in) % s.desc.stride_frames) == 0) ? k : -1;
-    }
-    s.d_frame_map.reserve(s.frame_map.size() ? s.frame_map.size() : 1, st);
-    if (!s.frame_map.empty())
-      XG_CUDA(cudaMemcpyAsync(s.d_frame_map.p, s.frame_map.data(),
-                              sizeof(int32_t) * s.frame_map.size(), cudaMemcpyHostToDevice, st));
-    s.frame_off_dirty = false;
+  if (s.block_frames <= 0) {
+    XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
+    upload_frame_tables(s);
+    transpose_range(s, 0, s.raw_frames, s.ev_frame.p, s.ev_val.p, s.row_ptr.p);
+    merge_classify(s, s.desc.avg_frames);
+    return;
   }
-
-  if (n > 0) {
-    int nbits = 32 - __builtin_clz((unsigned)P);  // bits to hold P (the drop key)
-    int passes = (nbits + 7) / 8;
-    const int ipt = items_per_lane(n);
-    int ntiles = (int)((n + RS_THREADS * ipt - 1) / (RS_THREADS * ipt));
-    s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
-    s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);
-    size_t ws = scan_workspace_bytes((int64_t)RS_DIGITS * ntiles);
-    size_t ws2 = scan_workspace_bytes(P);
-    s.scan_tmp.reserve(ws > ws2 ? ws : ws2, st);
-    // sparse series below 65,536 filter frames carry one packed word per item
-    // (frame, raw value) through the passes instead of a frame and a value
-    const bool dense = s.desc.dense != 0;
-    const bool packed = !dense && s.F <= 65536;
-    // the last pass also writes the kept items' keys, for the row pointers
-    s.keyA.reserve(n, st);
-    if (passes > 1) {
-      s.keyB.reserve(n, st);
-      s.frA.reserve(n, st);
-      if (!packed) s.vA.reserve(n, st);
-    }
-    if (passes > 2) {
-      s.frB.reserve(n, st);
-      if (!packed) s.vB.reserve(n, st);
-    }
-    const int chunk = 32 * ipt;
-    const int64_t nch = (n + chunk - 1) / chunk;
-    s.d_chunk_frame.reserve((size_t)nch, st);
-    k_chunk_frames<<<(s.raw_frames + 255) / 256, 256, 0, st>>>(s.raw_frames, s.d_frame_off.p, nch,
-                                                              chunk, s.d_chunk_frame.p);
+  // the error word keeps what earlier block transposes found; the counters restart
+  if (s.blk_base.empty())
+    XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
+  else
+    XG_CUDA(cudaMemsetAsync(&s.stats.p->nfloat, 0,
+                            sizeof(DevStats) - offsetof(DevStats, nfloat), st));
+  upload_frame_tables(s);
+  if (s.blk_raw_done < s.raw_frames) transpose_block(s, s.raw_frames);  // the last block
+  const int32_t nblk = (int32_t)s.blk_base.size();
+  s.blk_tot.reserve(P, st);
+  s.d_blk_base.reserve((size_t)std::max(nblk, 1), st);
+  if (nblk > 0) {
+    XG_CUDA(cudaMemcpyAsync(s.d_blk_base.p, s.blk_base.data(), sizeof(int64_t) * nblk,
+                            cudaMemcpyHostToDevice, st));
+    k_block_totals<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.blk_len.p, s.blk_tot.p);
     XG_CHECK_LAUNCH();
-    RawCfg rc{s.raw_idx.p, dense ? nullptr : s.raw_val.p, dense ? s.raw_valf.p : nullptr,
-              s.d_frame_off.p, s.d_frame_map.p, s.d_chunk_frame.p, s.raw_frames, n, P, s.F,
-              s.R_in, s.desc.stride_frames, s.has_flat ? s.d_flat.p : nullptr, s.stats.p};
-    uint32_t *kbuf[2] = {s.keyA.p, s.keyB.p};
-    int32_t *fbuf[2] = {s.frA.p, s.frB.p};
-    float *vbuf[2] = {s.vA.p, s.vB.p};
-    for (int pass = 0; pass < passes; pass++) {
-      bool first = pass == 0, last = pass == passes - 1;
-      PassCfg pc{};
-      pc.n = n;
-      pc.shift = 8 * pass;
-      pc.ntiles = ntiles;
-      pc.sentinel = (uint32_t)P;
-      if (!first) {
-        pc.key_in = kbuf[(pass - 1) & 1];
-        pc.fr_in = fbuf[(pass - 1) & 1];
-        pc.v_in = vbuf[(pass - 1) & 1];
-      }
-      if (last) {
-        pc.key_out = kbuf[pass & 1];  // not the pass's input
-        pc.fr_out = s.ev_frame.p;
-        pc.v_out = s.ev_val.p;
-      } else {
-        pc.key_out = kbuf[pass & 1];
-        pc.fr_out = fbuf[pass & 1];
-        pc.v_out = vbuf[pass & 1];
-      }
-      if (ipt == 16)
-        radix_pass<16>(s, first, last, packed, ntiles, rc, pc);
-      else
-        radix_pass<8>(s, first, last, packed, ntiles, rc, pc);
-    }
-  } else {
-    s.scan_tmp.reserve(scan_workspace_bytes(P), st);
-  }
-  if (n > 0) {
-    const uint32_t *keys = s.keyA.p;  // written by the last pass
-    const int passes = (32 - __builtin_clz((unsigned)P) + 7) / 8;
-    if (passes % 2 == 0) keys = s.keyB.p;
-    k_row_ptr<<<(unsigned)(((int64_t)P + 1 + 255) / 256), 256, 0, st>>>(keys, n, s.stats.p, P,
-                                                                        s.row_ptr.p);
+    exclusive_scan_i32_i64(s.blk_tot.p, s.row_ptr.p, P, s.scan_tmp.p, st);
+    k_gather_blocks<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.d_blk_base.p, s.blk_off.p,
+                                                     s.blk_len.p, s.blk_fr.p, s.blk_val.p,
+                                                     s.row_ptr.p, s.ev_frame.p, s.ev_val.p);
     XG_CHECK_LAUNCH();
   } else {
     XG_CUDA(cudaMemsetAsync(s.row_ptr.p, 0, sizeof(int64_t) * ((size_t)P + 1), st));
   }
-  const int pix_per_block = 256;
-  k_merge_classify<<<(P + pix_per_block - 1) / pix_per_block, 256, 0, st>>>(
-      P, s.F, s.desc.avg_frames, s.thread_cap, s.desc.normalize_by_framesum, s.row_ptr.p, s.d_mask.p, s.ev_frame.p,
-      s.ev_val.p,
-      s.row_len.p, s.pclass.p, ClassLists{s.wlist.p, s.llist.p, s.flist.p}, s.pixels_sum.p,
-      s.stats.p);
-  XG_CHECK_LAUNCH();
+  // the rows are merged already: classify them (avg 1: nothing left to merge)
+  merge_classify(s, 1);
 }
 
 }  // namespace xg

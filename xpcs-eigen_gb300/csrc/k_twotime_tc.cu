@@ -475,6 +475,9 @@ void run_twotime_exact(Series &s, const TwoTimeReq &req, const TwoTimeLayout &la
         XG_CHECK_LAUNCH();
         XG_CUDA(cudaEventRecord(e1, st));
         o.gram_flop += (double)ntiles * 2.0 * TC_BM * TC_BN * (double)Kp;
+        // the Gram's own work: the F(F+1)/2 upper-triangle cells (diagonal
+        // included) over the group's nr rows, without tile and K padding
+        o.gram_flop_alg += 2.0 * (double)nr * ((double)F * (F + 1) / 2.0);
         if (single)
           k_tc_single<false><<<dim3((F + 255) / 256, F), 256, 0, st>>>(
               F, s.tt_Gf.p, Fp, sgdev, req.average, inv_npix, s.tt_Cq.p, Cout);

@@ -9,8 +9,13 @@
 //  - push() copies a frame into the acquisition's resident raw buffers on its
 //    own stream and returns; the copies of different acquisitions overlap
 //    with each other and with the compute of acquisitions that finished.
-//  - finish() enqueues filter/transpose, multi-tau and the float64
-//    normalisation on the acquisition's stream; it returns at once.
+//    Every SERVER_BLOCK_FRAMES frames, the block is filtered and transposed
+//    on that stream into pixel-major rows that stay resident in HBM
+//    (xpcs_series_set_block_frames), so the event lists are built while the
+//    acquisition runs.
+//  - finish() enqueues the transpose of the last, partial block, the join of
+//    the blocks' rows, multi-tau and the float64 normalisation on the
+//    acquisition's stream; it returns at once.
 //  - result() waits for that work and reads g2/stderr; release() frees the
 //    series, which admits waiting acquisitions.
 // Every push records its ingest latency (arrival in push() to the end of the
@@ -112,13 +117,18 @@ void CUDART_CB on_final(void *p) {
   delete r;
 }
 
-// Device footprint of an acquisition: raw events and the transpose/list
-// buffers (~46 B per event), per-pixel tables and G2/IP/IF (12 B per delay).
+// Filter frames per incremental transpose block (2.56 s at 200 Hz).
+constexpr int32_t SERVER_BLOCK_FRAMES = 512;
+
+// Device footprint of an acquisition: raw events, the resident block rows and
+// the transpose/list buffers (~54 B per event), per-pixel tables and G2/IP/IF
+// (12 B per delay), and every block's row offsets and lengths (8 B per pixel).
 uint64_t estimate_footprint(const xpcs_series_desc &d, int64_t events) {
   const uint64_t P = (uint64_t)d.width * d.height;
   const DelaySchedule ds = delay_schedule(d.frames, d.delays_per_level);
-  return P * (12ull * ds.level.size() + 64) + (uint64_t)std::max<int64_t>(events, 0) * 46 +
-         (64ull << 20);
+  const uint64_t blocks = (uint64_t)std::max(d.frames, 0) / SERVER_BLOCK_FRAMES + 1;
+  return P * (12ull * ds.level.size() + 64 + 8 * blocks) +
+         (uint64_t)std::max<int64_t>(events, 0) * 54 + (64ull << 20);
 }
 
 void check_rc(int rc) {
@@ -164,6 +174,7 @@ void activate(Server &srv, const std::shared_ptr<Slot> &sl) {
     d.flatfield = sl->flat.empty() ? nullptr : sl->flat.data();
     d.device = srv.device;
     check_rc(xpcs_series_create(&d, &sl->s));
+    check_rc(xpcs_series_set_block_frames(sl->s, SERVER_BLOCK_FRAMES));
     sl->state = Slot::ACTIVE;
     size_t e0 = 0;
     for (size_t f = 0; f < sl->pnnz.size(); f++) {

@@ -208,7 +208,8 @@ struct TwoTimeOut {
   std::vector<int32_t> qbins;  // processed q bins present in the mapping, in mapping order
   int32_t frames = 0, window = 1, partials = 0, sg_rows = 0, sg_cols = 0;
   float gram_ms = 0.f;      // EXACT: tensor-core Gram kernel time
-  double gram_flop = 0.0;
+  double gram_flop = 0.0;      // multiply-adds of the tiles computed (2 x M x N x K each)
+  double gram_flop_alg = 0.0;  // of the upper triangle alone (2 x rows x F(F+1)/2)
 };
 
 // --------------------------------------------------------------- a series
@@ -253,6 +254,17 @@ struct Series {
   DBuf<int32_t> frA, frB;
   DBuf<float> vA, vB;
   DBuf<uint32_t> hist, hist_scan;
+  // incremental transposes (block_frames > 0): block-local pixel-major rows
+  int32_t block_frames = 0;   // filter frames per block; 0: one transpose at xpcs_multitau
+  int32_t blk_raw_done = 0;   // raw frames already transposed into blocks
+  int64_t blk_events = 0;     // events in the block store
+  std::vector<int64_t> blk_base;  // first event of every block in the store
+  DBuf<int64_t> d_blk_base;
+  DBuf<int32_t> blk_fr;       // block store: filter frames
+  DBuf<float> blk_val;        // block store: values
+  DBuf<int32_t> blk_off, blk_len;  // [block][P]: row start in its block, merged length
+  DBuf<int64_t> blk_rp;       // row pointers of the block being transposed
+  DBuf<int32_t> blk_tot;      // merged events per pixel over every block
   DBuf<int64_t> row_ptr;    // [P+1]
   DBuf<int32_t> row_len;    // events per pixel after merging duplicates
   DBuf<uint8_t> pclass;
@@ -359,6 +371,9 @@ void exclusive_scan_i32_i64(const int32_t *in, int64_t *out, int64_t n, void *ws
 
 // Kernel launchers
 void run_filter_transpose(Series &s);                       // k_transpose.cu
+// Incremental transposes: every complete block of ingested frames (k_transpose.cu)
+void transpose_ready_blocks(Series &s);
+void reset_blocks(Series &s);
 void run_multitau(Series &s, int mode);                      // k_multitau.cu
 void run_normalize(Series &s, bool want64, bool want32);     // k_normalize.cu
 void build_norm_chunks(Series &s);                           // k_normalize.cu

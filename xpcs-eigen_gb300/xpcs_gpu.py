@@ -38,7 +38,7 @@ EXPORTS = [
     "xpcs_autotune", "xpcs_server_create", "xpcs_server_destroy", "xpcs_server_submit",
     "xpcs_server_push_sparse", "xpcs_server_finish", "xpcs_server_state", "xpcs_server_result",
     "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
-    "xpcs_set_device_memory_limit", "xpcs_get_device_memory",
+    "xpcs_set_device_memory_limit", "xpcs_get_device_memory", "xpcs_series_set_block_frames",
 ]
 
 BATCH_F64 = 1
@@ -59,7 +59,8 @@ class TwoTimeDesc(C.Structure):
 class TwoTimeInfo(C.Structure):
     _fields_ = [("qbins", C.c_int32), ("frames", C.c_int32), ("window", C.c_int32),
                 ("partials", C.c_int32), ("sg_rows", C.c_int32), ("sg_cols", C.c_int32),
-                ("gram_ms", C.c_float), ("gram_flop", C.c_double)]
+                ("gram_ms", C.c_float), ("gram_flop", C.c_double),
+                ("gram_flop_algorithmic", C.c_double)]
 
 
 class ServerStats(C.Structure):
@@ -163,6 +164,7 @@ def lib() -> C.CDLL:
                                              C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_set_device_memory_limit.argtypes = [C.c_int32, C.c_uint64]
+        L.xpcs_series_set_block_frames.argtypes = [C.c_void_p, C.c_int32]
         L.xpcs_get_device_memory.argtypes = [C.c_int32, C.POINTER(C.c_uint64),
                                              C.POINTER(C.c_uint64)]
         L.xpcs_pin_host.argtypes = [C.c_void_p, C.c_uint64]
@@ -241,6 +243,11 @@ class Series:
     def reset(self):
         check(lib().xpcs_series_reset(self._h))
 
+    def set_block_frames(self, block_frames: int):
+        """Transpose frames in blocks of this many filter frames as they are
+        ingested (xpcs_series_set_block_frames); 0 = all at multitau()."""
+        check(lib().xpcs_series_set_block_frames(self._h, int(block_frames)))
+
     def ingest_sparse(self, nnz, idx, val):
         nnz = np.ascontiguousarray(nnz, np.uint32)
         idx = np.ascontiguousarray(idx, np.int32)
@@ -317,7 +324,8 @@ class Series:
         info = TwoTimeInfo()
         check(lib().xpcs_twotime(self._h, C.byref(d), mode, C.byref(info)))
         if not fetch:
-            return dict(gram_ms=info.gram_ms, gram_flop=info.gram_flop, qbins=info.qbins,
+            return dict(gram_ms=info.gram_ms, gram_flop=info.gram_flop,
+                        gram_flop_algorithmic=info.gram_flop_algorithmic, qbins=info.qbins,
                         frames=info.frames)
         Q, F = info.qbins, info.frames
         qs = np.empty(Q, np.int32)
@@ -329,7 +337,8 @@ class Series:
                                      _ptr(part)))
         return dict(qbins=qs, sg=sg, c2t={int(k): c2t[i] for i, k in enumerate(qs)},
                     g2full=full, g2partials=part, gram_ms=info.gram_ms,
-                    gram_flop=info.gram_flop)
+                    gram_flop=info.gram_flop,
+                    gram_flop_algorithmic=info.gram_flop_algorithmic)
 
     def autotune(self, mode=MODE_REFERENCE) -> int:
         """xpcs_autotune: pick this series' thread-kernel row capacity; returns it."""
