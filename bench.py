@@ -287,6 +287,15 @@ def run_batch(args, dev):
     for _ in range(args.batch_reps):
         plain()
     t_plain = (time.perf_counter() - t0) / args.batch_reps
+    # per-series device time of the plain path (one more pass, each series waited for)
+    per = []
+    for a, s_ in zip(mix, series):
+        s_.multitau(xg.MODE_REFERENCE)
+        s_.normalize(out=(np.empty((s_.D, s_.nq)), np.empty((s_.D, s_.nq)), None, None))
+        st = s_.stage_times()
+        per.append({"side": a.width, "frames": a.frames, "events": int(s_.info().raw_events),
+                    "filter_ms": st["filter_ms"], "multitau_ms": st["multitau_ms"],
+                    "normalize_ms": st["normalize_ms"], "step_ms": st["step_ms"]})
     b = xg.Batch(series)
     b.run(xg.MODE_REFERENCE, f64=True, autotune=True)  # tunes the chain count, captures
     t0 = time.perf_counter()
@@ -296,6 +305,7 @@ def run_batch(args, dev):
         dev_ms.append(b.stats()[0])
     t_batch = (time.perf_counter() - t0) / args.batch_reps
     _, kernels, lanes = b.stats()
+    start, end = b.timeline()
     # the batch's results are those of the plain run
     same = all(np.array_equal(s.normalized(f64=True)[0], o[0], equal_nan=True)
                for s, o in zip(series, outs))
@@ -303,6 +313,15 @@ def run_batch(args, dev):
     for s in series:
         s.close()
     n = len(mix)
+    busy = float(np.sum(end - start))
+    makespan = float(np.max(end)) if n else 0.0
+    order = np.argsort([-p["step_ms"] for p in per])
+    plain_dev = float(sum(p["step_ms"] for p in per))
+    top4 = float(sum(per[i]["step_ms"] for i in order[:4]))
+    timeline = [{"series": int(i), "side": per[i]["side"], "frames": per[i]["frames"],
+                 "events": per[i]["events"], "plain_step_ms": per[i]["step_ms"],
+                 "batch_start_ms": float(start[i]), "batch_end_ms": float(end[i])}
+                for i in range(n)]
     return {"workload": BATCH_DESC, "series": n, "raw_events": int(events),
             "pixel_frames": int(sum(a.width * a.height * a.frames for a in mix)),
             "plain_ms": t_plain * 1e3, "batched_ms": t_batch * 1e3,
@@ -311,7 +330,14 @@ def run_batch(args, dev):
             "batched_over_plain": t_plain / t_batch, "kernels_in_graph": int(kernels),
             "concurrent_chains": int(lanes),
             "thread_caps": {str(c): caps.count(c) for c in sorted(set(caps))},
-            "identical_results": bool(same), "reps": args.batch_reps}
+            "identical_results": bool(same), "reps": args.batch_reps,
+            "plain_device_ms_sum": plain_dev,
+            "plain_device_ms_largest_4": top4,
+            "plain_stage_ms_sum": {k: float(sum(p[k] for p in per))
+                                   for k in ("filter_ms", "multitau_ms", "normalize_ms")},
+            "batch_timeline": {"makespan_ms": makespan, "series_busy_ms_sum": busy,
+                               "mean_series_in_flight": busy / makespan if makespan else None,
+                               "per_series": timeline}}
 
 
 def run_serving(args, dev):

@@ -363,6 +363,11 @@ int xpcs_batch_run(xpcs_batch *b, int32_t mode, uint32_t flags);
  * number of kernels in the graph and the number of concurrent chains of
  * series in it (any pointer may be NULL). */
 int xpcs_batch_stats(xpcs_batch *b, float *ms, int64_t *kernels, int32_t *lanes);
+/* Occupancy timeline of the last run: for each member (in creation order),
+ * when its work started and ended, in ms from the start of the graph (the
+ * device's global timer, stamped by one-thread kernels in the graph around
+ * each member's work).  Either pointer may be NULL. */
+int xpcs_batch_timeline(xpcs_batch *b, float *start_ms, float *end_ms);
 void xpcs_batch_destroy(xpcs_batch *b);
 
 /* Serving (no reference counterpart): several acquisitions streamed at once.

@@ -156,3 +156,22 @@ def test_framesum_series_cannot_join_a_batch():
     finally:
         s.close()
         fs.close()
+
+
+def test_batch_timeline_covers_every_member():
+    data = [synth_member(i, *m) for i, m in enumerate(MIX)]
+    series = [open_member(*d) for d in data]
+    try:
+        b = xg.Batch(series)
+        with pytest.raises(xg.XpcsError):
+            b.timeline()  # not run yet
+        b.run(xg.MODE_REFERENCE, f64=True)
+        start, end = b.timeline()
+        ms = b.stats()[0]
+        assert start.shape == (len(series),) and np.all(start >= 0) and np.all(end > start)
+        # every member's work lies inside the graph's run (timer resolution slack)
+        assert float(np.max(end)) <= ms + 0.05
+        b.close()
+    finally:
+        for s in series:
+            s.close()

@@ -616,6 +616,18 @@ int xpcs_batch_stats(xpcs_batch *h, float *ms, int64_t *kernels, int32_t *lanes)
   });
 }
 
+int xpcs_batch_timeline(xpcs_batch *h, float *start_ms, float *end_ms) {
+  return guarded([&] {
+    need(h, "null batch");
+    Batch &b = *(Batch *)h;
+    if (b.start_ms.size() != b.ss.size()) throw Error(XPCS_ERR_STATE, "the batch has not run");
+    for (size_t i = 0; i < b.ss.size(); i++) {
+      if (start_ms) start_ms[i] = b.start_ms[i];
+      if (end_ms) end_ms[i] = b.end_ms[i];
+    }
+  });
+}
+
 void xpcs_batch_destroy(xpcs_batch *h) {
   if (!h) return;
   Batch *b = (Batch *)h;

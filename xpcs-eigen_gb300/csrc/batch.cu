@@ -28,6 +28,10 @@ Batch::~Batch() {
   if (exec) cudaGraphExecDestroy(exec);
   for (cudaEvent_t e : join)
     if (e) cudaEventDestroy(e);
+  if (origin) {
+    stamps.release(origin);
+    cudaStreamSynchronize(origin);
+  }
   if (fork) cudaEventDestroy(fork);
   if (t0) cudaEventDestroy(t0);
   if (t1) cudaEventDestroy(t1);
@@ -60,6 +64,7 @@ Batch *batch_create(Series *const *ss, int32_t n) {
     XG_CUDA(cudaEventCreate(&b->t1));
     b->join.assign(n, nullptr);
     for (auto &e : b->join) XG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->stamps.reserve(2 * (size_t)n + 1, b->origin);
   } catch (...) {
     delete b;
     throw;
@@ -116,6 +121,13 @@ int32_t autotune(Series &s, int mode) {
 
 namespace {
 
+// The device's global nanosecond timer, for the batch's occupancy timeline.
+__global__ void k_stamp(unsigned long long *dst) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  *dst = t;
+}
+
 void series_pass(Series &s, int mode, uint32_t flags) {
   run_filter_transpose(s);
   run_multitau(s, mode);
@@ -150,12 +162,18 @@ void build_graph(Batch &b, int mode, uint32_t flags, int lanes) {
   cudaGraph_t g = nullptr;
   const int64_t l0 = tl_launches;
   try {
+    k_stamp<<<1, 1, 0, b.origin>>>(b.stamps.p + 2 * n);
+    XG_CHECK_LAUNCH();
     XG_CUDA(cudaEventRecord(b.fork, b.origin));
     for (int i : order) {
       const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
       Series &s = *b.ss[i];
       XG_CUDA(cudaStreamWaitEvent(s.stream, last[c] < 0 ? b.fork : b.join[last[c]], 0));
+      k_stamp<<<1, 1, 0, s.stream>>>(b.stamps.p + 2 * i);
+      XG_CHECK_LAUNCH();
       series_pass(s, mode, flags);
+      k_stamp<<<1, 1, 0, s.stream>>>(b.stamps.p + 2 * i + 1);
+      XG_CHECK_LAUNCH();
       XG_CUDA(cudaEventRecord(b.join[i], s.stream));
       load[c] += s.raw_events + s.P;
       last[c] = i;
@@ -186,6 +204,17 @@ float launch(Batch &b) {
   XG_CUDA(cudaStreamSynchronize(b.origin));
   float ms = 0.f;
   XG_CUDA(cudaEventElapsedTime(&ms, b.t0, b.t1));
+  // each member's work in this run, from the fork (the occupancy timeline)
+  const size_t n = b.ss.size();
+  std::vector<unsigned long long> t(2 * n + 1);
+  XG_CUDA(cudaMemcpy(t.data(), b.stamps.p, sizeof(unsigned long long) * t.size(),
+                     cudaMemcpyDeviceToHost));
+  b.start_ms.assign(n, 0.f);
+  b.end_ms.assign(n, 0.f);
+  for (size_t i = 0; i < n; i++) {
+    b.start_ms[i] = (float)((double)(long long)(t[2 * i] - t[2 * n]) * 1e-6);
+    b.end_ms[i] = (float)((double)(long long)(t[2 * i + 1] - t[2 * n]) * 1e-6);
+  }
   return ms;
 }
 

@@ -335,6 +335,8 @@ struct Batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
   std::vector<cudaEvent_t> join;
+  DBuf<unsigned long long> stamps; // %globaltimer at each member's start and end, then the fork
+  std::vector<float> start_ms, end_ms;  // of the last run, from the graph's fork
   std::vector<int64_t> gens;       // member generations at capture
   int mode = -1;
   uint32_t flags = 0;

@@ -39,6 +39,7 @@ EXPORTS = [
     "xpcs_server_push_sparse", "xpcs_server_finish", "xpcs_server_state", "xpcs_server_result",
     "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
     "xpcs_set_device_memory_limit", "xpcs_get_device_memory", "xpcs_series_set_block_frames",
+    "xpcs_batch_timeline",
 ]
 
 BATCH_F64 = 1
@@ -165,6 +166,7 @@ def lib() -> C.CDLL:
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_set_device_memory_limit.argtypes = [C.c_int32, C.c_uint64]
         L.xpcs_series_set_block_frames.argtypes = [C.c_void_p, C.c_int32]
+        L.xpcs_batch_timeline.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_get_device_memory.argtypes = [C.c_int32, C.POINTER(C.c_uint64),
                                              C.POINTER(C.c_uint64)]
         L.xpcs_pin_host.argtypes = [C.c_void_p, C.c_uint64]
@@ -386,6 +388,13 @@ class Batch:
         lanes = C.c_int32(0)
         check(lib().xpcs_batch_stats(self._h, C.byref(ms), C.byref(k), C.byref(lanes)))
         return ms.value, k.value, lanes.value
+
+    def timeline(self):
+        """(start_ms, end_ms) of every member's work in the last run, from the launch."""
+        a = np.zeros(len(self.series), np.float32)
+        b = np.zeros(len(self.series), np.float32)
+        check(lib().xpcs_batch_timeline(self._h, _ptr(a), _ptr(b)))
+        return a, b
 
     def close(self):
         if getattr(self, "_h", None):
