@@ -44,10 +44,11 @@ WORKLOAD_DESC = ("1024x1024 detector, 10000 sparse IMM frames (uint16 counts), P
 
 
 def workload_desc(acq) -> str:
-    if (acq.width, acq.height, acq.frames) == (1024, 1024, 10000):
+    if (acq.width, acq.height, acq.frames, acq.mean) == (1024, 1024, 10000, 0.005):
         return WORKLOAD_DESC
-    return (f"{acq.width}x{acq.height} detector, {acq.frames} sparse IMM frames, otherwise as the "
-            "1024x1024 10000-frame series (a reduced case for profiling)")
+    return (f"{acq.width}x{acq.height} detector, {acq.frames} sparse IMM frames, mean "
+            f"{acq.mean:g} photons/pixel/frame, otherwise as the 1024x1024 10000-frame series "
+            "(a reduced case for profiling)")
 
 
 def bench_config(acq, delays: int, qbins: int, raw_events: int, world: int) -> dict:
@@ -149,12 +150,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_series_data(name=WORKLOAD, width=None, frames=None):
+def make_series_data(name=WORKLOAD, width=None, frames=None, mean=None):
     over = {}
     if width:
         over.update(width=width, height=width)
     if frames:
         over["frames"] = frames
+    if mean:
+        over["mean"] = mean
     acq = xs.preset(name, **over)
     dq, sq, _, _ = xs.maps(acq)
     nnz, idx, val = xs.sparse_frames(acq)
@@ -199,7 +202,7 @@ def run_reference_arm(args, dist):
         return
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
-    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames)
+    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames, mean=args.mean)
     qm = oracle.QMap(dq, sq)
     lv, _ = oracle.delays(acq.frames, acq.dpl)
     for _ in range(args.warmup):
@@ -580,7 +583,7 @@ def run_gpu_arm(args, dist):
     import xpcs_gpu as xg
 
     dev = dist.local
-    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames)
+    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames, mean=args.mean)
     F, P = acq.frames, acq.width * acq.height
     xg.pin(idx)
     xg.pin(val)
@@ -757,6 +760,8 @@ def main():
                     help="square detector side (reduced case for profiling; default 1024)")
     ap.add_argument("--frames", type=int, default=None,
                     help="frames in the series (reduced case for profiling; default 10000)")
+    ap.add_argument("--mean", type=float, default=None,
+                    help="photons per pixel per frame (profiling case; default 0.005)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     dist = Dist()

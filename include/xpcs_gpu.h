@@ -207,12 +207,32 @@ int xpcs_side_stats(xpcs_series *s, float *pixel_sum, float *frame_sum,
 int xpcs_get_normalized(xpcs_series *s, double *g2, double *stderr_, float *g2_f32,
                         float *stderr_f32);
 
+/* Kernel knobs of a series (no reference counterpart).  Results do not
+ * depend on them; only the time does.
+ *  thread_cap            warps per pixel: rows of up to this many events run
+ *                        one thread per pixel (32, 48, 64, 80 or 112; the
+ *                        default is 80), longer rows one warp per pixel;
+ *  scratch_extra         the level-fold schedule: extra scratch words per
+ *                        thread (0 or 8 beyond the delays of a level and the
+ *                        levels); levels of at most 32 x words bins take the
+ *                        bitmask pair search;
+ *  radix_items_per_lane  the transpose's event tile: 8 or 16 items per lane
+ *                        (tiles of 2,048 or 4,096 events; 0 chooses by series
+ *                        size). */
+typedef struct {
+  int32_t thread_cap;
+  int32_t scratch_extra;
+  int32_t radix_items_per_lane;
+} xpcs_tuning;
+int xpcs_series_get_tuning(xpcs_series *s, xpcs_tuning *t);
+int xpcs_series_set_tuning(xpcs_series *s, const xpcs_tuning *t);
+
 /* Autotuner (no reference counterpart).  Times the filter and multi-tau
- * passes of the ingested frames with each row capacity of the
- * thread-per-pixel kernel (32, 48, 64, 80, 112 events; longer rows go to the
- * warp-per-pixel kernel) and keeps the fastest for this series.  Results do
- * not depend on the choice; only the time does.  The default without tuning
- * is 80.  *thread_cap (may be NULL) receives the choice. */
+ * passes of the ingested frames over the knobs above, one knob at a time
+ * (thread_cap, then scratch_extra, then radix_items_per_lane), keeping the
+ * fastest value of each, and sets them on the series.  *thread_cap (may be
+ * NULL) receives the chosen row capacity; xpcs_series_get_tuning gives all
+ * three. */
 int xpcs_autotune(xpcs_series *s, int32_t mode, int32_t *thread_cap);
 
 /* Waits for the handle's stream; reports deferred device errors. */

@@ -175,3 +175,30 @@ def test_batch_timeline_covers_every_member():
     finally:
         for s in series:
             s.close()
+
+
+@pytest.mark.parametrize("mode", [xg.MODE_REFERENCE, xg.MODE_EXACT])
+def test_every_knob_setting_gives_the_same_bits(mode):
+    """Row capacity (warps per pixel), scratch words (level-fold schedule) and
+    transpose tile change the work, never the results; bad values are refused."""
+    members = [synth_member(i, *m) for i, m in enumerate(MIX[:3])]
+    for acq, dq, sq, frames in members:
+        s = open_member(acq, dq, sq, frames)
+        try:
+            ref = alone(s, mode)
+            for cap, extra, ipt in ((32, 0, 8), (48, 8, 16), (64, 8, 0), (112, 0, 16),
+                                    (80, 8, 8)):
+                s.set_tuning(cap, extra, ipt)
+                assert s.tuning() == {"thread_cap": cap, "scratch_extra": extra,
+                                      "radix_items_per_lane": ipt}
+                assert_same(alone(s, mode), ref)
+            s.autotune(mode)
+            t = s.tuning()
+            assert t["thread_cap"] in (32, 48, 64, 80, 112) and t["scratch_extra"] in (0, 8)
+            assert t["radix_items_per_lane"] in (8, 16)
+            assert_same(alone(s, mode), ref)
+            for bad in ((40, 0, 0), (80, 4, 0), (80, 0, 12)):
+                with pytest.raises(xg.XpcsError):
+                    s.set_tuning(*bad)
+        finally:
+            s.close()

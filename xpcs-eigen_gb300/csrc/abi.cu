@@ -585,6 +585,38 @@ int xpcs_autotune(xpcs_series *h, int32_t mode, int32_t *thread_cap) {
   });
 }
 
+int xpcs_series_get_tuning(xpcs_series *h, xpcs_tuning *t) {
+  return guarded([&] {
+    need(h && t, "null argument");
+    Series &s = *(Series *)h;
+    t->thread_cap = s.thread_cap;
+    t->scratch_extra = s.scr_extra;
+    t->radix_items_per_lane = s.radix_ipt;
+  });
+}
+
+int xpcs_series_set_tuning(xpcs_series *h, const xpcs_tuning *t) {
+  return guarded([&] {
+    need(h && t, "null argument");
+    bool cap_ok = false;
+    for (int c : MT_THREAD_CAPS) cap_ok = cap_ok || c == t->thread_cap;
+    need(cap_ok, "thread_cap must be 32, 48, 64, 80 or 112");
+    need(t->scratch_extra == 0 || t->scratch_extra == 8, "scratch_extra must be 0 or 8");
+    need(t->radix_items_per_lane == 0 || t->radix_items_per_lane == 8 ||
+             t->radix_items_per_lane == 16,
+         "radix_items_per_lane must be 0, 8 or 16");
+    Series &s = *(Series *)h;
+    DeviceGuard g(s.device);
+    XG_CUDA(cudaStreamSynchronize(s.stream));
+    s.thread_cap = t->thread_cap;
+    s.scr_extra = t->scratch_extra;
+    s.radix_ipt = t->radix_items_per_lane;
+    s.have_multitau = false;
+    s.have_norm64 = s.have_norm32 = false;
+    s.generation++;
+  });
+}
+
 int xpcs_batch_create(xpcs_series *const *series, int32_t count, xpcs_batch **out) {
   return guarded([&] {
     need(series && out && count > 0, "bad batch arguments");

@@ -20,6 +20,8 @@
 #include <algorithm>
 #include <numeric>
 
+#include <initializer_list>
+
 #include "xpcs_internal.h"
 
 namespace xg {
@@ -72,51 +74,75 @@ Batch *batch_create(Series *const *ss, int32_t n) {
   return b;
 }
 
-// Times filter + multi-tau of the series' frames with every thread-kernel row
-// capacity (after one untimed pass that sizes the buffers) and keeps the
-// fastest.  A change of capacity changes the pixel classification, so it
-// counts as a change of the series for captured batch graphs.
+// Autotuner: times filter + multi-tau of the series' frames (one untimed pass
+// sizes the buffers, the second pass of each candidate is timed) over the
+// kernel knobs, one knob at a time, keeping the fastest value of each before
+// moving to the next:
+//   1. warps per pixel: the row capacity of the thread-per-pixel kernel (a
+//      thread per pixel up to CAP events, a warp per pixel above it);
+//   2. the level-fold schedule: scratch words per lane of the thread kernel,
+//      which decide up to which level (32 x words bins) the pair search runs
+//      on the occupancy bitmask instead of the sparse two-candidate checks;
+//   3. the event tile of the transpose: 8 or 16 items per lane (tiles of
+//      2,048 or 4,096 events).
+// A change of any knob changes the work (pixel classes, kernel launch), so it
+// counts as a change of the series for captured batch graphs.  Results do not
+// depend on the knobs.
 int32_t autotune(Series &s, int mode) {
   cudaStream_t st = s.stream;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   XG_CUDA(cudaEventCreate(&e0));
   XG_CUDA(cudaEventCreate(&e1));
-  const int32_t before = s.thread_cap;
-  int32_t best = before;
-  float best_ms = 0.f;
-  try {
-    run_filter_transpose(s);
-    run_multitau(s, mode);
-    for (int k = 0; k < MT_THREAD_NCAPS; k++) {
-      s.thread_cap = MT_THREAD_CAPS[k];
-      float ms = 0.f;
-      for (int rep = 0; rep < 2; rep++) {  // the second pass is timed
-        XG_CUDA(cudaEventRecord(e0, st));
-        run_filter_transpose(s);
-        run_multitau(s, mode);
-        XG_CUDA(cudaEventRecord(e1, st));
-        XG_CUDA(cudaEventSynchronize(e1));
-        XG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      }
-      if (k == 0 || ms < best_ms) {
+  const int32_t cap0 = s.thread_cap, scr0 = s.scr_extra, ipt0 = s.radix_ipt;
+  auto time_pass = [&]() {
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; rep++) {  // the second pass is timed
+      XG_CUDA(cudaEventRecord(e0, st));
+      run_filter_transpose(s);
+      run_multitau(s, mode);
+      XG_CUDA(cudaEventRecord(e1, st));
+      XG_CUDA(cudaEventSynchronize(e1));
+      XG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    return ms;
+  };
+  // one knob: try each value, keep the fastest
+  auto search = [&](int32_t &knob, std::initializer_list<int32_t> values) {
+    int32_t best = knob;
+    float best_ms = 0.f;
+    bool first = true;
+    for (int32_t v : values) {
+      knob = v;
+      const float ms = time_pass();
+      if (first || ms < best_ms) {
         best_ms = ms;
-        best = s.thread_cap;
+        best = v;
+        first = false;
       }
     }
+    knob = best;
+  };
+  try {
+    s.scr_extra = 0;
+    s.radix_ipt = 0;
+    search(s.thread_cap, {32, 48, 64, 80, 112});
+    search(s.scr_extra, {0, 8});
+    search(s.radix_ipt, {8, 16});
   } catch (...) {
-    s.thread_cap = before;
+    s.thread_cap = cap0;
+    s.scr_extra = scr0;
+    s.radix_ipt = ipt0;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     throw;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  s.thread_cap = best;
   s.tuned = true;
   s.have_multitau = false;
   s.have_norm64 = s.have_norm32 = false;
   s.generation++;
-  return best;
+  return s.thread_cap;
 }
 
 namespace {

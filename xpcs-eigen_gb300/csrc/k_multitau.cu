@@ -174,7 +174,7 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
   const int D = pl->D;
   const McArrays ar = mc_arrays(plan_g, D);
   const int P = pl->P, nlev = pl->nlev, mode = pl->mode;
-  const int scr = max(pl->acc, nlev);
+  const int scr = pl->scr;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t *wbase = (uint32_t *)smem + (size_t)warp * (CAP + scr) * 32;
   uint32_t *row = wbase + lane;
@@ -938,6 +938,7 @@ std::vector<uint8_t> make_plan(const Series &s, int mode) {
   }
   pl->nlev = nlev;
   pl->acc = acc;
+  pl->scr = std::max(acc, nlev) + std::max(0, s.scr_extra);
   for (int k = 1; k < D; k++)
     if (t_ip[k] >= t_ip[k - 1] || tau_abs[k] <= tau_abs[k - 1])
       throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay thresholds are not monotone");
@@ -997,11 +998,12 @@ void run_multitau(Series &s, int mode) {
   // once per mode (a captured batch graph must not copy from host memory)
   std::vector<uint8_t> plan = make_plan(s, mode);
   const McPlan *hp = (const McPlan *)plan.data();
-  if (s.plan_mode != mode) {
+  if (s.plan_mode != mode || s.plan_scr != hp->scr) {
     s.plan.reserve(plan.size(), st);
     XG_CUDA(cudaMemcpyAsync(s.plan.p, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
     XG_CUDA(cudaStreamSynchronize(st));
     s.plan_mode = mode;
+    s.plan_scr = hp->scr;
   }
   const size_t nD = (size_t)D * P;
   s.G2.reserve(nD ? nD : 1, st);
@@ -1010,7 +1012,8 @@ void run_multitau(Series &s, int mode) {
   if (D == 0 || P == 0) return;
   const int scr = std::max(hp->acc, hp->nlev);
   const ThreadKernel ktt = thread_kernel(s.thread_cap);
-  const size_t smt = thread_smem(scr, s.thread_cap), smw = warp_smem(D, scr, MT_WARP_CAP, WP_WARPS);
+  const size_t smt = thread_smem(hp->scr, s.thread_cap),
+               smw = warp_smem(D, scr, MT_WARP_CAP, WP_WARPS);
   const size_t smm = warp_smem(D, scr, MT_MID_CAP, MID_WARPS);
   const size_t sml = warp_smem(D, scr, MT_LONG_CAP, LONG_WARPS);
   if (smt > 227 * 1024 || smw > 227 * 1024 || smm > 227 * 1024 || sml > 227 * 1024)

@@ -657,7 +657,7 @@ void transpose_range(Series &s, int32_t r0, int32_t r1, int32_t *ev_fr, float *e
   XG_CUDA(cudaMemsetAsync(&s.stats.p->dropped, 0, sizeof(unsigned long long), st));
   const int nbits = 32 - __builtin_clz((unsigned)P);  // bits to hold P (the drop key)
   const int passes = (nbits + 7) / 8;
-  const int ipt = items_per_lane(n);
+  const int ipt = s.radix_ipt == 8 || s.radix_ipt == 16 ? s.radix_ipt : items_per_lane(n);
   const int ntiles = (int)((n + RS_THREADS * ipt - 1) / (RS_THREADS * ipt));
   s.hist.reserve((size_t)RS_DIGITS * ntiles, st);
   s.hist_scan.reserve((size_t)RS_DIGITS * ntiles, st);

@@ -162,6 +162,7 @@ int na_build_plan(int32_t P, int32_t F, int32_t dpl, int32_t mode, uint8_t *buf,
   }
   pl->nlev = nlev;
   pl->acc = 1;
+  pl->scr = nlev > 1 ? nlev : 1;
   return D;
 }
 

@@ -127,6 +127,8 @@ struct McLevel {
 // Kernel-side description of a multi-tau run; lives in device memory.
 struct McPlan {
   int32_t P, D, F, nlev, mode, acc;
+  int32_t scr;  // scratch words per lane of the thread-per-pixel kernel (>= acc, nlev): levels of
+                // at most 32 * scr bins take the bitmask pair search (the level-fold schedule)
   McLevel lv[MAX_LEVELS];
   // followed in device memory by the per-delay arrays (McArrays)
 };
@@ -288,7 +290,10 @@ struct Series {
   DBuf<uint8_t> plan;       // McPlan + tau_lvl[D] + denom[D]
   int32_t plan_mode = -1;   // mode of the plan in `plan` (-1: none uploaded)
   int32_t thread_cap = MT_THREAD_CAP_DEFAULT;  // rows up to this length: thread per pixel
-  bool tuned = false;       // thread_cap chosen by xpcs_autotune
+  int32_t scr_extra = 0;    // scratch words beyond max(delays of a level, levels)
+  int32_t radix_ipt = 0;    // transpose items per lane (event tile / 256); 0: by series size
+  int32_t plan_scr = -1;    // scratch words of the uploaded plan
+  bool tuned = false;       // thread_cap, scr_extra, radix_ipt chosen by xpcs_autotune
   DBuf<float> G2, IP, IF;
   bool have_multitau = false;
   bool have_norm64 = false, have_norm32 = false;

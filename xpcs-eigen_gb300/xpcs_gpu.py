@@ -39,7 +39,7 @@ EXPORTS = [
     "xpcs_server_push_sparse", "xpcs_server_finish", "xpcs_server_state", "xpcs_server_result",
     "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
     "xpcs_set_device_memory_limit", "xpcs_get_device_memory", "xpcs_series_set_block_frames",
-    "xpcs_batch_timeline",
+    "xpcs_batch_timeline", "xpcs_series_get_tuning", "xpcs_series_set_tuning",
 ]
 
 BATCH_F64 = 1
@@ -82,6 +82,11 @@ class XpcsError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"xpcs {STATUS.get(code, code)}: {msg}")
         self.code = code
+
+
+class Tuning(C.Structure):
+    _fields_ = [("thread_cap", C.c_int32), ("scratch_extra", C.c_int32),
+                ("radix_items_per_lane", C.c_int32)]
 
 
 class SeriesDesc(C.Structure):
@@ -167,6 +172,8 @@ def lib() -> C.CDLL:
         L.xpcs_set_device_memory_limit.argtypes = [C.c_int32, C.c_uint64]
         L.xpcs_series_set_block_frames.argtypes = [C.c_void_p, C.c_int32]
         L.xpcs_batch_timeline.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.xpcs_series_get_tuning.argtypes = [C.c_void_p, C.POINTER(Tuning)]
+        L.xpcs_series_set_tuning.argtypes = [C.c_void_p, C.POINTER(Tuning)]
         L.xpcs_get_device_memory.argtypes = [C.c_int32, C.POINTER(C.c_uint64),
                                              C.POINTER(C.c_uint64)]
         L.xpcs_pin_host.argtypes = [C.c_void_p, C.c_uint64]
@@ -244,6 +251,16 @@ class Series:
 
     def reset(self):
         check(lib().xpcs_series_reset(self._h))
+
+    def tuning(self) -> dict:
+        """The series' kernel knobs (xpcs_series_get_tuning)."""
+        t = Tuning()
+        check(lib().xpcs_series_get_tuning(self._h, C.byref(t)))
+        return {n: getattr(t, n) for n, _ in Tuning._fields_}
+
+    def set_tuning(self, thread_cap=80, scratch_extra=0, radix_items_per_lane=0):
+        t = Tuning(thread_cap, scratch_extra, radix_items_per_lane)
+        check(lib().xpcs_series_set_tuning(self._h, C.byref(t)))
 
     def set_block_frames(self, block_frames: int):
         """Transpose frames in blocks of this many filter frames as they are
@@ -343,7 +360,9 @@ class Series:
                     gram_flop_algorithmic=info.gram_flop_algorithmic)
 
     def autotune(self, mode=MODE_REFERENCE) -> int:
-        """xpcs_autotune: pick this series' thread-kernel row capacity; returns it."""
+        """xpcs_autotune: search this series' kernel knobs (row capacity of the
+        thread kernel, scratch words, transpose tile); returns the row capacity
+        (tuning() gives all three)."""
         c = C.c_int32(0)
         check(lib().xpcs_autotune(self._h, mode, C.byref(c)))
         return c.value
