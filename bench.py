@@ -262,8 +262,10 @@ def run_batch(args, dev):
     """Batched vs plain per-series throughput on the 64-series mix: the same
     series, resident in HBM, run one after another through the per-series
     calls (xpcs_multitau + xpcs_normalize, each waited for) and as one batch
-    graph (xpcs_batch_run).  Every series is autotuned first (xpcs_autotune),
-    and both forms run once untimed to size their buffers."""
+    graph (xpcs_batch_run, autotuned: members' knobs, the graph's form -- work
+    queue or chains -- and its chain count).  Every series is autotuned first
+    (xpcs_autotune), and both paths run once untimed to size their buffers.
+    The batch form the autotuner did not keep is timed too."""
     import xpcs_gpu as xg
 
     mix = batch_mix(args.batch_series)
@@ -309,6 +311,19 @@ def run_batch(args, dev):
     t_batch = (time.perf_counter() - t0) / args.batch_reps
     _, kernels, lanes = b.stats()
     start, end = b.timeline()
+    queue, _ = b.form()
+    # the other form, its chain count tuned, for comparison
+    b.set_form(not queue)
+    b.run(xg.MODE_REFERENCE, f64=True, autotune=True)
+    other_ms = []
+    for _ in range(args.batch_reps):
+        b.run(xg.MODE_REFERENCE, f64=True, autotune=True)
+        other_ms.append(b.stats()[0])
+    other_chains = b.form()[1]
+    forms = {("work_queue" if queue else "chains"):
+             {"device_ms": statistics.median(dev_ms), "chains": int(lanes)},
+             ("chains" if queue else "work_queue"):
+             {"device_ms": statistics.median(other_ms), "chains": int(other_chains)}}
     # the batch's results are those of the plain run
     same = all(np.array_equal(s.normalized(f64=True)[0], o[0], equal_nan=True)
                for s, o in zip(series, outs))
@@ -332,6 +347,7 @@ def run_batch(args, dev):
             "plain_series_per_s": n / t_plain, "batched_series_per_s": n / t_batch,
             "batched_over_plain": t_plain / t_batch, "kernels_in_graph": int(kernels),
             "concurrent_chains": int(lanes),
+            "form": "work_queue" if queue else "chains", "forms": forms,
             "thread_caps": {str(c): caps.count(c) for c in sorted(set(caps))},
             "identical_results": bool(same), "reps": args.batch_reps,
             "plain_device_ms_sum": plain_dev,

@@ -358,16 +358,22 @@ int xpcs_get_twotime(xpcs_series *s, int32_t *qbins, float *sg, float *c2t, floa
 /* Batches: no counterpart in the reference, which runs one series per
  * process.  A batch holds several series handles of one device (uneven frame
  * counts, detector sizes and occupancies) and runs the whole path for all of
- * them -- filter/transpose, multi-tau and normalisation -- as one CUDA graph in
- * which the series' kernels are independent branches, so that small series
- * fill the GPU together instead of one after another (the series are dealt,
- * largest first, onto a number of concurrent chains; XPCS_BATCH_AUTOTUNE
- * times the candidate chain counts on the first run).  The graph is captured
- * on the first run and replayed until a member's frames, the mode or the flags
- * change (then it is captured again).  The work of each series is the same as
- * xpcs_multitau + xpcs_normalize on its own, so results are bit-identical to
- * running the series alone.  Member handles must outlive the batch and must
- * not be used by other threads while xpcs_batch_run runs.
+ * them -- filter/transpose, multi-tau and normalisation -- as one CUDA graph,
+ * captured on the first run and replayed until a member's frames, the mode or
+ * the flags change (then it is captured again).  Members are dealt, largest
+ * first, onto a number of concurrent chains.  Two forms:
+ *  - work queue (the default): the chains run every member's transpose, then
+ *    the multi-tau of all members runs as persistent launches over a device
+ *    work queue -- one per thread-kernel row capacity, pulling 32-pixel groups
+ *    of every member, and one per warp-per-pixel row tier, pulling rows of
+ *    every member -- then the chains run every member's normalisation;
+ *  - chains: each member's whole path runs on its chain.
+ * XPCS_BATCH_AUTOTUNE times both forms with 1 .. all chains on the first run
+ * (and tunes each member's knobs, xpcs_autotune) and keeps the fastest.  The
+ * work of each series is the same as xpcs_multitau + xpcs_normalize on its
+ * own, so results are bit-identical to running the series alone.  Member
+ * handles must outlive the batch and must not be used by other threads while
+ * xpcs_batch_run runs.
  *  flags: XPCS_BATCH_F64 (float64 normalisation), XPCS_BATCH_F32 (float32
  *  normalisation in the reference's operation order), XPCS_BATCH_AUTOTUNE
  *  (tune each member's kernel choice first); read the results with
@@ -388,6 +394,11 @@ int xpcs_batch_stats(xpcs_batch *b, float *ms, int64_t *kernels, int32_t *lanes)
  * device's global timer, stamped by one-thread kernels in the graph around
  * each member's work).  Either pointer may be NULL. */
 int xpcs_batch_timeline(xpcs_batch *b, float *start_ms, float *end_ms);
+/* Chooses the form of the next runs (1: work queue, 0: chains); autotuning
+ * then keeps this form and tunes only the chain count.  get_form reports the
+ * form and chain count in use (either pointer may be NULL). */
+int xpcs_batch_set_form(xpcs_batch *b, int32_t work_queue);
+int xpcs_batch_get_form(xpcs_batch *b, int32_t *work_queue, int32_t *chains);
 void xpcs_batch_destroy(xpcs_batch *b);
 
 /* Serving (no reference counterpart): several acquisitions streamed at once.

@@ -202,3 +202,35 @@ def test_every_knob_setting_gives_the_same_bits(mode):
                     s.set_tuning(*bad)
         finally:
             s.close()
+
+
+LONG_ROWS = [(48, 4000, 0.15, 8, (10, 300)), (24, 8000, 0.25, 8, (5, 800))]
+
+
+@pytest.mark.parametrize("queue", [True, False])
+def test_both_batch_forms_equal_each_series_alone(queue):
+    """The work-queue form (multi-tau of every member as persistent launches
+    pulling 32-pixel groups and rows from device counters) and the chains form
+    give each member the bits it gets alone: rows of every kernel class, from
+    short thread-per-pixel rows to 1,000-4,000-event warp-per-pixel rows and
+    float rows (flatfield, dense)."""
+    members = [open_member(*synth_member(i, *m)) for i, m in enumerate(MIX + LONG_ROWS)]
+    goldens = [golden_member(n) for n in ("sparse_flat", "dense_dark")]
+    series = members + [s for _, s in goldens]
+    try:
+        solo = [alone(s, xg.MODE_REFERENCE) for s in series]
+        with xg.Batch(series) as b:
+            b.set_form(queue)
+            b.run(xg.MODE_REFERENCE, f64=True, f32=True)
+            assert b.form() == (queue, len(series))
+            for s, r in zip(series, solo):
+                assert_same(results(s), r)
+            b.run(xg.MODE_REFERENCE, f64=True, f32=True, autotune=True)
+            assert b.form()[0] == queue  # autotuning keeps the chosen form
+            for s, r in zip(series, solo):
+                assert_same(results(s), r)
+            start, end = b.timeline()
+            assert np.all(end > start)
+    finally:
+        for s in series:
+            s.close()

@@ -648,6 +648,32 @@ int xpcs_batch_stats(xpcs_batch *h, float *ms, int64_t *kernels, int32_t *lanes)
   });
 }
 
+int xpcs_batch_set_form(xpcs_batch *h, int32_t work_queue) {
+  return guarded([&] {
+    need(h, "null batch");
+    need(work_queue == 0 || work_queue == 1, "work_queue must be 0 or 1");
+    Batch &b = *(Batch *)h;
+    DeviceGuard g(b.device);
+    XG_CUDA(cudaStreamSynchronize(b.origin));
+    b.queue = work_queue != 0;
+    b.form_tuned = true;
+    b.lanes_tuned = false;
+    if (b.exec) {
+      cudaGraphExecDestroy(b.exec);
+      b.exec = nullptr;
+    }
+  });
+}
+
+int xpcs_batch_get_form(xpcs_batch *h, int32_t *work_queue, int32_t *chains) {
+  return guarded([&] {
+    need(h, "null batch");
+    Batch &b = *(Batch *)h;
+    if (work_queue) *work_queue = b.queue ? 1 : 0;
+    if (chains) *chains = b.lanes;
+  });
+}
+
 int xpcs_batch_timeline(xpcs_batch *h, float *start_ms, float *end_ms) {
   return guarded([&] {
     need(h, "null batch");

@@ -30,6 +30,13 @@ Batch::~Batch() {
   if (exec) cudaGraphExecDestroy(exec);
   for (cudaEvent_t e : join)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : join2)
+    if (e) cudaEventDestroy(e);
+  if (fork2) cudaEventDestroy(fork2);
+  if (origin) {
+    mtq.tab.release(origin);
+    mtq.next.release(origin);
+  }
   if (origin) {
     stamps.release(origin);
     cudaStreamSynchronize(origin);
@@ -66,6 +73,9 @@ Batch *batch_create(Series *const *ss, int32_t n) {
     XG_CUDA(cudaEventCreate(&b->t1));
     b->join.assign(n, nullptr);
     for (auto &e : b->join) XG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->join2.assign(n, nullptr);
+    for (auto &e : b->join2) XG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    XG_CUDA(cudaEventCreateWithFlags(&b->fork2, cudaEventDisableTiming));
     b->stamps.reserve(2 * (size_t)n + 1, b->origin);
   } catch (...) {
     delete b;
@@ -169,7 +179,16 @@ bool stale(const Batch &b, int mode, uint32_t flags) {
   return false;
 }
 
-void build_graph(Batch &b, int mode, uint32_t flags, int lanes) {
+// The batch as one CUDA graph.  Members are dealt, largest first, onto
+// `lanes` chains that run side by side.
+//   chains form: each member's whole path (transpose, multi-tau,
+//     normalisation) runs on its chain;
+//   work-queue form: the chains run every member's transpose; then the
+//     multi-tau of all members runs as persistent work-queue launches (one per
+//     thread-kernel row capacity, one per warp-per-pixel row tier) that pull
+//     32-pixel groups and rows of every member from device counters; then the
+//     chains run every member's normalisation.
+void build_graph(Batch &b, int mode, uint32_t flags, int lanes, bool queue) {
   if (b.exec) {
     cudaGraphExecDestroy(b.exec);
     b.exec = nullptr;
@@ -184,6 +203,7 @@ void build_graph(Batch &b, int mode, uint32_t flags, int lanes) {
   });
   std::vector<int64_t> load(lanes, 0);
   std::vector<int> last(lanes, -1);  // last series of each chain
+  std::vector<int> chain(n, 0);
   XG_CUDA(cudaStreamBeginCapture(b.origin, cudaStreamCaptureModeRelaxed));
   cudaGraph_t g = nullptr;
   const int64_t l0 = tl_launches;
@@ -197,15 +217,37 @@ void build_graph(Batch &b, int mode, uint32_t flags, int lanes) {
       XG_CUDA(cudaStreamWaitEvent(s.stream, last[c] < 0 ? b.fork : b.join[last[c]], 0));
       k_stamp<<<1, 1, 0, s.stream>>>(b.stamps.p + 2 * i);
       XG_CHECK_LAUNCH();
-      series_pass(s, mode, flags);
-      k_stamp<<<1, 1, 0, s.stream>>>(b.stamps.p + 2 * i + 1);
-      XG_CHECK_LAUNCH();
+      if (queue) {
+        run_filter_transpose(s);
+      } else {
+        series_pass(s, mode, flags);
+        k_stamp<<<1, 1, 0, s.stream>>>(b.stamps.p + 2 * i + 1);
+        XG_CHECK_LAUNCH();
+      }
       XG_CUDA(cudaEventRecord(b.join[i], s.stream));
       load[c] += s.raw_events + s.P;
       last[c] = i;
+      chain[i] = c;
     }
     for (int c = 0; c < lanes; c++)
       if (last[c] >= 0) XG_CUDA(cudaStreamWaitEvent(b.origin, b.join[last[c]], 0));
+    if (queue) {
+      mt_queue_run(b.ss, b.mtq, b.origin);
+      XG_CUDA(cudaEventRecord(b.fork2, b.origin));
+      std::vector<int> last2(lanes, -1);
+      for (int i : order) {
+        const int c = chain[i];
+        Series &s = *b.ss[i];
+        XG_CUDA(cudaStreamWaitEvent(s.stream, last2[c] < 0 ? b.fork2 : b.join2[last2[c]], 0));
+        run_normalize(s, (flags & XPCS_BATCH_F64) != 0, (flags & XPCS_BATCH_F32) != 0);
+        k_stamp<<<1, 1, 0, s.stream>>>(b.stamps.p + 2 * i + 1);
+        XG_CHECK_LAUNCH();
+        XG_CUDA(cudaEventRecord(b.join2[i], s.stream));
+        last2[c] = i;
+      }
+      for (int c = 0; c < lanes; c++)
+        if (last2[c] >= 0) XG_CUDA(cudaStreamWaitEvent(b.origin, b.join2[last2[c]], 0));
+    }
   } catch (...) {
     cudaStreamEndCapture(b.origin, &g);
     if (g) cudaGraphDestroy(g);
@@ -221,6 +263,7 @@ void build_graph(Batch &b, int mode, uint32_t flags, int lanes) {
     throw Error(XPCS_ERR_CUDA, cudaGetErrorString(e));
   }
   b.lanes = lanes;
+  b.queue = queue;
 }
 
 float launch(Batch &b) {
@@ -251,26 +294,34 @@ void capture(Batch &b, int mode, uint32_t flags) {
   // eager pass: buffers reach their sizes, frame tables and plans are uploaded
   for (Series *s : b.ss) series_pass(*s, mode, flags);
   for (Series *s : b.ss) XG_CUDA(cudaStreamSynchronize(s->stream));
+  mt_queue_build(b.ss, b.mtq, b.origin);
   const int n = (int)b.ss.size();
   if ((flags & XPCS_BATCH_AUTOTUNE) && !b.lanes_tuned) {
+    // both forms, each with 1 .. n chains; the fastest graph is kept
     int best = n;
+    bool best_queue = b.queue;
     float best_ms = 0.f;
     bool first = true;
-    for (int lanes : {1, 2, 4, 8, 16, n}) {
-      if (lanes > n) continue;
-      build_graph(b, mode, flags, lanes);
-      launch(b);
-      const float ms = launch(b);
-      if (first || ms < best_ms) {
-        best_ms = ms;
-        best = lanes;
-        first = false;
+    for (bool queue : {true, false}) {
+      if (b.form_tuned && queue != b.queue) continue;  // a form the caller chose
+      for (int lanes : {1, 2, 4, 8, 16, n}) {
+        if (lanes > n) continue;
+        build_graph(b, mode, flags, lanes, queue);
+        launch(b);
+        const float ms = launch(b);
+        if (first || ms < best_ms) {
+          best_ms = ms;
+          best = lanes;
+          best_queue = queue;
+          first = false;
+        }
       }
     }
     b.lanes = best;
+    b.queue = best_queue;
     b.lanes_tuned = true;
   }
-  build_graph(b, mode, flags, b.lanes);
+  build_graph(b, mode, flags, b.lanes, b.queue);
   b.mode = mode;
   b.flags = flags;
   b.gens.resize(b.ss.size());

@@ -161,13 +161,20 @@ __device__ __forceinline__ void bins_pairs(const uint32_t *row, int m, int lf, i
     if (k < count) acc[k * 32] = a[k];
 }
 
+// One warp's 32 consecutive pixels p0 .. p0+31 of a series: the body of the
+// thread-per-pixel kernel, shared by its per-series launch and by the batch's
+// work-queue launch.  wbase: the warp's (CAP + scratch words) x 32 words of
+// shared memory.
 template <int CAP>
-__global__ void __launch_bounds__(MT_WARPS * 32, 8)
-k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
-            const int32_t *__restrict__ row_len, const uint8_t *__restrict__ pclass,
-            const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
-            float *__restrict__ G2, float *__restrict__ IP, float *__restrict__ IF) {
-  extern __shared__ __align__(16) uint8_t smem[];
+__device__ __forceinline__ void mt_thread_warp(const uint8_t *__restrict__ plan_g,
+                                               const int64_t *__restrict__ row_ptr,
+                                               const int32_t *__restrict__ row_len,
+                                               const uint8_t *__restrict__ pclass,
+                                               const int32_t *__restrict__ ev_frame,
+                                               const float *__restrict__ ev_val,
+                                               float *__restrict__ G2, float *__restrict__ IP,
+                                               float *__restrict__ IF, int p0,
+                                               uint32_t *wbase) {
   // the plan is read from global memory: every lane of a warp reads the same
   // words (one L1-cached broadcast), and shared memory is left to the rows
   const McPlan *pl = (const McPlan *)plan_g;
@@ -175,12 +182,10 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
   const McArrays ar = mc_arrays(plan_g, D);
   const int P = pl->P, nlev = pl->nlev, mode = pl->mode;
   const int scr = pl->scr;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *wbase = (uint32_t *)smem + (size_t)warp * (CAP + scr) * 32;
+  const int lane = threadIdx.x & 31;
   uint32_t *row = wbase + lane;
   int32_t *acc = (int32_t *)(row + CAP * 32);  // scratch, also S(t_end) per level
 
-  const int p0 = (blockIdx.x * MT_WARPS + warp) * 32;
   if (p0 >= P) return;
   const int p = p0 + lane;
   const bool mine = p < P && pclass[p] == PCLASS_THREAD;
@@ -417,6 +422,20 @@ k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_
   }
 }
 
+template <int CAP>
+__global__ void __launch_bounds__(MT_WARPS * 32, 8)
+k_mt_thread(const uint8_t *__restrict__ plan_g, const int64_t *__restrict__ row_ptr,
+            const int32_t *__restrict__ row_len, const uint8_t *__restrict__ pclass,
+            const int32_t *__restrict__ ev_frame, const float *__restrict__ ev_val,
+            float *__restrict__ G2, float *__restrict__ IP, float *__restrict__ IF) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int scr = ((const McPlan *)plan_g)->scr;
+  const int warp = threadIdx.x >> 5;
+  uint32_t *wbase = (uint32_t *)smem + (size_t)warp * (CAP + scr) * 32;
+  mt_thread_warp<CAP>(plan_g, row_ptr, row_len, pclass, ev_frame, ev_val, G2, IP, IF,
+                      (blockIdx.x * MT_WARPS + warp) * 32, wbase);
+}
+
 // ------------------------------------------------------- warp per pixel
 
 // lower_bound over a contiguous packed row (frame in the high half)
@@ -477,6 +496,117 @@ __device__ int compact_row(uint32_t *row, int m, int lastframe, int lane) {
 //     the level.  On sorted levels where a fifth of the bins hold an entry,
 //     the prefix-sum array (done with after IP/IF) holds the values by bin
 //     and a source finds each partner by one lookup.
+// One pixel p of a series with a row of n0 events (min_n < n0 <= cap): the
+// body of the warp-per-pixel kernel, shared by its per-series launches and by
+// the batch's work-queue launches.  pl / ar: the plan (shared or global
+// memory); row, S: the warp's 2 x cap words; acc: this lane's accumulators
+// (acc[k * 32]).
+__device__ __forceinline__ void mt_warp_pixel(const McPlan *pl, const McArrays &ar, int p,
+                                              const int64_t *__restrict__ row_ptr,
+                                              const int32_t *__restrict__ row_len,
+                                              const int32_t *__restrict__ ev_frame,
+                                              const float *__restrict__ ev_val,
+                                              float *__restrict__ G2, float *__restrict__ IP,
+                                              float *__restrict__ IF, int cap, uint32_t *row,
+                                              int32_t *S, int32_t *acc) {
+  const int P = pl->P, mode = pl->mode, D = pl->D;
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const int n0 = row_len[p];
+  const int64_t b = row_ptr[p];
+  int carry = 0;
+  for (int c0 = 0; c0 < n0; c0 += 32) {
+    const int i = c0 + lane;
+    int x = 0;
+    if (i < n0) {
+      x = __float2int_rn(ev_val[b + i]);
+      row[i] = pk(ev_frame[b + i], x);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, x, o);
+      if (lane >= o) x += y;
+    }
+    if (i < n0) S[i] = x + carry;
+    carry += __shfl_sync(FULL, x, 31);
+  }
+  __syncwarp();
+  // IP(d) = S(t_ip[d]); IF(d) = S(t_end of its level) - S(tau_abs[d]); S(T) = sum of
+  // v over frames < T
+  for (int d = lane; d < D; d += 32) {
+    const int g = ar.gi[d];
+    const int lvl = pl->lv[g].level;
+    const int c_ip = lower_bound_row(row, n0, ar.t_ip[d]);
+    const int c_end = lower_bound_row(row, n0, pl->lv[g].t_end);
+    const int c_tau = lower_bound_row(row, n0, ar.tau_abs[d]);
+    const int ip = c_ip ? S[c_ip - 1] : 0;
+    const int iff = (c_end ? S[c_end - 1] : 0) - (c_tau ? S[c_tau - 1] : 0);
+    IP[(size_t)d * P + p] = scaled_quotient(ip, lvl, ar.denom[d], ar.rcp[d]);
+    IF[(size_t)d * P + p] = scaled_quotient(iff, lvl, ar.denom[d], ar.rcp[d]);
+  }
+  int m = n0;
+  bool J = true, U = true;  // junction at m sorted; stale suffix [m, n0) sorted
+  for (int gi = 0; gi < pl->nlev; gi++) {
+    const McLevel L = pl->lv[gi];
+    if (L.compact && m > 0) {
+      const int m2 = compact_row(row, m, L.lastframe, lane);
+      U = (m2 < m) ? (J && U) : U;
+      J = (m2 == 0 || m2 >= n0) ? true : (pk_t(row[m2 - 1]) <= pk_t(row[m2]));
+      m = m2;
+    }
+    const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
+    const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
+    for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
+    const int lf = L.lastframe;
+    if (sorted && tlo >= 1 && lf <= cap && 5 * m >= lf) {
+      // at least a fifth of the level's bins hold an entry: the prefix sums
+      // S are done with, and S becomes the row's values by bin, so that each
+      // source finds its partner for every delay with one lookup (a missing
+      // bin reads 0, which adds nothing)
+      for (int bq = lane; bq < lf; bq += 32) S[bq] = 0;
+      __syncwarp();
+      for (int k = lane; k < m; k += 32) S[pk_t(row[k])] = pk_v(row[k]);
+      __syncwarp();
+      for (int i = lane; i < m; i += 32) {
+        const uint32_t wi = row[i];
+        const int ti = pk_t(wi), vi = pk_v(wi);
+        for (int k = 0; k < L.count; k++) {
+          const int tb = ti + tlo + k;
+          if (tb < lf) acc[k * 32] += vi * S[tb];
+        }
+      }
+    } else {
+      int i = lane, j = lane + 1;
+      uint32_t wi = i < m ? row[i] : 0u;
+      uint32_t wj = j < m ? row[j] : 0u;
+      while (i < m) {
+        const int d = pk_t(wj) - pk_t(wi);
+        if (j < m && d <= thi) {
+          if (d >= tlo && (sorted || lower_bound_row(row, n0, pk_t(wj)) == j))
+            acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
+          j++;
+        } else {
+          i += 32;
+          if (i >= m) break;
+          wi = row[i];
+          j = i + 1;
+        }
+        wj = j < m ? row[j] : 0u;
+      }
+    }
+    int mine = 0;
+    for (int k = 0; k < L.count; k++) {
+      const int tot = __reduce_add_sync(FULL, acc[k * 32]);
+      if (lane == k) mine = tot;
+    }
+    if (lane < L.count) {
+      const int d = L.first + lane;
+      G2[(size_t)d * P + p] = scaled_quotient(mine, 2 * L.level, ar.denom[d], ar.rcp[d]);
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void __launch_bounds__(256)
 k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
           const int32_t *__restrict__ count_p, int32_t min_n, int32_t cap,
@@ -490,109 +620,97 @@ k_mt_warp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ list,
   __syncthreads();
   const McPlan *pl = (const McPlan *)smem;
   const McArrays ar = mc_arrays(smem, D);
-  const int P = pl->P, mode = pl->mode, ACC = max(pl->acc, pl->nlev);
+  const int ACC = max(pl->acc, pl->nlev);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
   uint32_t *row = (uint32_t *)(smem + pb) + (size_t)warp * (2 * cap + 32 * ACC);
   int32_t *S = (int32_t *)(row + cap);
   int32_t *acc = S + cap + lane;  // acc[k * 32]: this lane's accumulator k
-  const unsigned FULL = 0xffffffffu;
   const int nw = *count_p;
   for (int q = blockIdx.x * nwb + warp; q < nw; q += gridDim.x * nwb) {
     const int p = list[q];
     const int n0 = row_len[p];
     if (n0 <= min_n || n0 > cap) continue;  // another launch's share of the list
-    const int64_t b = row_ptr[p];
-    int carry = 0;
-    for (int c0 = 0; c0 < n0; c0 += 32) {
-      const int i = c0 + lane;
-      int x = 0;
-      if (i < n0) {
-        x = __float2int_rn(ev_val[b + i]);
-        row[i] = pk(ev_frame[b + i], x);
-      }
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL, x, o);
-        if (lane >= o) x += y;
-      }
-      if (i < n0) S[i] = x + carry;
-      carry += __shfl_sync(FULL, x, 31);
+    mt_warp_pixel(pl, ar, p, row_ptr, row_len, ev_frame, ev_val, G2, IP, IF, cap, row, S, acc);
+  }
+}
+
+// ------------------------------------------------ batch work-queue launches
+//
+// The multi-tau of every member of a batch as persistent grids that pull work
+// items from a device counter: 32-pixel groups of every member with the same
+// thread-kernel row capacity in one launch, the warp-per-pixel rows of every
+// member in one launch per row tier.  Small members' items run beside large
+// members' items, and no member's kernel leaves a tail of idle SMs.
+
+// Thread-per-pixel items: group g of the queue is group g - first of the
+// member whose range holds it.  wbase strides by the batch's largest scratch.
+template <int CAP>
+__global__ void __launch_bounds__(MT_WARPS * 32, 8)
+k_mt_thread_queue(const MtQueueMember *__restrict__ tab, int32_t n, int32_t total,
+                  int32_t scr_max, int32_t *__restrict__ next) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *wbase = (uint32_t *)smem + (size_t)warp * (CAP + scr_max) * 32;
+  for (;;) {
+    int g = 0;
+    if (lane == 0) g = atomicAdd(next, 1);
+    g = __shfl_sync(0xffffffffu, g, 0);
+    if (g >= total) break;
+    int lo = 0, hi = n - 1;  // the last member whose first group is <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid].first <= g) lo = mid;
+      else hi = mid - 1;
     }
+    const MtQueueMember &m = tab[lo];
+    mt_thread_warp<CAP>(m.plan, m.row_ptr, m.row_len, m.pclass, m.ev_frame, m.ev_val, m.G2, m.IP,
+                        m.IF, (g - m.first) * 32, wbase);
     __syncwarp();
-    // IP(d) = S(t_ip[d]); IF(d) = S(t_end of its level) - S(tau_abs[d]); S(T) = sum of
-    // v over frames < T
-    for (int d = lane; d < D; d += 32) {
-      const int g = ar.gi[d];
-      const int lvl = pl->lv[g].level;
-      const int c_ip = lower_bound_row(row, n0, ar.t_ip[d]);
-      const int c_end = lower_bound_row(row, n0, pl->lv[g].t_end);
-      const int c_tau = lower_bound_row(row, n0, ar.tau_abs[d]);
-      const int ip = c_ip ? S[c_ip - 1] : 0;
-      const int iff = (c_end ? S[c_end - 1] : 0) - (c_tau ? S[c_tau - 1] : 0);
-      IP[(size_t)d * P + p] = scaled_quotient(ip, lvl, ar.denom[d], ar.rcp[d]);
-      IF[(size_t)d * P + p] = scaled_quotient(iff, lvl, ar.denom[d], ar.rcp[d]);
+  }
+}
+
+// Warp-per-pixel items: entry q of the members' warp lists (use_long = 0) or
+// long-row lists, concatenated in table order; rows outside (min_n, cap]
+// belong to another tier's launch.  The plan is read from global memory.
+__global__ void __launch_bounds__(256)
+k_mt_warp_queue(const MtQueueMember *__restrict__ tab, int32_t n, int32_t use_long,
+                int32_t min_n, int32_t cap, int32_t acc_max, int32_t *__restrict__ next) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  int32_t *pref = (int32_t *)smem;  // [n + 1]: first entry of each member's list
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    int32_t t = 0;
+    for (int i = 0; i < n; i++) {
+      pref[i] = t;
+      t += use_long ? tab[i].stats->nlong : tab[i].stats->nwarp;
     }
-    int m = n0;
-    bool J = true, U = true;  // junction at m sorted; stale suffix [m, n0) sorted
-    for (int gi = 0; gi < pl->nlev; gi++) {
-      const McLevel L = pl->lv[gi];
-      if (L.compact && m > 0) {
-        const int m2 = compact_row(row, m, L.lastframe, lane);
-        U = (m2 < m) ? (J && U) : U;
-        J = (m2 == 0 || m2 >= n0) ? true : (pk_t(row[m2 - 1]) <= pk_t(row[m2]));
-        m = m2;
-      }
-      const bool sorted = mode != XPCS_MODE_REFERENCE || (J && U);
-      const int tlo = L.tau_lo, thi = L.tau_lo + L.count - 1;
-      for (int k = 0; k < L.count; k++) acc[k * 32] = 0;
-      const int lf = L.lastframe;
-      if (sorted && tlo >= 1 && lf <= cap && 5 * m >= lf) {
-        // at least a fifth of the level's bins hold an entry: the prefix sums
-        // S are done with, and S becomes the row's values by bin, so that each
-        // source finds its partner for every delay with one lookup (a missing
-        // bin reads 0, which adds nothing)
-        for (int bq = lane; bq < lf; bq += 32) S[bq] = 0;
-        __syncwarp();
-        for (int k = lane; k < m; k += 32) S[pk_t(row[k])] = pk_v(row[k]);
-        __syncwarp();
-        for (int i = lane; i < m; i += 32) {
-          const uint32_t wi = row[i];
-          const int ti = pk_t(wi), vi = pk_v(wi);
-          for (int k = 0; k < L.count; k++) {
-            const int tb = ti + tlo + k;
-            if (tb < lf) acc[k * 32] += vi * S[tb];
-          }
-        }
-      } else {
-        int i = lane, j = lane + 1;
-        uint32_t wi = i < m ? row[i] : 0u;
-        uint32_t wj = j < m ? row[j] : 0u;
-        while (i < m) {
-          const int d = pk_t(wj) - pk_t(wi);
-          if (j < m && d <= thi) {
-            if (d >= tlo && (sorted || lower_bound_row(row, n0, pk_t(wj)) == j))
-              acc[(d - tlo) * 32] += pk_v(wi) * pk_v(wj);
-            j++;
-          } else {
-            i += 32;
-            if (i >= m) break;
-            wi = row[i];
-            j = i + 1;
-          }
-          wj = j < m ? row[j] : 0u;
-        }
-      }
-      int mine = 0;
-      for (int k = 0; k < L.count; k++) {
-        const int tot = __reduce_add_sync(FULL, acc[k * 32]);
-        if (lane == k) mine = tot;
-      }
-      if (lane < L.count) {
-        const int d = L.first + lane;
-        G2[(size_t)d * P + p] = scaled_quotient(mine, 2 * L.level, ar.denom[d], ar.rcp[d]);
-      }
-      __syncwarp();
+    pref[n] = t;
+  }
+  __syncthreads();
+  const int total = pref[n];
+  const size_t pref_bytes = mc_align16(sizeof(int32_t) * (size_t)(n + 1));
+  uint32_t *row = (uint32_t *)(smem + pref_bytes) + (size_t)warp * (2 * cap + 32 * acc_max);
+  int32_t *S = (int32_t *)(row + cap);
+  int32_t *acc = S + cap + lane;
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(next, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= total) break;
+    int lo = 0, hi = n - 1;  // the last member whose list starts at or before q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (pref[mid] <= q) lo = mid;
+      else hi = mid - 1;
     }
+    const MtQueueMember &m = tab[lo];
+    const int p = (use_long ? m.llist : m.wlist)[q - pref[lo]];
+    const int n0 = m.row_len[p];
+    if (n0 <= min_n || n0 > cap) continue;
+    const McPlan *pl = (const McPlan *)m.plan;
+    const McArrays ar = mc_arrays(m.plan, pl->D);
+    mt_warp_pixel(pl, ar, p, m.row_ptr, m.row_len, m.ev_frame, m.ev_val, m.G2, m.IP, m.IF, cap,
+                  row, S, acc);
   }
 }
 
@@ -969,6 +1087,43 @@ size_t warp_smem(int D, int acc, int cap, int warps) {
   return mc_plan_bytes(D) + (size_t)warps * (2 * cap + 32 * acc) * sizeof(int32_t);
 }
 
+// The float rows of a series (flatfield, average, hot pixels, dense data,
+// normalize_by_framesum) on st: the warp-per-row replay when the schedule
+// allows it, else the thread-per-row one.
+void launch_float_rows(Series &s, const McPlan &hp, cudaStream_t st, int sms) {
+  const int P = s.P;
+  size_t ne = s.raw_events > 0 ? (size_t)s.raw_events : 1;
+  s.sc_frame.reserve(ne, st);
+  s.sc_val.reserve(ne, st);
+  int grid = std::max(1, std::min((P + 127) / 128, sms * 8));
+  const float *fscale = nullptr;
+  if (s.desc.normalize_by_framesum) {
+    prepare_framesum_scale(s);
+    fscale = s.d_fscale.p;
+  }
+  int kmax = 0;
+  for (int g = 0; g < hp.nlev; g++) kmax = std::max(kmax, hp.lv[g].tau_lo + hp.lv[g].count - 1);
+  if (kmax <= FW_MAXC && hp.acc <= FW_MAXC) {
+    const size_t wb =
+        (64 * 9 + FW_WIN * 5 + (3 * (size_t)hp.acc + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
+    const size_t smf = FW_WARPS * wb;
+    XG_CUDA(cudaFuncSetAttribute(k_mt_fwarp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smf));
+    int per_sm = 0;
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mt_fwarp, FW_WARPS * 32,
+                                                          smf));
+    XG_CUDA(cudaMemsetAsync(&s.stats.p->fnext, 0, sizeof(int32_t), st));
+    k_mt_fwarp<<<sms * std::max(1, per_sm), FW_WARPS * 32, smf, st>>>(
+        s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p, s.ev_frame.p, s.ev_val.p,
+        fscale, s.sc_frame.p, s.sc_val.p, s.G2.p, s.IP.p, s.IF.p);
+  } else {
+    k_mt_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p,
+                                     s.ev_frame.p, s.ev_val.p, fscale, s.sc_frame.p, s.sc_val.p,
+                                     s.G2.p, s.IP.p, s.IF.p);
+  }
+  XG_CHECK_LAUNCH();
+}
+
 }  // namespace
 
 // The float nearest to 1/b (ties to even) for an integer b in [1, 2^24]:
@@ -1045,37 +1200,94 @@ void run_multitau(Series &s, int mode) {
       s.ev_frame.p, s.ev_val.p, s.G2.p, s.IP.p, s.IF.p);
   XG_CHECK_LAUNCH();
   XG_CUDA(cudaEventRecord(s.ev[5], st));
-  size_t ne = s.raw_events > 0 ? (size_t)s.raw_events : 1;
-  s.sc_frame.reserve(ne, st);
-  s.sc_val.reserve(ne, st);
-  int grid = std::max(1, std::min((P + 127) / 128, sms * 8));
-  const float *fscale = nullptr;
-  if (s.desc.normalize_by_framesum) {
-    prepare_framesum_scale(s);
-    fscale = s.d_fscale.p;
-  }
-  int kmax = 0;
-  for (int g = 0; g < hp->nlev; g++) kmax = std::max(kmax, hp->lv[g].tau_lo + hp->lv[g].count - 1);
-  if (kmax <= FW_MAXC && hp->acc <= FW_MAXC) {
-    const size_t wb =
-        (64 * 9 + FW_WIN * 5 + (3 * (size_t)hp->acc + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
-    const size_t smf = FW_WARPS * wb;
-    XG_CUDA(cudaFuncSetAttribute(k_mt_fwarp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smf));
-    int per_sm = 0;
-    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mt_fwarp, FW_WARPS * 32,
-                                                          smf));
-    XG_CUDA(cudaMemsetAsync(&s.stats.p->fnext, 0, sizeof(int32_t), st));
-    k_mt_fwarp<<<sms * std::max(1, per_sm), FW_WARPS * 32, smf, st>>>(
-        s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p, s.ev_frame.p, s.ev_val.p,
-        fscale, s.sc_frame.p, s.sc_val.p, s.G2.p, s.IP.p, s.IF.p);
-  } else {
-    k_mt_float<<<grid, 128, 0, st>>>(s.plan.p, s.flist.p, s.stats.p, s.row_ptr.p, s.row_len.p,
-                                     s.ev_frame.p, s.ev_val.p, fscale, s.sc_frame.p, s.sc_val.p,
-                                     s.G2.p, s.IP.p, s.IF.p);
-  }
-  XG_CHECK_LAUNCH();
+  launch_float_rows(s, *hp, st, sms);
   XG_CUDA(cudaEventRecord(s.ev[6], st));
+}
+
+void mt_queue_build(const std::vector<Series *> &ss, MtQueue &q, cudaStream_t st) {
+  std::vector<MtQueueMember> tab;
+  q.cap_first.assign(MT_THREAD_NCAPS, 0);
+  q.cap_count.assign(MT_THREAD_NCAPS, 0);
+  q.cap_groups.assign(MT_THREAD_NCAPS, 0);
+  q.scr_max = q.acc_max = 1;
+  for (int c = 0; c < MT_THREAD_NCAPS; c++) {
+    q.cap_first[c] = (int32_t)tab.size();
+    int32_t groups = 0;
+    for (Series *sp : ss) {
+      Series &s = *sp;
+      if (s.thread_cap != MT_THREAD_CAPS[c] || s.D == 0 || s.P == 0) continue;
+      const McPlan hp = *(const McPlan *)make_plan(s, s.plan_mode).data();
+      q.scr_max = std::max(q.scr_max, hp.scr);
+      q.acc_max = std::max(q.acc_max, std::max(hp.acc, hp.nlev));
+      MtQueueMember m{s.plan.p, s.row_ptr.p, s.row_len.p, s.pclass.p, s.ev_frame.p, s.ev_val.p,
+                      s.G2.p, s.IP.p, s.IF.p, s.wlist.p, s.llist.p, s.stats.p, groups,
+                      (s.P + 31) / 32};
+      groups += m.groups;
+      tab.push_back(m);
+    }
+    q.cap_count[c] = (int32_t)tab.size() - q.cap_first[c];
+    q.cap_groups[c] = groups;
+  }
+  q.tab.reserve(std::max<size_t>(tab.size(), 1), st);
+  if (!tab.empty())
+    XG_CUDA(cudaMemcpyAsync(q.tab.p, tab.data(), sizeof(MtQueueMember) * tab.size(),
+                            cudaMemcpyHostToDevice, st));
+  q.next.reserve(MT_THREAD_NCAPS + 3, st);
+  XG_CUDA(cudaStreamSynchronize(st));
+}
+
+void mt_queue_run(const std::vector<Series *> &ss, MtQueue &q, cudaStream_t st) {
+  const int32_t n = q.cap_first.empty() ? 0 : q.cap_first.back() + q.cap_count.back();
+  if (n == 0) return;
+  int dev = 0, sms = 0;
+  XG_CUDA(cudaGetDevice(&dev));
+  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  XG_CUDA(cudaMemsetAsync(q.next.p, 0, sizeof(int32_t) * (MT_THREAD_NCAPS + 3), st));
+  using QueueKernel = void (*)(const MtQueueMember *, int32_t, int32_t, int32_t, int32_t *);
+  const QueueKernel kq[MT_THREAD_NCAPS] = {k_mt_thread_queue<32>, k_mt_thread_queue<48>,
+                                           k_mt_thread_queue<64>, k_mt_thread_queue<80>,
+                                           k_mt_thread_queue<112>};
+  for (int c = 0; c < MT_THREAD_NCAPS; c++) {
+    if (!q.cap_count[c]) continue;
+    const size_t smt = thread_smem(q.scr_max, MT_THREAD_CAPS[c]);
+    if (smt > 227 * 1024)
+      throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay schedule too large for the multi-tau kernels");
+    XG_CUDA(cudaFuncSetAttribute(kq[c], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
+    int per_sm = 0;
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kq[c], MT_WARPS * 32, smt));
+    const int blocks = std::min(sms * std::max(1, per_sm), (q.cap_groups[c] + MT_WARPS - 1) /
+                                                               MT_WARPS);
+    kq[c]<<<std::max(1, blocks), MT_WARPS * 32, smt, st>>>(q.tab.p + q.cap_first[c],
+                                                           q.cap_count[c], q.cap_groups[c],
+                                                           q.scr_max, q.next.p + c);
+    XG_CHECK_LAUNCH();
+  }
+  // the warp-per-pixel tiers over every member: rows of 81-256, 257-1024 and
+  // 1025-4096 events (the thread kernels above wrote zeros for those pixels)
+  const int tiers[3][4] = {{0, 0, MT_WARP_CAP, WP_WARPS},
+                           {1, MT_WARP_CAP, MT_MID_CAP, MID_WARPS},
+                           {1, MT_MID_CAP, MT_LONG_CAP, LONG_WARPS}};
+  const size_t pref_bytes = mc_align16(sizeof(int32_t) * (size_t)(n + 1));
+  for (int t = 0; t < 3; t++) {
+    const int cap = tiers[t][2], warps = tiers[t][3];
+    const size_t sm = pref_bytes + (size_t)warps * (2 * cap + 32 * q.acc_max) * sizeof(int32_t);
+    if (sm > 227 * 1024)
+      throw Error(XPCS_ERR_INVALID_ARGUMENT, "delay schedule too large for the multi-tau kernels");
+    XG_CUDA(cudaFuncSetAttribute(k_mt_warp_queue, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm));
+    int per_sm = 0;
+    XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mt_warp_queue, warps * 32,
+                                                          sm));
+    k_mt_warp_queue<<<sms * std::max(1, per_sm), warps * 32, sm, st>>>(
+        q.tab.p, n, tiers[t][0], tiers[t][1], cap, q.acc_max, q.next.p + MT_THREAD_NCAPS + t);
+    XG_CHECK_LAUNCH();
+  }
+  for (Series *sp : ss) {  // float rows, member by member (none in integer data)
+    Series &s = *sp;
+    if (s.D == 0 || s.P == 0) continue;
+    const McPlan hp = *(const McPlan *)make_plan(s, s.plan_mode).data();
+    launch_float_rows(s, hp, st, sms);
+  }
 }
 
 }  // namespace xg

@@ -331,6 +331,36 @@ struct Series {
   size_t pinned_cap = 0;
 };
 
+// ------------------------------------------------- batch multi-tau queue
+
+// A batch member as the work-queue multi-tau kernels see it (device memory).
+struct MtQueueMember {
+  const uint8_t *plan;
+  const int64_t *row_ptr;
+  const int32_t *row_len;
+  const uint8_t *pclass;
+  const int32_t *ev_frame;
+  const float *ev_val;
+  float *G2, *IP, *IF;
+  const int32_t *wlist, *llist;
+  const DevStats *stats;
+  int32_t first;   // the member's first 32-pixel group in its capacity's queue
+  int32_t groups;  // its 32-pixel groups
+};
+
+// The members of a batch in one table, grouped by thread-kernel row capacity.
+struct MtQueue {
+  DBuf<MtQueueMember> tab;
+  DBuf<int32_t> next;                   // one queue counter per launch
+  std::vector<int32_t> cap_first, cap_count, cap_groups;  // per MT_THREAD_CAPS entry
+  int32_t scr_max = 0, acc_max = 0;
+};
+// Builds the table (after an eager pass has sized every buffer and uploaded
+// every plan); enqueues the multi-tau of every member as work-queue launches
+// (k_multitau.cu).
+void mt_queue_build(const std::vector<Series *> &ss, MtQueue &q, cudaStream_t st);
+void mt_queue_run(const std::vector<Series *> &ss, MtQueue &q, cudaStream_t st);
+
 // --------------------------------------------------------------- a batch
 
 struct Batch {
@@ -349,6 +379,11 @@ struct Batch {
   float last_ms = 0.f;
   int32_t lanes = 0;               // concurrent chains of series in the graph (0: one per series)
   bool lanes_tuned = false;
+  bool queue = true;               // multi-tau as one work-queue launch over all members
+  MtQueue mtq;
+  std::vector<cudaEvent_t> join2;  // work-queue form: ends of each member's second phase
+  cudaEvent_t fork2 = nullptr;     // work-queue form: the multi-tau launches are done
+  bool form_tuned = false;
   ~Batch();
 };
 Batch *batch_create(Series *const *ss, int32_t n);   // batch.cu

@@ -40,6 +40,7 @@ EXPORTS = [
     "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
     "xpcs_set_device_memory_limit", "xpcs_get_device_memory", "xpcs_series_set_block_frames",
     "xpcs_batch_timeline", "xpcs_series_get_tuning", "xpcs_series_set_tuning",
+    "xpcs_batch_set_form", "xpcs_batch_get_form",
 ]
 
 BATCH_F64 = 1
@@ -173,6 +174,9 @@ def lib() -> C.CDLL:
         L.xpcs_series_set_block_frames.argtypes = [C.c_void_p, C.c_int32]
         L.xpcs_batch_timeline.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_series_get_tuning.argtypes = [C.c_void_p, C.POINTER(Tuning)]
+        L.xpcs_batch_set_form.argtypes = [C.c_void_p, C.c_int32]
+        L.xpcs_batch_get_form.argtypes = [C.c_void_p, C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32)]
         L.xpcs_series_set_tuning.argtypes = [C.c_void_p, C.POINTER(Tuning)]
         L.xpcs_get_device_memory.argtypes = [C.c_int32, C.POINTER(C.c_uint64),
                                              C.POINTER(C.c_uint64)]
@@ -407,6 +411,16 @@ class Batch:
         lanes = C.c_int32(0)
         check(lib().xpcs_batch_stats(self._h, C.byref(ms), C.byref(k), C.byref(lanes)))
         return ms.value, k.value, lanes.value
+
+    def set_form(self, work_queue: bool):
+        """Work-queue form (True) or chains form (False) for the next runs."""
+        check(lib().xpcs_batch_set_form(self._h, 1 if work_queue else 0))
+
+    def form(self):
+        """(work_queue, chains) of the graph in use."""
+        q, c = C.c_int32(0), C.c_int32(0)
+        check(lib().xpcs_batch_get_form(self._h, C.byref(q), C.byref(c)))
+        return bool(q.value), c.value
 
     def timeline(self):
         """(start_ms, end_ms) of every member's work in the last run, from the launch."""
