@@ -690,6 +690,26 @@ def run_gpu_arm(args, dist):
             if len(parts) == 2 and not ln.startswith("#") and parts[0] == top:
                 traffic = int(parts[1])
 
+    # the instruction-issue roofline of the same kernel: warp instructions of one launch (ncu,
+    # committed) over its CUDA-event time, against 4 issue slots per SM per cycle
+    issue = None
+    ip = ROOT / "profiles" / "instructions.txt"
+    if ip.exists() and (acq.width, acq.height, F, acq.mean) == (1024, 1024, 10000, 0.005):
+        for ln in ip.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) == 2 and not ln.startswith("#") and parts[0] == top:
+                n_inst = int(parts[1])
+                mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+                sms = xg.device_sm_count(dev)
+                if mhz and sms and cand[top][1] > 0:
+                    ach = n_inst / (cand[top][1] * 1e-3)
+                    pk = sms * 4 * mhz * 1e6
+                    issue = {"warp_instructions": n_inst,
+                             "warp_instructions_per_event": n_inst / max(int(info.events), 1),
+                             "achieved": ach, "peak": pk, "unit": "warp instructions/s",
+                             "frac": ach / pk,
+                             "peak_note": f"{sms} SMs x 4 schedulers x {mhz:g} MHz (median "
+                                          "SM clock during the timed region)"}
     h2d = int(idx.nbytes + val.nbytes + 8 * (F + 1))
     d2h = int(sum(a.nbytes for a in out if a is not None))
     s.multitau(xg.MODE_REFERENCE)
@@ -715,7 +735,8 @@ def run_gpu_arm(args, dist):
         "roofline": {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
-                     "algorithmic_bytes": cand[top][0], "traffic": traffic},
+                     "algorithmic_bytes": cand[top][0], "traffic": traffic,
+                     "issue": issue},
         "clocks": clk,
         "gpu_launches": launches,
     }

@@ -249,6 +249,11 @@ int xpcs_get_stage_times(xpcs_series *s, xpcs_stage_times *t);
  * again.  0 = no limit (the default).  xpcs_get_device_memory reports the
  * bytes the library holds on the device and the limit. */
 int xpcs_set_device_memory_limit(int32_t device, uint64_t bytes);
+/* Streaming multiprocessors and compute capability of a device (no reference
+ * counterpart; for rooflines and launch sizing by callers).  Any pointer may
+ * be NULL. */
+int xpcs_device_properties(int32_t device, int32_t *sm_count, int32_t *cc_major,
+                           int32_t *cc_minor);
 int xpcs_get_device_memory(int32_t device, uint64_t *used, uint64_t *limit);
 
 /* Page-lock (cudaHostRegister) / release a caller buffer so that ingest copies

@@ -73,3 +73,10 @@ def test_pixel_index_outside_the_detector_is_an_input_error():
         G2 = s.g2ipif()[0]
     assert same_bits(G2, fx["ref_G2"])
     assert np.all(np.isfinite(G2))
+
+
+def test_device_properties_and_bad_ordinal():
+    assert xg.device_sm_count(0) >= 1
+    with pytest.raises(xg.XpcsError) as e:
+        xg.device_sm_count(1 << 20)
+    assert e.value.code == 1

@@ -796,6 +796,29 @@ int xpcs_get_stage_times(xpcs_series *h, xpcs_stage_times *t) {
   });
 }
 
+int xpcs_device_properties(int32_t device, int32_t *sm_count, int32_t *cc_major,
+                           int32_t *cc_minor) {
+  return guarded([&] {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      throw Error(XPCS_ERR_NO_DEVICE, "no CUDA device");
+    need(device >= 0 && device < ndev, "device ordinal out of range");
+    int v = 0;
+    if (sm_count) {
+      XG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device));
+      *sm_count = v;
+    }
+    if (cc_major) {
+      XG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMajor, device));
+      *cc_major = v;
+    }
+    if (cc_minor) {
+      XG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMinor, device));
+      *cc_minor = v;
+    }
+  });
+}
+
 int xpcs_set_device_memory_limit(int32_t device, uint64_t bytes) {
   return guarded([&] {
     need(device >= 0 && device < ACCT_DEVICES, "device ordinal out of range");

@@ -40,7 +40,7 @@ EXPORTS = [
     "xpcs_server_release", "xpcs_server_get_stats", "xpcs_twotime", "xpcs_get_twotime",
     "xpcs_set_device_memory_limit", "xpcs_get_device_memory", "xpcs_series_set_block_frames",
     "xpcs_batch_timeline", "xpcs_series_get_tuning", "xpcs_series_set_tuning",
-    "xpcs_batch_set_form", "xpcs_batch_get_form",
+    "xpcs_batch_set_form", "xpcs_batch_get_form", "xpcs_device_properties",
 ]
 
 BATCH_F64 = 1
@@ -175,6 +175,7 @@ def lib() -> C.CDLL:
         L.xpcs_batch_timeline.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.xpcs_series_get_tuning.argtypes = [C.c_void_p, C.POINTER(Tuning)]
         L.xpcs_batch_set_form.argtypes = [C.c_void_p, C.c_int32]
+        L.xpcs_device_properties.argtypes = [C.c_int32] + [C.POINTER(C.c_int32)] * 3
         L.xpcs_batch_get_form.argtypes = [C.c_void_p, C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int32)]
         L.xpcs_series_set_tuning.argtypes = [C.c_void_p, C.POINTER(Tuning)]
@@ -527,6 +528,13 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def device_sm_count(device: int = 0) -> int:
+    """Streaming multiprocessors of a device (xpcs_device_properties)."""
+    n = C.c_int32(0)
+    check(lib().xpcs_device_properties(device, C.byref(n), None, None))
+    return n.value
 
 
 def set_device_memory_limit(device: int, nbytes: int) -> None:
