@@ -495,7 +495,12 @@ __device__ int compact_row(uint32_t *row, int m, int lastframe, int lane) {
 //     visits into its own accumulators, summed over the warp at the end of
 //     the level.  On sorted levels where a fifth of the bins hold an entry,
 //     the prefix-sum array (done with after IP/IF) holds the values by bin
-//     and a source finds each partner by one lookup.
+//     and a source finds each partner by one lookup.  On other sorted levels
+//     of delays <= 64 where the row could reach every delay (m x (thi + 1) >=
+//     lastframe), the same words hold the row's occupancy bitmask: a source
+//     reads the 64 bins after it, finds its first partner's index by a
+//     population count over the bins below tau_lo and visits only the
+//     occupied bins of the delay window.
 // One pixel p of a series with a row of n0 events (min_n < n0 <= cap): the
 // body of the warp-per-pixel kernel, shared by its per-series launches and by
 // the batch's work-queue launches.  pl / ar: the plan (shared or global
@@ -575,6 +580,45 @@ __device__ __forceinline__ void mt_warp_pixel(const McPlan *pl, const McArrays &
           if (tb < lf) acc[k * 32] += vi * S[tb];
         }
       }
+    } else if (sorted && tlo >= 1 && thi <= 64 && lf <= 32 * cap && m * (thi + 1) >= lf) {
+      // about one entry or more per delay window: S (done with after IP/IF)
+      // becomes the level's occupancy bitmask.  Bins of the prefix are distinct
+      // and increasing, so the entry at bin b is at position popcount(bits
+      // below b): one 64-bit window of the mask after a source's bin gives the
+      // position of its first partner (entries closer than the smallest delay
+      // are counted, not visited) and which delays have a partner
+      uint32_t *mk = (uint32_t *)S;
+      const int nw = (lf + 31) >> 5;
+      for (int q = lane; q < nw; q += 32) mk[q] = 0u;
+      __syncwarp();
+      for (int k = lane; k < m; k += 32) {
+        const int t = pk_t(row[k]);
+        atomicOr(&mk[t >> 5], 1u << (t & 31));
+      }
+      __syncwarp();
+      const uint64_t gap = (1ull << (tlo - 1)) - 1ull;
+      const uint32_t cmask = L.count >= 32 ? 0xffffffffu : ((1u << L.count) - 1u);
+      for (int i = lane; i < m; i += 32) {
+        const uint32_t wi = row[i];
+        const int ti = pk_t(wi);
+        if (ti + tlo >= lf) break;  // this and later sources have no partner below lastframe
+        const int s0 = ti + 1, q = s0 >> 5, sh = s0 & 31;  // s0 < lf: word q exists
+        const uint32_t m0 = mk[q];
+        const uint32_t m1 = q + 1 < nw ? mk[q + 1] : 0u;
+        const uint32_t m2 = q + 2 < nw ? mk[q + 2] : 0u;
+        const uint64_t W =
+            ((uint64_t)__funnelshift_r(m1, m2, sh) << 32) | __funnelshift_r(m0, m1, sh);
+        int j = i + 1 + __popcll(W & gap);
+        uint32_t w = (uint32_t)(W >> (tlo - 1)) & cmask;
+        const int vi = pk_v(wi);
+        while (w) {
+          const int k = __ffs(w) - 1;
+          acc[k * 32] += vi * pk_v(row[j]);
+          j++;
+          w &= w - 1u;
+        }
+      }
+      __syncwarp();
     } else {
       int i = lane, j = lane + 1;
       uint32_t wi = i < m ? row[i] : 0u;
