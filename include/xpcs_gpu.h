@@ -167,7 +167,9 @@ int xpcs_set_dark(xpcs_series *s, const int16_t *dark, int32_t ndark);
  * GPU as frames arrive; only kept pixels are stored. */
 int xpcs_ingest_dense(xpcs_series *s, const int16_t *frames, int32_t nframes);
 
-/* As xpcs_ingest_dense with the frames already in device memory. */
+/* As xpcs_ingest_dense with the frames already in device memory.  They are
+ * read on the series' stream: keep them unchanged until the series has
+ * synchronised (xpcs_synchronize or any call that returns results). */
 int xpcs_ingest_dense_device(xpcs_series *s, const int16_t *frames_device, int32_t nframes);
 
 /* The --darkout datasets DarkAvg / DarkStd (main.cpp:459-478): float64

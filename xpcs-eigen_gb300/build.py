@@ -56,7 +56,8 @@ def _stale(target: Path, deps) -> bool:
 def build_gpu(force: bool = False, verbose: bool = False) -> Path:
     OBJ.mkdir(parents=True, exist_ok=True)
     headers = [INCLUDE / "xpcs_gpu.h", CSRC / "xpcs_internal.h", CSRC / "f64emu.cuh",
-               CSRC / "mt_replay.cuh"]
+               CSRC / "mt_replay.cuh",
+               CSRC / "classify.cuh"]
     jobs = []
     objs = []
     for src in GPU_SOURCES:

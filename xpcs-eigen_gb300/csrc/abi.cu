@@ -143,6 +143,11 @@ void free_series(Series *s) {
     s->dn_offsets.release(st);
     s->dn_frame_end.release(st);
     s->dn_prep.release(st);
+    s->dn_pend.release(st);
+    s->dn_tot.release(st);
+    s->dn_sum.release(st);
+    s->blk_pk.release(st);
+    s->d_blk_r0.release(st);
     s->d_frame_off.release(st);
     s->d_frame_map.release(st);
     s->d_chunk_frame.release(st);
@@ -237,6 +242,7 @@ int xpcs_series_create(const xpcs_series_desc *desc, xpcs_series **out) {
     s->P = desc->width * desc->height;
     s->F = desc->frames;
     s->R_in = desc->stride_frames * desc->avg_frames;
+    s->dense_px = desc->dense && s->R_in == 1;
     s->delays = delay_schedule(s->F, desc->delays_per_level);
     s->D = (int32_t)s->delays.level.size();
     s->qmap = build_qmap(desc->dqmap, desc->sqmap, s->P);

@@ -23,6 +23,7 @@
 #include <climits>
 #include <vector>
 
+#include "classify.cuh"
 #include "f64emu.cuh"
 #include "xpcs_internal.h"
 
@@ -286,6 +287,317 @@ __global__ void k_frame_ends(int32_t n, int32_t T, const int64_t *__restrict__ o
   if (f < n) frame_end[f] = offsets[(size_t)(f + 1) * T];
 }
 
+// ------------------------------------------------------- pixel-major blocks
+//
+// Series without stride or frame averaging (every raw frame is its own filter
+// frame, so a pixel never has two events of one frame): a run of at most
+// 65,536 frames goes straight to pixel-major rows, one block of the series'
+// block store, with no frame-major stream and no transpose.
+//   count   each pixel's kept frames per slice of the run;
+//   prefix  per pixel, the slice counts become offsets within its row; the
+//           rows are padded to whole 32-byte sectors (8 entries) and a scan
+//           over the pixels places them in the block;
+//   write   each lane appends its 8 pixels' kept frames as packed words
+//           ((frame - run start) << 16 | raw value) to per-pixel sectors in
+//           shared memory and stores every completed sector as one aligned
+//           32-byte write.  Only completed sectors reach memory, so no partly
+//           written line waits in L2 for the rest of its row (every pixel's
+//           row grows at once: their open lines would not fit in L2).
+//   gather  (when the series finishes) one warp per pixel reads its packed
+//           rows of every block and forms the values with the pixel's dark
+//           level and gain held in registers, as the reference forms them.
+// A row's events come out in frame order, the order a stable transpose of the
+// frame-major stream gives them, so the event lists are the same bit for bit.
+
+// counts[y * P + p] = kept frames of pixel p in slice y of the run.
+__global__ void __launch_bounds__(KB_WARPS * 32)
+k_dense_count_px(ChunkCfg c, int32_t *__restrict__ counts) {
+  constexpr int FU = 2 * KB_FU;  // frames in flight: the count pass is load-bound
+  const int lane = threadIdx.x & 31;
+  const int t = blockIdx.x * KB_WARPS + (threadIdx.x >> 5);
+  if (t >= c.T) return;
+  const int p0 = t * KB_WPIX + lane * KB_LPIX;
+  int32_t rm[KB_LPIX], k[KB_LPIX];
+#pragma unroll
+  for (int j = 0; j < KB_LPIX; j++) {
+    rm[j] = p0 + j < c.P ? c.rmin[p0 + j] : KB_NEVER;
+    k[j] = 0;
+  }
+  // every raw frame is its own filter frame: frames from F on are not used
+  const int f0 = blockIdx.y * c.fslice, f1 = min(min(c.n, f0 + c.fslice), c.F - c.r0);
+  for (int fb = f0; fb < f1; fb += FU) {
+    uint4 x[FU];
+    bool used[FU];
+#pragma unroll
+    for (int u = 0; u < FU; u++) {
+      used[u] = fb + u < f1;
+      if (used[u]) x[u] = load8(c, fb + u, p0);
+    }
+#pragma unroll
+    for (int u = 0; u < FU; u++) {
+      if (used[u]) {
+#pragma unroll
+        for (int j = 0; j < KB_LPIX; j++) k[j] += raw_at(x[u], j) >= rm[j] ? 1 : 0;
+      }
+    }
+  }
+  int32_t *dst = counts + (size_t)blockIdx.y * c.P + p0;
+  if (c.vec && p0 + KB_LPIX <= c.P) {  // P % 8 == 0: 32-byte aligned
+    ((int4 *)dst)[0] = make_int4(k[0], k[1], k[2], k[3]);
+    ((int4 *)dst)[1] = make_int4(k[4], k[5], k[6], k[7]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < KB_LPIX; j++)
+      if (p0 + j < c.P) dst[j] = k[j];
+  }
+}
+
+constexpr int KB_SECTOR = 8;  // packed 4-byte entries per 32-byte sector
+
+// Per pixel: its slice counts become exclusive offsets within its row of the
+// block; len[p] = the row's length, padded[p] = the length rounded up to
+// whole sectors (the row's room in the block); *sum += the lengths.
+__global__ void k_dense_prefix_px(int32_t P, int32_t ns, int32_t *__restrict__ counts,
+                                  int32_t *__restrict__ padded, int32_t *__restrict__ len,
+                                  unsigned long long *__restrict__ sum) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p - (int)(threadIdx.x & 31) >= P) return;  // whole warp past the end
+  int32_t run = 0;
+  if (p < P) {
+    for (int y = 0; y < ns; y++) {
+      int32_t *c = counts + (size_t)y * P + p;
+      const int32_t k = *c;
+      *c = run;
+      run += k;
+    }
+    len[p] = run;
+    padded[p] = (run + KB_SECTOR - 1) & ~(KB_SECTOR - 1);
+  }
+  const unsigned w = __reduce_add_sync(0xffffffffu, (unsigned)run);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(sum, (unsigned long long)w);
+}
+
+// Shared memory of the write pass, per warp: one open sector (8 entries) for
+// each of its 256 pixels, laid out [pixel j of the lane][slot][lane] so that
+// the lanes' stores of one j fall in distinct banks, then each pixel's next
+// entry in the block, [j][lane].  Every word is private to its lane: shared
+// memory serves as storage that a lane can index by the pixel it is on.
+constexpr size_t KB_PX_SMEM = (size_t)KB_WARPS * KB_WPIX * (KB_SECTOR + 1) * 4;
+
+// Stores entries [lo, hi) of the open sector of the lane's pixel j at sector
+// address dst (32-byte aligned): the whole sector at once when lo = 0 and
+// hi = 8, else entry by entry (the first sector of a run that starts inside
+// it, shared with the previous slice, and the last, partly filled one).
+__device__ __forceinline__ void px_flush(const uint32_t *stg, int j, int lane, uint32_t *dst,
+                                         int lo, int hi) {
+  const uint32_t *q = stg + (size_t)j * KB_SECTOR * 32 + lane;
+  if (lo == 0 && hi == KB_SECTOR) {
+    const uint4 a = make_uint4(q[0], q[32], q[64], q[96]);
+    const uint4 b = make_uint4(q[128], q[160], q[192], q[224]);
+    ((uint4 *)dst)[0] = a;
+    ((uint4 *)dst)[1] = b;
+  } else {
+    for (int e = lo; e < hi; e++) dst[e] = q[e * 32];
+  }
+}
+
+// rp: the rows' starts in the block ([P + 1], from the scan of the padded
+// lengths), pre: each (slice, pixel) run's offset within its row, out: the
+// block's packed entries.  The slice-0 blocks also record each row's start.
+// A lane visits only the kept pixels of each frame (7 % of them on a CCD at
+// 0.02 photons/pixel/frame): their bits come from one compare per pixel, and
+// the pixel index of a kept bit addresses the lane's shared-memory words.
+__global__ void __launch_bounds__(KB_WARPS * 32, 3)
+k_dense_write_px(ChunkCfg c, const int32_t *__restrict__ pre, const int64_t *__restrict__ rp,
+                 uint32_t *__restrict__ out, int32_t *__restrict__ blk_off) {
+  extern __shared__ __align__(16) uint32_t px_stg[];
+  constexpr int FU = 2 * KB_FU;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = blockIdx.x * KB_WARPS + w;
+  if (t >= c.T) return;
+  uint32_t *stg = px_stg + (size_t)w * KB_WPIX * KB_SECTOR;
+  int32_t *so = (int32_t *)(px_stg + (size_t)KB_WARPS * KB_WPIX * KB_SECTOR) +
+                (size_t)w * KB_WPIX + lane;  // so[j * 32]: pixel j's next entry
+  const int p0 = t * KB_WPIX + lane * KB_LPIX;
+  const int32_t *pre_y = pre + (size_t)blockIdx.y * c.P;
+  int32_t rm[KB_LPIX];
+  uint32_t first = 0;  // 3 bits per pixel: where its run starts in its first sector
+#pragma unroll
+  for (int j = 0; j < KB_LPIX; j++) {
+    const int p = p0 + j;
+    int32_t o = 0;
+    if (p < c.P) {
+      rm[j] = c.rmin[p];
+      const int64_t r = rp[p];
+      o = (int32_t)r + pre_y[p];
+      if (blockIdx.y == 0) blk_off[p] = (int32_t)r;
+    } else {
+      rm[j] = KB_NEVER;
+    }
+    so[j * 32] = o;
+    first |= (uint32_t)(o & (KB_SECTOR - 1)) << (3 * j);
+  }
+  uint32_t open_first = (1u << KB_LPIX) - 1u;  // bit j: pixel j's open sector is its run's first
+  // every raw frame is its own filter frame: frames from F on are not used
+  const int f0 = blockIdx.y * c.fslice, f1 = min(min(c.n, f0 + c.fslice), c.F - c.r0);
+  for (int fb = f0; fb < f1; fb += FU) {
+    uint4 x[FU];
+    bool used[FU];
+#pragma unroll
+    for (int u = 0; u < FU; u++) {
+      used[u] = fb + u < f1;
+      if (used[u]) x[u] = load8(c, fb + u, p0);
+    }
+#pragma unroll
+    for (int u = 0; u < FU; u++) {
+      unsigned m = used[u] ? keep_mask(x[u], rm) : 0u;
+      const uint32_t fr = (uint32_t)(fb + u) << 16;
+      while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1u;
+        const int32_t raw = raw_at(x[u], j);
+        const int32_t o = so[j * 32];
+        const int slot = o & (KB_SECTOR - 1);
+        stg[(j * KB_SECTOR + slot) * 32 + lane] = fr | (uint32_t)(raw & 0xffff);
+        so[j * 32] = o + 1;
+        if (slot == KB_SECTOR - 1) {
+          const int lo = ((open_first >> j) & 1u) ? (int)((first >> (3 * j)) & 7u) : 0;
+          px_flush(stg, j, lane, out + (o + 1 - KB_SECTOR), lo, KB_SECTOR);
+          open_first &= ~(1u << j);
+        }
+      }
+    }
+  }
+  // the last, partly filled sector of every run
+#pragma unroll
+  for (int j = 0; j < KB_LPIX; j++) {
+    const int32_t o = so[j * 32];
+    const int hi = o & (KB_SECTOR - 1);
+    if (hi != 0) {
+      const int lo = ((open_first >> j) & 1u) ? (int)((first >> (3 * j)) & 7u) : 0;
+      px_flush(stg, j, lane, out + (o - hi), lo, hi);
+    }
+  }
+}
+
+// Per pixel: its row length summed over the blocks.
+__global__ void k_px_totals(int32_t P, int32_t nblk, const int32_t *__restrict__ blk_len,
+                            int32_t *__restrict__ tot) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  int32_t t = 0;
+  for (int32_t k = 0; k < nblk; k++) t += blk_len[(size_t)k * P + p];
+  tot[p] = t;
+}
+
+constexpr int KB_VT = 128;  // raw values from a pixel's threshold up in its value table
+
+struct PxGather {
+  int32_t P, F, tcap, force_float, nblk, has_dark;
+  const int64_t *blk_base;
+  const int32_t *blk_r0, *blk_off, *blk_len;
+  const uint32_t *pk;
+  const int64_t *row_ptr;
+  const uint8_t *mask;
+  const int32_t *rmin;
+  const double *avg, *flat;
+  const DensePrep *prep;
+  int32_t *fr;
+  float *val;
+  int32_t *row_len;
+  uint8_t *pclass;
+  ClassLists cl;
+  DevStats *stats;
+};
+
+// One block per 32 pixels, each warp taking 4 of them in turn: a pixel's
+// packed entries of every block, in block order, become (frame, value) in its
+// row of the event lists.  For a given pixel the value is a function of the
+// raw value alone: the warp first forms it, as the frame-major write does,
+// for the 128 raw values from the pixel's threshold up (where nearly all kept
+// values lie) and looks those up; others are formed directly.  The row's
+// length, whether every value is an integer and sum |v| are collected on the
+// way, and the block's first warp classifies the 32 pixels as the merge pass
+// does for transposed rows (no row has two events of one frame here).
+__global__ void __launch_bounds__(256)
+k_dense_gather_px(PxGather g) {
+  __shared__ float s_tab[KB_WARPS][KB_VT];
+  __shared__ int32_t s_n[32], s_nonint[32];
+  __shared__ long long s_tot[32];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int pb = blockIdx.x * 32;
+  for (int q = 0; q < 32 / KB_WARPS; q++) {
+    const int loc = q * KB_WARPS + w, p = pb + loc;
+    if (p >= g.P) break;
+    const int32_t rlo = g.rmin[p];
+    int32_t n = 0;
+    bool nonint = false;
+    long long tot = 0;
+    if (rlo < KB_NEVER) {
+      for (int i = lane; i < KB_VT; i += 32)
+        s_tab[w][i] = rlo + i <= 32767
+                          ? dense_event_value(rlo + i, g.has_dark, g.avg, g.flat, g.prep, p)
+                          : 0.f;
+      __syncwarp();
+      int64_t d = g.row_ptr[p];
+      for (int32_t k = 0; k < g.nblk; k++) {
+        const int32_t nk = g.blk_len[(size_t)k * g.P + p];
+        const int64_t src = g.blk_base[k] + g.blk_off[(size_t)k * g.P + p];
+        const int32_t r0 = g.blk_r0[k];
+        // four 32-entry chunks' loads in flight before any is used
+        for (int32_t i0 = 0; i0 < nk; i0 += 4 * 32) {
+          uint32_t e[4];
+#pragma unroll
+          for (int h = 0; h < 4; h++) {
+            const int32_t i = i0 + h * 32 + lane;
+            e[h] = i < nk ? __ldcs(g.pk + src + i) : 0u;
+          }
+#pragma unroll
+          for (int h = 0; h < 4; h++) {
+            if (i0 + h * 32 >= nk) break;  // the same for every lane
+            const int32_t i = i0 + h * 32 + lane;
+            bool ni = false;
+            unsigned a = 0;
+            if (i < nk) {
+              const int32_t raw = (int16_t)(e[h] & 0xffffu);
+              const int32_t t = raw - rlo;  // >= 0: kept values pass the threshold
+              const float v = t < KB_VT ? s_tab[w][t]
+                                        : dense_event_value(raw, g.has_dark, g.avg, g.flat,
+                                                            g.prep, p);
+              g.fr[d + i] = r0 + (int32_t)(e[h] >> 16);
+              g.val[d + i] = v;
+              ni = !(v == truncf(v) && fabsf(v) < 16777216.f);
+              a = ni ? 0u : (unsigned)fabsf(v);
+            }
+            nonint = nonint || __any_sync(FULL, ni);
+            tot += __reduce_add_sync(FULL, a);
+          }
+        }
+        d += nk;
+        n += nk;
+      }
+      __syncwarp();  // the table is rebuilt for the warp's next pixel
+    }
+    if (lane == 0) {
+      s_n[loc] = n;
+      s_nonint[loc] = nonint ? 1 : 0;
+      s_tot[loc] = tot;
+      g.row_len[p] = n;
+    }
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int p = pb + lane;
+    const bool has = p < g.P;
+    const int32_t n = has ? s_n[lane] : 0;
+    uint8_t c = has && g.mask[p] ? pixel_class(n, s_nonint[lane] == 0, s_tot[lane], g.F, g.tcap)
+                                 : (uint8_t)PCLASS_EMPTY;
+    if (g.force_float && c != PCLASS_EMPTY) c = PCLASS_FLOAT;  // values rescaled later
+    record_class_warp(has, p, c, n, g.pclass, g.cl, g.stats);
+  }
+}
+
 }  // namespace
 
 void dense_set_dark(Series &s, const int16_t *dark_host, int32_t nd) {
@@ -314,10 +626,170 @@ void dense_set_dark(Series &s, const int16_t *dark_host, int32_t nd) {
   s.rmin_ready = true;
 }
 
+namespace {
+
+// Raw frames r0 .. r0+n-1, at raw on the device, as the next block of the
+// block store; runs longer than 65,536 frames (the packed frame field), or
+// whose padded rows would not fit the block's 32-bit row offsets, are split
+// in halves (one frame holds at most P < 2^31 events).
+void dense_px_block(Series &s, const int16_t *raw, int32_t n, int32_t r0) {
+  if (n <= 0) return;
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P, T = (P + KB_WPIX - 1) / KB_WPIX;
+  if (n > 65536) {
+    const int32_t h = n / 2;
+    dense_px_block(s, raw, h, r0);
+    dense_px_block(s, raw + (size_t)h * P, n - h, r0 + h);
+    return;
+  }
+  int sms = 0;
+  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device));
+  const int gx = (T + KB_WARPS - 1) / KB_WARPS;
+  // slices of at least 64 frames, enough of them for 4 blocks per SM
+  const int want = std::max(1, std::min((n + 63) / 64, (4 * sms + gx - 1) / gx));
+  const int fslice = (n + want - 1) / want;
+  const int ns = (n + fslice - 1) / fslice;
+  const int vec = (P % KB_LPIX == 0) && ((uintptr_t)raw % 16 == 0);
+  ChunkCfg c{raw, n, P, T, r0, s.R_in, s.desc.stride_frames, s.F, vec, fslice, s.rmin.p};
+  const size_t k = s.blk_base.size();
+  s.dn_counts.reserve((size_t)ns * P, st);
+  s.dn_tot.reserve(P, st);
+  s.blk_rp.reserve((size_t)P + 1, st);
+  s.scan_tmp.reserve(scan_workspace_bytes(P), st);
+  s.blk_off.grow((k + 1) * (size_t)P, k * (size_t)P, st);
+  s.blk_len.grow((k + 1) * (size_t)P, k * (size_t)P, st);
+  const dim3 grid(gx, ns);
+  k_dense_count_px<<<grid, KB_WARPS * 32, 0, st>>>(c, s.dn_counts.p);
+  XG_CHECK_LAUNCH();
+  s.dn_sum.reserve(1, st);
+  XG_CUDA(cudaMemsetAsync(s.dn_sum.p, 0, sizeof(unsigned long long), st));
+  k_dense_prefix_px<<<(P + 255) / 256, 256, 0, st>>>(P, ns, s.dn_counts.p, s.dn_tot.p,
+                                                      s.blk_len.p + k * P, s.dn_sum.p);
+  XG_CHECK_LAUNCH();
+  exclusive_scan_i32_i64(s.dn_tot.p, s.blk_rp.p, P, s.scan_tmp.p, st);
+  int64_t total = 0;  // padded entries of the block
+  unsigned long long events = 0;
+  XG_CUDA(cudaMemcpyAsync(&total, s.blk_rp.p + P, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  XG_CUDA(cudaMemcpyAsync(&events, s.dn_sum.p, sizeof(events), cudaMemcpyDeviceToHost, st));
+  XG_CUDA(cudaStreamSynchronize(st));
+  if (total > (int64_t)INT32_MAX) {
+    const int32_t h = n / 2;
+    dense_px_block(s, raw, h, r0);
+    dense_px_block(s, raw + (size_t)h * P, n - h, r0 + h);
+    return;
+  }
+  // sector-aligned block start: rows and their sectors are 32-byte aligned
+  const int64_t base = s.blk_events;
+  s.blk_pk.grow((size_t)(base + std::max<int64_t>(total, KB_SECTOR)), (size_t)base, st);
+  XG_CUDA(cudaFuncSetAttribute(k_dense_write_px, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)KB_PX_SMEM));
+  k_dense_write_px<<<grid, KB_WARPS * 32, KB_PX_SMEM, st>>>(c, s.dn_counts.p, s.blk_rp.p,
+                                                          s.blk_pk.p + base, s.blk_off.p + k * P);
+  XG_CHECK_LAUNCH();
+  s.blk_base.push_back(base);
+  s.blk_r0.push_back(r0);
+  // the device copies of the block tables are kept current here, so that
+  // finishing the series (graph-captured in batches) uploads nothing
+  s.d_blk_base.grow(k + 1, k, st);
+  s.d_blk_r0.grow(k + 1, k, st);
+  XG_CUDA(cudaMemcpyAsync(s.d_blk_base.p + k, &s.blk_base[k], sizeof(int64_t),
+                          cudaMemcpyHostToDevice, st));
+  XG_CUDA(cudaMemcpyAsync(s.d_blk_r0.p + k, &s.blk_r0[k], sizeof(int32_t),
+                          cudaMemcpyHostToDevice, st));
+  s.blk_events = base + total;  // a multiple of KB_SECTOR
+  s.blk_raw_done = r0 + n;
+  s.raw_events += (int64_t)events;
+  if (s.raw_events >= ((int64_t)1 << 32))
+    throw Error(XPCS_ERR_INVALID_ARGUMENT, "more than 2^32 events in one series");
+}
+
+// Frames per block of the pixel-major form: runs shorter than this wait in the
+// pending buffer, so that each block's per-pixel tables (8 B per pixel) stay
+// small beside its events.
+int32_t px_block_frames(int32_t P) {
+  return (int32_t)std::max<int64_t>(1, std::min<int64_t>(256, (512ll << 20) / (2ll * P)));
+}
+
+void dense_px_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_device) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P, bf = px_block_frames(P);
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  DBuf<int16_t> staging;
+  int32_t f = 0;
+  while (f < nframes) {
+    const int32_t left = nframes - f;
+    const int16_t *src = frames + (size_t)f * P;
+    if (s.dn_pend_n == 0 && left >= bf) {
+      // a long run: straight to blocks (host frames through a staging buffer
+      // of up to 1 GB)
+      int32_t m = left;
+      const int16_t *raw = src;
+      if (!on_device) {
+        m = (int32_t)std::min<int64_t>(left, std::max<int64_t>(bf, (1ll << 30) / (2ll * P)));
+        staging.reserve((size_t)m * P, st);
+        XG_CUDA(cudaMemcpyAsync(staging.p, src, sizeof(int16_t) * (size_t)m * P,
+                                cudaMemcpyHostToDevice, st));
+        raw = staging.p;
+      }
+      dense_px_block(s, raw, m, s.raw_frames);
+      s.raw_frames += m;
+      f += m;
+    } else {
+      // a short run waits for more frames
+      const int32_t m = std::min(left, bf - s.dn_pend_n);
+      s.dn_pend.reserve((size_t)bf * P, st);
+      if (s.dn_pend_n == 0) s.dn_pend_r0 = s.raw_frames;
+      XG_CUDA(cudaMemcpyAsync(s.dn_pend.p + (size_t)s.dn_pend_n * P, src,
+                              sizeof(int16_t) * (size_t)m * P, kind, st));
+      s.dn_pend_n += m;
+      s.raw_frames += m;
+      f += m;
+      if (s.dn_pend_n == bf) dense_px_flush(s);
+    }
+  }
+  // host frames: the copies are done before the staging buffer goes back
+  if (!on_device) XG_CUDA(cudaStreamSynchronize(st));
+  staging.release(st);
+}
+
+}  // namespace
+
+void dense_px_flush(Series &s) {
+  if (!s.dense_px || s.dn_pend_n == 0) return;
+  const int32_t n = s.dn_pend_n;
+  s.dn_pend_n = 0;
+  dense_px_block(s, s.dn_pend.p, n, s.dn_pend_r0);
+}
+
+void dense_px_gather(Series &s) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P, nblk = (int32_t)s.blk_base.size();
+  s.blk_tot.reserve(P, st);
+  if (nblk > 0) {
+    k_px_totals<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.blk_len.p, s.blk_tot.p);
+    XG_CHECK_LAUNCH();
+  } else {
+    XG_CUDA(cudaMemsetAsync(s.blk_tot.p, 0, sizeof(int32_t) * (size_t)P, st));
+  }
+  exclusive_scan_i32_i64(s.blk_tot.p, s.row_ptr.p, P, s.scan_tmp.p, st);
+  PxGather g{P, s.F, s.thread_cap, s.desc.normalize_by_framesum, nblk, s.has_dark ? 1 : 0,
+             s.d_blk_base.p, s.d_blk_r0.p, s.blk_off.p, s.blk_len.p, s.blk_pk.p, s.row_ptr.p,
+             s.d_mask.p, s.rmin.p, s.dark_avg.p, s.has_flat ? s.d_flat.p : nullptr,
+             (const DensePrep *)s.dn_prep.p, s.ev_frame.p, s.ev_val.p, s.row_len.p, s.pclass.p,
+             ClassLists{s.wlist.p, s.llist.p, s.flist.p}, s.stats.p};
+  k_dense_gather_px<<<(P + 31) / 32, KB_WARPS * 32, 0, st>>>(g);
+  XG_CHECK_LAUNCH();
+}
+
 void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_device) {
   cudaStream_t st = s.stream;
   const int32_t P = s.P, T = (P + KB_WPIX - 1) / KB_WPIX;
   if (!s.rmin_ready) dense_set_dark(s, nullptr, 0);
+  if (s.dense_px) {
+    dense_px_ingest(s, frames, nframes, on_device);
+    s.have_multitau = false;
+    return;
+  }
   // frames per pass: host frames go through a 256 MB staging buffer; frames
   // already on the device are taken up to 4096 at a time (one host sync each)
   const int64_t by_bytes = std::max<int64_t>(1, (256ll << 20) / (2ll * P));

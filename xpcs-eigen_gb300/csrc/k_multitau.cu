@@ -826,17 +826,34 @@ __device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x)
   return first;
 }
 
-// entries tb .. tb+31 of the level's row into their ring slots, with their
-// findable flags
-__device__ __forceinline__ void fw_load_tile(int tb, int lane, int L, int n0, bool all_find,
-                                             const int32_t *idx, const float *val, int32_t *ridx,
-                                             float *rval, uint8_t *rfind) {
+// Entry tb + lane of the level's row with its findable flag, fetched into
+// registers (fw_fetch) some time before it goes into its ring slot (fw_put),
+// so that the load's latency passes while a tile is processed.
+struct FwEntry {
+  int32_t x;
+  float v;
+  uint8_t f;
+};
+
+__device__ __forceinline__ FwEntry fw_fetch(int tb, int lane, int L, int n0, bool all_find,
+                                            const int32_t *idx, const float *val) {
+  FwEntry e{0, 0.f, 0};
+  const int j = tb + lane;
+  if (j < L) {
+    e.x = idx[j];
+    e.v = val[j];
+    e.f = all_find ? 1 : (lower_bound_g(idx, n0, e.x) == j);
+  }
+  return e;
+}
+
+__device__ __forceinline__ void fw_put(int tb, int lane, int L, const FwEntry &e, int32_t *ridx,
+                                       float *rval, uint8_t *rfind) {
   const int j = tb + lane, slot = j & 63;
   if (j < L) {
-    const int32_t x = idx[j];
-    ridx[slot] = x;
-    rval[slot] = val[j];
-    rfind[slot] = all_find ? 1 : (lower_bound_g(idx, n0, x) == j);
+    ridx[slot] = e.x;
+    rval[slot] = e.v;
+    rfind[slot] = e.f;
   }
 }
 
@@ -876,11 +893,26 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
     const int n0 = row_len[p];
     int32_t *idx = sc_frame + b;
     float *val = sc_val + b;
-    for (int i = lane; i < n0; i += 32) {
-      const int32_t f = ev_frame[b + i];
-      idx[i] = f;
-      // normalize_by_framesum: v / (frameSum[f] / mean) (main.cpp:330-333)
-      val[i] = fscale ? __fdiv_rn(ev_val[b + i], fscale[f]) : ev_val[b + i];
+    for (int i0 = 0; i0 < n0; i0 += 4 * 32) {
+      int32_t f[4];
+      float x[4];
+#pragma unroll
+      for (int h = 0; h < 4; h++) {  // the loads first, in flight together
+        const int i = i0 + h * 32 + lane;
+        if (i < n0) {
+          f[h] = ev_frame[b + i];
+          x[h] = ev_val[b + i];
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 4; h++) {
+        const int i = i0 + h * 32 + lane;
+        if (i < n0) {
+          idx[i] = f[h];
+          // normalize_by_framesum: v / (frameSum[f] / mean) (main.cpp:330-333)
+          val[i] = fscale ? __fdiv_rn(x[h], fscale[f[h]]) : x[h];
+        }
+      }
     }
     __syncwarp();
     int L = n0;
@@ -897,20 +929,36 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
           dead = true;  // nothing is kept: lastIndex becomes 1 on a stale entry
         } else {
           int out = 0, carry_h = -1;
+          // chunks of 32 entries, each loaded two chunks ahead: a chunk's
+          // pass writes only below its own end, so the entries in flight
+          // are never overwritten before they are used
+          int32_t ia = lane < prevL ? idx[lane] : INT_MAX;
+          float va = lane < prevL ? val[lane] : 0.f;
+          int32_t ia1 = 32 + lane < prevL ? idx[32 + lane] : INT_MAX;
+          float va1 = 32 + lane < prevL ? val[32 + lane] : 0.f;
           for (int base = 0; base < prevL; base += 32) {
+            const int a2 = base + 64 + lane;
+            const int32_t ia2 = a2 < prevL ? idx[a2] : INT_MAX;
+            const float va2 = a2 < prevL ? val[a2] : 0.f;
             const int a = base + lane;
             const bool in = a < prevL;
-            const int32_t ia = in ? idx[a] : INT_MAX;
-            const float va = in ? val[a] : 0.f;
             const bool has_b = a + 1 < prevL;
-            const int32_t ib = has_b ? idx[a + 1] : INT_MAX;
+            // the next entry: the lane above's, or the next chunk's first
+            int32_t ib = __shfl_down_sync(0xffffffffu, ia, 1);
+            float vb = __shfl_down_sync(0xffffffffu, va, 1);
+            const int32_t ib1 = __shfl_sync(0xffffffffu, ia1, 0);
+            const float vb1 = __shfl_sync(0xffffffffu, va1, 0);
+            if (lane == 31) {
+              ib = ib1;
+              vb = vb1;
+            }
             const int h = ia >> 1, hb = ib >> 1;
             int hp = __shfl_up_sync(0xffffffffu, h, 1);
             if (lane == 0) hp = carry_h;
             const bool keep = in && (a == 0 || h != hp) && h < lastframe;
             const bool merge = keep && has_b && hb == h;
             float sv = va;
-            if (merge) sv = __fadd_rn(va, val[a + 1]);
+            if (merge) sv = __fadd_rn(va, vb);
             sv = __fmul_rn(sv, 0.5f);  // == sv / 2 (exact scaling)
             const unsigned bal = __ballot_sync(0xffffffffu, keep);
             const bool stop = __any_sync(0xffffffffu, in && h >= lastframe);
@@ -924,6 +972,10 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
             out += __popc(bal);
             __syncwarp();
             if (stop) break;
+            ia = ia1;
+            va = va1;
+            ia1 = ia2;
+            va1 = va2;
           }
           L = out;
           tail_sorted = tail_sorted && (L >= prevL || junction_ok);
@@ -945,9 +997,11 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
       const int nchain = 3 * cnt;
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
       // ring slots past the row end are never read (partners stop at L)
-      fw_load_tile(0, lane, L, n0, all_find, idx, val, ridx, rval, rfind);
-      if (L > 32) fw_load_tile(32, lane, L, n0, all_find, idx, val, ridx, rval, rfind);
+      fw_put(0, lane, L, fw_fetch(0, lane, L, n0, all_find, idx, val), ridx, rval, rfind);
+      fw_put(32, lane, L, fw_fetch(32, lane, L, n0, all_find, idx, val), ridx, rval, rfind);
       for (int base = 0; base < L; base += 32) {
+        // the tile after next, in flight while this one is processed
+        const FwEntry nx = fw_fetch(base + 64, lane, L, n0, all_find, idx, val);
         __syncwarp();
         const int r = base + lane;
         const bool valid = r < L;
@@ -1028,7 +1082,7 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
         }
         __syncwarp();
         // the tile after next replaces this one in the ring
-        if (base + 64 < L) fw_load_tile(base + 64, lane, L, n0, all_find, idx, val, ridx, rval, rfind);
+        fw_put(base + 64, lane, L, nx, ridx, rval, rfind);
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {

@@ -13,7 +13,8 @@
 // (rows are in frame order); the event lists are stably re-sorted by frame
 // (giving frame-major, pixel-ascending order), summed per frame, then stably
 // re-sorted by static bin (keeping that order inside each bin) and summed per
-// bin and per (window, bin).
+// bin and per (window, bin).  Pixel-major dense series, whose finishing pass
+// skips the pixel sums, get them here from their rows.
 #include <vector>
 
 #include "xpcs_internal.h"
@@ -118,6 +119,19 @@ __global__ void k_part_partial(int32_t S, int32_t nwin, int32_t sw, int64_t n,
   partial[(size_t)w * S + sb] = __fdiv_rn(acc, den);
 }
 
+// pixels_sum_[pix] += v over a row in frame order, for rows whose finishing
+// pass does not form the sums (pixel-major dense series).
+__global__ void k_row_sums(int32_t P, const int64_t *__restrict__ row_ptr,
+                           const int32_t *__restrict__ row_len, const float *__restrict__ val,
+                           float *__restrict__ ps) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int64_t b = row_ptr[p];
+  float a = 0.f;
+  for (int32_t i = 0; i < row_len[p]; i++) a = __fadd_rn(a, val[b + i]);
+  ps[p] = a;
+}
+
 __global__ void k_pixel_sums(int32_t P, int32_t F, const float *__restrict__ ps,
                              float *__restrict__ out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -141,6 +155,11 @@ void run_side_stats(Series &s, const SideOut &out) {
         *d_part = d_tot + S;
   XG_CUDA(cudaMemsetAsync(s.side_out.p, 0, sizeof(float) * nout, st));
   const int bs = 256;
+  if (s.dense_px) {
+    k_row_sums<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.row_ptr.p, s.row_len.p, s.ev_val.p,
+                                                  s.pixels_sum.p);
+    XG_CHECK_LAUNCH();
+  }
   k_pixel_sums<<<(P + bs - 1) / bs, bs, 0, st>>>(P, F, s.pixels_sum.p, d_pix);
   XG_CHECK_LAUNCH();
   if (n > 0) {

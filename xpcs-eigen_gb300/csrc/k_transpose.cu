@@ -25,6 +25,7 @@
 #include <cstddef>
 
 #include "f64emu.cuh"
+#include "classify.cuh"
 #include "xpcs_internal.h"
 
 namespace xg {
@@ -371,45 +372,6 @@ __global__ void k_row_ptr(const uint32_t *__restrict__ keys, int64_t n,
     }
   }
   row_ptr[p] = first;
-}
-
-// Work lists of the multi-tau kernels (pixel indices per class).
-struct ClassLists {
-  int32_t *wlist, *llist, *flist;
-};
-
-// Classification of the pixels of one warp (all 32 lanes call it; lanes
-// without a pixel pass has = false): pclass, the float/warp work lists and the
-// counters, one atomic per warp and counter.
-__device__ __forceinline__ void record_class_warp(bool has, int32_t p, uint8_t c, int32_t n,
-                                                  uint8_t *pclass, const ClassLists &cl,
-                                                  DevStats *stats) {
-  const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-  if (has) pclass[p] = c;
-  const bool live = has && c != PCLASS_EMPTY;
-  const unsigned mv = __ballot_sync(FULL, live);
-  const unsigned mw = __ballot_sync(FULL, live && c == PCLASS_WARP);
-  const unsigned ml = __ballot_sync(FULL, live && c == PCLASS_LONG);
-  const unsigned mf = __ballot_sync(FULL, live && c == PCLASS_FLOAT);
-  const unsigned ev = __reduce_add_sync(FULL, live ? (unsigned)n : 0u);
-  int bw = 0, bl = 0, bf = 0;
-  if (lane == 0) {
-    if (mv) {
-      atomicAdd(&stats->nvalid, __popc(mv));
-      atomicAdd(&stats->events, (unsigned long long)ev);
-    }
-    if (mw) bw = atomicAdd(&stats->nwarp, __popc(mw));
-    if (ml) bl = atomicAdd(&stats->nlong, __popc(ml));
-    if (mf) bf = atomicAdd(&stats->nfloat, __popc(mf));
-  }
-  bw = __shfl_sync(FULL, bw, 0);
-  bl = __shfl_sync(FULL, bl, 0);
-  bf = __shfl_sync(FULL, bf, 0);
-  if (live && c == PCLASS_WARP) cl.wlist[bw + __popc(mw & lt)] = p;
-  if (live && c == PCLASS_LONG) cl.llist[bl + __popc(ml & lt)] = p;
-  if (live && c == PCLASS_FLOAT) cl.flist[bf + __popc(mf & lt)] = p;
 }
 
 // Per-lane merge of one pixel's row: events of the same filter frame summed in
@@ -837,6 +799,27 @@ __global__ void k_gather_blocks(int32_t P, int32_t nblk, const int64_t *__restri
   }
 }
 
+// Every pixel's block segments gathered into its row of the series' event
+// lists (d_blk_base on the device already), then classified (the rows are
+// merged already: avg 1 leaves nothing to merge).
+void gather_blocks(Series &s) {
+  cudaStream_t st = s.stream;
+  const int32_t P = s.P, nblk = (int32_t)s.blk_base.size();
+  s.blk_tot.reserve(P, st);
+  if (nblk > 0) {
+    k_block_totals<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.blk_len.p, s.blk_tot.p);
+    XG_CHECK_LAUNCH();
+    exclusive_scan_i32_i64(s.blk_tot.p, s.row_ptr.p, P, s.scan_tmp.p, st);
+    k_gather_blocks<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.d_blk_base.p, s.blk_off.p,
+                                                     s.blk_len.p, s.blk_fr.p, s.blk_val.p,
+                                                     s.row_ptr.p, s.ev_frame.p, s.ev_val.p);
+    XG_CHECK_LAUNCH();
+  } else {
+    XG_CUDA(cudaMemsetAsync(s.row_ptr.p, 0, sizeof(int64_t) * ((size_t)P + 1), st));
+  }
+  merge_classify(s, 1);
+}
+
 // Transposes the next block, ending at raw frame r1, into the block store.
 void transpose_block(Series &s, int32_t r1) {
   cudaStream_t st = s.stream;
@@ -863,7 +846,8 @@ void transpose_block(Series &s, int32_t r1) {
 }  // namespace
 
 void transpose_ready_blocks(Series &s) {
-  if (s.block_frames <= 0) return;
+  // pixel-major dense series write their blocks as frames arrive
+  if (s.block_frames <= 0 || s.dense_px) return;
   const int32_t step = s.block_frames * s.R_in;
   // raw frames past the series' last filter frame are never used
   const int32_t limit = std::min<int64_t>(s.raw_frames, (int64_t)s.F * s.R_in);
@@ -877,17 +861,26 @@ void transpose_ready_blocks(Series &s) {
 
 void reset_blocks(Series &s) {
   s.blk_base.clear();
+  s.blk_r0.clear();
   s.blk_events = 0;
   s.blk_raw_done = 0;
+  s.dn_pend_n = 0;
 }
 
 void run_filter_transpose(Series &s) {
   cudaStream_t st = s.stream;
   const int32_t P = s.P;
+  dense_px_flush(s);  // frames still pending become the last block
   reserve_lists(s);
   const size_t nalloc = s.raw_events > 0 ? (size_t)s.raw_events : 1;
   s.ev_frame.reserve(nalloc, st);
   s.ev_val.reserve(nalloc, st);
+  s.scan_tmp.reserve(scan_workspace_bytes(P), st);
+  if (s.dense_px) {
+    XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
+    dense_px_gather(s);  // gathers and classifies
+    return;
+  }
   if (s.block_frames <= 0) {
     XG_CUDA(cudaMemsetAsync(s.stats.p, 0, sizeof(DevStats), st));
     upload_frame_tables(s);
@@ -904,23 +897,11 @@ void run_filter_transpose(Series &s) {
   upload_frame_tables(s);
   if (s.blk_raw_done < s.raw_frames) transpose_block(s, s.raw_frames);  // the last block
   const int32_t nblk = (int32_t)s.blk_base.size();
-  s.blk_tot.reserve(P, st);
   s.d_blk_base.reserve((size_t)std::max(nblk, 1), st);
-  if (nblk > 0) {
+  if (nblk > 0)
     XG_CUDA(cudaMemcpyAsync(s.d_blk_base.p, s.blk_base.data(), sizeof(int64_t) * nblk,
                             cudaMemcpyHostToDevice, st));
-    k_block_totals<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.blk_len.p, s.blk_tot.p);
-    XG_CHECK_LAUNCH();
-    exclusive_scan_i32_i64(s.blk_tot.p, s.row_ptr.p, P, s.scan_tmp.p, st);
-    k_gather_blocks<<<(P + 255) / 256, 256, 0, st>>>(P, nblk, s.d_blk_base.p, s.blk_off.p,
-                                                     s.blk_len.p, s.blk_fr.p, s.blk_val.p,
-                                                     s.row_ptr.p, s.ev_frame.p, s.ev_val.p);
-    XG_CHECK_LAUNCH();
-  } else {
-    XG_CUDA(cudaMemsetAsync(s.row_ptr.p, 0, sizeof(int64_t) * ((size_t)P + 1), st));
-  }
-  // the rows are merged already: classify them (avg 1: nothing left to merge)
-  merge_classify(s, 1);
+  gather_blocks(s);
 }
 
 }  // namespace xg

@@ -250,6 +250,17 @@ struct Series {
   DBuf<int64_t> dn_offsets;
   DBuf<int64_t> dn_frame_end;
   DBuf<uint8_t> dn_prep;  // per pixel: EmuSubPrep of the dark level, EmuMulPrep of the gain
+  // dense series without stride or averaging: the filter writes pixel-major
+  // blocks of the block store directly; the frames of small ingests wait in
+  // dn_pend (raw frames dn_pend_r0 .. +dn_pend_n) until a block's worth is there
+  bool dense_px = false;
+  DBuf<int16_t> dn_pend;
+  int32_t dn_pend_n = 0, dn_pend_r0 = 0;
+  DBuf<int32_t> dn_tot;  // per-pixel padded row lengths of the block being written
+  DBuf<unsigned long long> dn_sum;  // kept events of the block being written
+  DBuf<uint32_t> blk_pk;  // their block store: (frame - block start) << 16 | raw value
+  std::vector<int32_t> blk_r0;  // first raw frame of every block
+  DBuf<int32_t> d_blk_r0;
 
   // transpose / event lists
   DBuf<uint32_t> keyA, keyB;
@@ -446,6 +457,8 @@ void get_twotime(Series &s, int32_t *qbins, float *sg, float *c2t, float *g2full
 // Dense frames (k_dense.cu)
 void dense_set_dark(Series &s, const int16_t *dark_host, int32_t ndark);
 void dense_ingest(Series &s, const int16_t *frames, int32_t nframes, bool on_device);
+void dense_px_flush(Series &s);  // pending frames of a pixel-major dense series -> a block
+void dense_px_gather(Series &s);  // its blocks -> the event lists and row_ptr
 void dense_get_dark(Series &s, double *avg, double *sd);
 
 // Upload caller-held pixel-major rows and classify their pixels (xpcs_multitau2)
