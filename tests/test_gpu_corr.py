@@ -1,7 +1,9 @@
 """The C++ `corr` driver end to end: for every golden case the IMM frames and
 the analysis file are rebuilt from the fixture's inputs, `corr --g2out
 --darkout` runs on them, and every dataset it writes must be bit-identical to
-what the reference's own `corr` wrote for the same inputs."""
+what the reference's own `corr` wrote for the same inputs.  The analysis file
+is an HDF5 file (written into, as the reference does, and read back with the
+independent walk of tests/h5walk.py) or the XH5C container."""
 import subprocess
 from pathlib import Path
 
@@ -9,8 +11,27 @@ import numpy as np
 import pytest
 
 import build
+import h5walk
 import refio
 from fixtures import CASES, TWOTIME_CASES, load, load_twotime, same_bits_nan
+
+FORMATS = ["hdf5", "xh5c"]
+
+
+def _as_format(cfg: Path, fmt: str) -> Path:
+    """The analysis file in the given format (the XH5C file converted)."""
+    if fmt == "xh5c":
+        return cfg
+    h5 = cfg.with_suffix(".hdf5.h5")
+    r = subprocess.run([str(build.build_h5tool()), "from-xh5c", str(cfg), str(h5)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    return h5
+
+
+def _exchange(cfg: Path, fmt: str) -> dict:
+    sets = h5walk.read(cfg) if fmt == "hdf5" else refio.read_xh5c(cfg)
+    return {k.split("/")[-1]: v for k, v in sets.items() if k.startswith("/exchange/")}
 
 DATASETS = ["G2", "IP", "IF", "norm-0-g2", "norm-0-stderr", "pixelSum", "frameSum",
             "partition-mean-total", "partition-mean-partial", "timestamp_clock",
@@ -46,14 +67,15 @@ def corr():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("fmt", FORMATS)
 @pytest.mark.parametrize("case", CASES)
-def test_corr_matches_reference_outputs(corr, case, tmp_path):
+def test_corr_matches_reference_outputs(corr, case, fmt, tmp_path):
     fx = load(case)
-    cfg = _write_inputs(fx, tmp_path)
+    cfg = _as_format(_write_inputs(fx, tmp_path), fmt)
     r = subprocess.run([str(corr), str(cfg), "--g2out", "--darkout"], cwd=tmp_path,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
-    out = {k.split("/")[-1]: v for k, v in refio.read_xh5c(cfg).items() if k.startswith("/exchange/")}
+    out = _exchange(cfg, fmt)
     for name in DATASETS:
         ref = fx["ref_" + name.replace("-", "_")]
         assert name in out, name
@@ -64,8 +86,9 @@ def test_corr_matches_reference_outputs(corr, case, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("fmt", FORMATS)
 @pytest.mark.parametrize("case", TWOTIME_CASES)
-def test_corr_twotime_matches_reference_outputs(corr, case, tmp_path):
+def test_corr_twotime_matches_reference_outputs(corr, case, fmt, tmp_path):
     fx = load_twotime(case)
     imm = tmp_path / "frames.imm"
     refio.write_imm_sparse(imm, fx["H"], fx["W"], fx["nnz"], fx["idx"], fx["val"])
@@ -74,10 +97,11 @@ def test_corr_twotime_matches_reference_outputs(corr, case, tmp_path):
     cfg = tmp_path / "analysis.h5"
     refio.write_xh5c(cfg, refio.config_entries(fx["W"], fx["H"], fx["dqmap"], fx["sqmap"], imm,
                                                first=1, last=fx["F"], dpl=4, twotime=tt))
+    cfg = _as_format(cfg, fmt)
     args = [str(corr), str(cfg)] + (["--frame_threading"] if fx["frame_threading"] else [])
     r = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
-    out = {k.split("/")[-1]: v for k, v in refio.read_xh5c(cfg).items() if k.startswith("/exchange/")}
+    out = _exchange(cfg, fmt)
     names = ["sg", "g2full", "g2partials", "pixelSum", "frameSum"] + \
         [k[4:] for k in fx if k.startswith("ref_g2_")]
     for name in names:

@@ -59,6 +59,25 @@ def test_valid_input_passes_the_dry_run(corr, tmp_path):
     assert f"{int(fx['nnz'].sum())} events" in out and "input is valid" in out
 
 
+def test_hdf5_analysis_file_passes_the_dry_run(corr, tmp_path):
+    """The analysis file as HDF5 (the XH5C case converted by h5lite): the
+    driver reads the configuration from it and validates the frames."""
+    from build import build_h5tool
+    fx, _, path = _case(tmp_path)
+    h5 = tmp_path / "analysis_hdf5.h5"
+    r = subprocess.run([str(build_h5tool()), "from-xh5c", str(path), str(h5)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    rc, out = _run(corr, h5)
+    assert rc == 0, out
+    assert f"{int(fx['nnz'].sum())} events" in out and "input is valid" in out
+    # a chunk of the file cut away: a reading error naming HDF5, not a crash
+    b = h5.read_bytes()
+    h5.write_bytes(b[: len(b) // 3])
+    rc, out = _run(corr, h5)
+    assert rc == 1 and "HDF5" in out
+
+
 def test_dense_input_passes_the_dry_run(corr, tmp_path):
     fx = load("dense_dark")
     imm = tmp_path / "frames.imm"

@@ -105,13 +105,26 @@ def build_synth_gpu(force: bool = False) -> Path:
 
 def build_corr(force: bool = False) -> Path:
     """The C++ `corr` driver, linked against libxpcs_gpu.so (rpath $ORIGIN)."""
-    srcs = [HOST / "corr_main.cpp", HOST / "xh5c.cpp", HOST / "imm.cpp"]
-    deps = srcs + [HOST / "xh5c.h", HOST / "imm.h", INCLUDE / "xpcs_gpu.h", LIB_GPU]
+    srcs = [HOST / "corr_main.cpp", HOST / "xh5c.cpp", HOST / "h5lite.cpp", HOST / "imm.cpp"]
+    deps = srcs + [HOST / "xh5c.h", HOST / "h5lite.h", HOST / "imm.h", INCLUDE / "xpcs_gpu.h",
+                   LIB_GPU]
     if force or _stale(CORR, deps):
         _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", str(INCLUDE), "-o", str(CORR)]
              + [str(x) for x in srcs] + ["-L", str(BUILD), "-lxpcs_gpu",
                                          "-Wl,-rpath,$ORIGIN"])
     return CORR
+
+
+H5TOOL = BUILD / "h5lite_tool"
+
+
+def build_h5tool(force: bool = False) -> Path:
+    """The h5lite command line (dump / create / put / from-xh5c) used by the tests."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    srcs = [HOST / "h5lite_tool.cpp", HOST / "h5lite.cpp", HOST / "xh5c.cpp"]
+    if force or _stale(H5TOOL, srcs + [HOST / "h5lite.h", HOST / "xh5c.h"]):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", "-o", str(H5TOOL)] + [str(x) for x in srcs])
+    return H5TOOL
 
 
 def build_all(force: bool = False) -> None:
@@ -121,6 +134,7 @@ def build_all(force: bool = False) -> None:
         for f in futs:
             f.result()
     build_corr(force)
+    build_h5tool(force)
 
 
 if __name__ == "__main__":

@@ -9,8 +9,13 @@
 //   multi-tau analysis tau, norm-0-g2, norm-0-stderr (and with --g2out
 //   G2/IP/IF), for the two-time analysis (analysis_type Twotime) sg,
 //   C2T_all/g2_<q>, g2full, g2partials; with --darkout DarkAvg/DarkStd.
-// The analysis file is read and written in the XH5C container format
-// (xh5c.h).  Extra flags: --mode=exact (lookup over the live prefix only),
+// The analysis file is an HDF5 file (h5lite.h: the results are written into
+// it, new datasets and groups appended, existing ones of the same type and
+// shape overwritten, as H5Result does) or an XH5C container with the same
+// paths (xh5c.h); the two are told apart by the file's signature.  Datasets
+// are written contiguous, without the reference's optional deflate
+// (h5_result.cpp:82-95): the values are the same, only the storage differs.
+// Extra flags: --mode=exact (lookup over the live prefix only),
 // --fp64 (write the float64 normalisation), --device=N, --block=N (frames
 // per ingest call), --dry-run (read and check the configuration and every
 // frame the analysis would use, report, and stop before any GPU work).
@@ -143,7 +148,8 @@ int main(int argc, char **argv) {
   const std::string entry = fl.entry.empty() ? "/xpcs" : fl.entry;
   xh5c::File cfg;
   if (!cfg.load(cfg_path)) {
-    fprintf(stderr, "corr: cannot read %s\n", cfg_path.c_str());
+    fprintf(stderr, "corr: cannot read %s%s%s\n", cfg_path.c_str(),
+            cfg.error().empty() ? "" : ": ", cfg.error().c_str());
     return 1;
   }
   try {
@@ -415,7 +421,8 @@ int main(int argc, char **argv) {
            st.filter_ms, st.multitau_ms, st.normalize_ms);
     xpcs_series_destroy(s);
     if (!cfg.save(cfg_path)) {
-      fprintf(stderr, "corr: cannot write %s\n", cfg_path.c_str());
+      fprintf(stderr, "corr: cannot write %s%s%s\n", cfg_path.c_str(),
+              cfg.error().empty() ? "" : ": ", cfg.error().c_str());
       return 1;
     }
   } catch (const std::exception &e) {
