@@ -185,3 +185,64 @@ def test_not_hdf5_and_truncated_files_are_errors(tool, tmp_path):
     junk = tmp_path / "junk.h5"
     junk.write_bytes(os.urandom(4096))
     assert run(tool, "dump", junk, ok=False).returncode != 0
+
+
+def _vlstr_file(path, name: str, text: str):
+    """A file built byte by byte from the format specification: version 0
+    superblock, a root symbol-table group with one link, and a scalar
+    variable-length string dataset whose characters live in a global heap
+    collection (the way h5py stores Python strings)."""
+    import struct
+
+    def pad8(b):
+        return b + b"\0" * (-len(b) % 8)
+
+    def v1_header(msgs):
+        body = b"".join(struct.pack("<HHB3x", t, len(pad8(d)), 0) + pad8(d) for t, d in msgs)
+        return struct.pack("<BBHII4x", 1, 0, len(msgs), 1, len(body)) + body
+
+    U = 0xFFFFFFFFFFFFFFFF
+    out = bytearray(96)  # the superblock, filled in last
+    def put(b):
+        while len(out) % 8:
+            out.append(0)
+        a = len(out)
+        out.extend(b)
+        return a
+    tb = text.encode()
+    gcol = b"GCOL" + bytes([1, 0, 0, 0])
+    obj = struct.pack("<HH4xQ", 1, 0, len(tb)) + pad8(tb)
+    free = 4096 - 16 - len(obj)
+    gcol += struct.pack("<Q", 4096) + obj + struct.pack("<HH4xQ", 0, 0, free - 16) + b"\0" * (free - 16)
+    g = put(gcol)
+    elem = put(struct.pack("<IQI", len(tb), g, 1))
+    char = bytes([0x10, 0, 0, 0]) + struct.pack("<IHH", 1, 0, 8)
+    vl = bytes([0x19, 0x01, 0, 0]) + struct.pack("<I", 16) + char
+    space = bytes([1, 0, 0, 0, 0, 0, 0, 0])
+    layout = bytes([3, 1]) + struct.pack("<QQ", elem, 16)
+    ds = put(v1_header([(0x01, space), (0x03, vl), (0x08, layout)]))
+    nm = pad8(name.encode() + b"\0")
+    seg = b"\0" * 8 + nm + struct.pack("<QQ", 1, 16)
+    seg_a = put(seg)
+    heap = put(b"HEAP" + b"\0" * 4 + struct.pack("<QQQ", len(seg), 8 + len(nm), seg_a))
+    snod = put((b"SNOD" + bytes([1, 0]) + struct.pack("<H", 1)
+                + struct.pack("<QQI4x16x", 8, ds, 0)).ljust(8 + 8 * 40, b"\0"))
+    tree = put((b"TREE" + bytes([0, 0]) + struct.pack("<HQQ", 1, U, U)
+                + struct.pack("<QQQ", 0, snod, 8)).ljust(24 + 33 * 8 + 32 * 8, b"\0"))
+    root = put(v1_header([(0x11, struct.pack("<QQ", tree, heap))]))
+    sb = (b"\x89HDF\r\n\x1a\n" + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", 4, 16, 0)
+          + struct.pack("<QQQQ", 0, U, len(out), U)
+          + struct.pack("<QQI4xQQ", 0, root, 1, tree, heap))
+    out[:96] = sb
+    Path(path).write_bytes(bytes(out))
+
+
+def test_variable_length_string_from_a_global_heap(tool, tmp_path):
+    f = tmp_path / "vl.h5"
+    _vlstr_file(f, "output_data", "/exchange_run7")
+    d = dump(tool, f)
+    assert d["/output_data"][0].startswith("str") and d["/output_data"][2] == '"/exchange_run7"'
+    # the writer appends next to it and the string survives
+    run(tool, "put", f, "/exchange/tau", "f32", "2", 1, 2)
+    d = dump(tool, f)
+    assert d["/output_data"][2] == '"/exchange_run7"' and d["/exchange/tau"][2] == "1 2"
