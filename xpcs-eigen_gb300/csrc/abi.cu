@@ -96,6 +96,8 @@ void sync_and_check(Series &s) {
     XG_CUDA(cudaMemcpy(&st, s.stats.p, sizeof(DevStats), cudaMemcpyDeviceToHost));
     if (st.error & DEVERR_PIXEL_INDEX)
       throw Error(XPCS_ERR_INPUT, "a sparse frame holds a pixel index outside the detector");
+    if (st.error & DEVERR_WAIT)
+      throw Error(XPCS_ERR_CUDA, "an asynchronous copy did not complete within its wait limit");
   }
 }
 
@@ -165,6 +167,7 @@ void free_series(Series *s) {
     DBuf<float> *ttf[] = {&s->tt_V, &s->tt_sg, &s->tt_sga, &s->tt_C, &s->tt_full, &s->tt_part};
     for (auto *b : ttf) b->release(st);
     s->d_fscale.release(st);
+    s->n_unsafe.release(st);
     s->tt_err.release(st);
     s->tt_flags.release(st);
     s->tt_XT.release(st);

@@ -24,8 +24,6 @@
 //   k_f32_transpose / k_entry_f32 / k_q_f32 replay the reference's sequential
 //   float operations in its order, including the running-mean/M2 update of
 //   every pixel.
-#include <cuda_pipeline.h>
-
 #include <algorithm>
 #include <vector>
 
@@ -239,10 +237,10 @@ __global__ void k_norm_finish(int NQ, int D, const int32_t *__restrict__ qep,
 constexpr int TR_K = 32, TR_T = 32;  // transpose tile: mapped pixels x taus
 
 __global__ void __launch_bounds__(256)
-k_f32_transpose(int NK, int D, int P, const int32_t *__restrict__ pix,
+k_f32_transpose(int NK, int D, int Dp, int P, const int32_t *__restrict__ pix,
                 const float *__restrict__ G2, const float *__restrict__ IP,
                 const float *__restrict__ IF, float *__restrict__ Tg, float *__restrict__ Ti,
-                float *__restrict__ Tf, float *__restrict__ X) {
+                float *__restrict__ Tf, float *__restrict__ X, int32_t *__restrict__ unsafe) {
   __shared__ float sg[TR_T][TR_K + 1], si[TR_T][TR_K + 1], sf[TR_T][TR_K + 1];
   const int k0 = blockIdx.x * TR_K, t0 = blockIdx.y * TR_T;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
@@ -263,15 +261,21 @@ k_f32_transpose(int NK, int D, int P, const int32_t *__restrict__ pix,
   const int t = t0 + tx;
   for (int r = ty; r < TR_K; r += 8) {
     const int kk = k0 + r;
+    bool bad = false;
     if (kk < NK && t < D) {
       const float g = sg[tx][r], a = si[tx][r], b = sf[tx][r];
-      const size_t o = (size_t)kk * D + t;
+      const size_t o = (size_t)kk * Dp + t;
       Tg[o] = g;
       Ti[o] = a;
       Tf[o] = b;
-      const float x = __fdiv_rn(g, __fmul_rn(a, b));
-      X[o] = isnan(x) ? 0.f : x;
+      float x = __fdiv_rn(g, __fmul_rn(a, b));
+      x = isnan(x) ? 0.f : x;
+      X[o] = x;
+      bad = !(x == 0.f || (x >= 0x1p-20f && x <= 0x1p20f));
     }
+    // any ratio outside the range where the q-ring replay's running mean
+    // needs no special case (k_q_f32)
+    if (__any_sync(0xffffffffu, bad) && tx == 0) atomicOr(unsafe, 1);
   }
 }
 
@@ -285,63 +289,121 @@ __device__ __forceinline__ float div_count(float a, float n, int ni, float y) {
 }
 
 // The replay kernels below run one block per q ring (or per entry) and one
-// thread per tau.  The rows [k][0..D) of the block's pixel range are streamed
-// into shared memory in chunks of `ch` rows (up to 32, fewer for long delay
-// lists) by asynchronous copies (two buffers: chunk c+1 is in flight while
-// the threads step through chunk c), so each thread's sequential chain reads
-// shared memory instead of waiting on global loads.
+// thread per tau.  The rows [k][0..Dp) of the block's pixel range (Dp: the
+// delays padded to a multiple of 4, so that every row range is a 16-byte
+// aligned, contiguous span) are brought into shared memory in chunks of up to
+// 256 rows by 1-D bulk copies (cp.async.bulk, one per array, issued by one
+// thread and completing on an mbarrier), double-buffered: chunk c+1 is in
+// flight while the threads step through chunk c, so each thread's sequential
+// chain reads shared memory instead of waiting on global loads.
 constexpr int FR_SMEM = 200 * 1024;  // shared memory budget of a replay block
+constexpr uint32_t FR_WAIT_LIMIT = 1u << 22;  // polls before a wait is given up
 
-// copies rows [r0, r0 + nrow) of the D-wide arrays into the shared buffers
-__device__ __forceinline__ void fr_issue(const float *const *src, float *const *dst, int narr,
-                                         int64_t r0, int nrow, int D) {
-  const int n = nrow * D;
-  for (int a = 0; a < narr; a++) {
-    const float *g = src[a] + (size_t)r0 * D;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) __pipeline_memcpy_async(dst[a] + i, g + i, 4);
+__device__ __forceinline__ uint32_t fr_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void fr_bar_init(uint64_t *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fr_u32(bar)));
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fr_u32(bar + 1)));
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Waits for the phase of the given parity; false after FR_WAIT_LIMIT polls.
+__device__ __forceinline__ bool fr_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = fr_u32(bar);
+  for (uint32_t it = 0; it < FR_WAIT_LIMIT; it++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
   }
-  __pipeline_commit();
+  return false;
+}
+
+// One thread: rows [r0, r0 + nrow) of each row-major [k][Dp] array into
+// dst[a], completing on bar.
+__device__ __forceinline__ void fr_bulk(const float *const *src, float *const *dst, int narr,
+                                        int64_t r0, int nrow, int Dp, uint64_t *bar) {
+  const uint32_t bytes = (uint32_t)nrow * (uint32_t)Dp * 4u;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fr_u32(bar)),
+               "r"(bytes * (uint32_t)narr)
+               : "memory");
+  for (int a = 0; a < narr; a++)
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(fr_u32(dst[a])), "l"(src[a] + (size_t)r0 * Dp), "r"(bytes), "r"(fr_u32(bar))
+        : "memory");
+}
+
+// The chunk loop shared by the replay kernels: `narr` arrays of the rows
+// [k0, k0 + n) streamed through the two buffers of `buf` ([2][narr][ch][Dp]),
+// `step(b, rows, row0)` called by every thread for each chunk in order (b:
+// the chunk's buffer, row0: its first row in the range).  Returns false, after setting DEVERR_WAIT, if a copy's
+// wait expired; the copies still in flight are then waited for (again with a
+// limit) before the block leaves.
+template <class Step>
+__device__ __forceinline__ bool fr_stream(const float *const *src, int narr, int64_t k0, int n,
+                                          int ch, int Dp, float *buf, uint64_t *bar,
+                                          int32_t *err, Step step) {
+  const int t = threadIdx.x, nch = (n + ch - 1) / ch;
+  const size_t bw = (size_t)narr * ch * Dp;
+  auto issue = [&](int c) {
+    float *dst[3];
+    for (int a = 0; a < narr; a++) dst[a] = buf + (size_t)(c & 1) * bw + (size_t)a * ch * Dp;
+    fr_bulk(src, dst, narr, k0 + (int64_t)c * ch, min(ch, n - c * ch), Dp, &bar[c & 1]);
+  };
+  if (t == 0) fr_bar_init(bar);
+  __syncthreads();
+  if (t == 0) {
+    if (nch > 0) issue(0);
+    if (nch > 1) issue(1);
+  }
+  bool ok = true;
+  int c = 0;
+  for (; c < nch; c++) {
+    ok = __syncthreads_and(fr_wait(&bar[c & 1], (uint32_t)(c >> 1) & 1u)) != 0;
+    if (!ok) break;
+    step(c & 1, min(ch, n - c * ch), c * ch);
+    __syncthreads();  // every thread is done with the buffer before it is refilled
+    if (t == 0 && c + 2 < nch) issue(c + 2);
+  }
+  if (!ok && t == 0) {
+    atomicOr(err, DEVERR_WAIT);
+    // the copies issued for chunks c and c + 1, if any, before the block goes
+    for (int d = c; d < min(c + 2, nch); d++) fr_wait(&bar[d & 1], (uint32_t)(d >> 1) & 1u);
+  }
+  return ok;
 }
 
 // One block per entry, thread tau: the entry's sums of G2, IP, IF in pixel
 // order, / pixels, ratio (corr.cpp:966-1013).
-__global__ void k_entry_f32(int NE, int D, int FR_CH, const int32_t *__restrict__ epp,
+__global__ void k_entry_f32(int NE, int D, int Dp, int FR_CH, const int32_t *__restrict__ epp,
                             const float *__restrict__ Tg, const float *__restrict__ Ti,
-                            const float *__restrict__ Tf, float *__restrict__ ratio) {
-  extern __shared__ float fr_buf[];  // [2][3][FR_CH][D]
+                            const float *__restrict__ Tf, float *__restrict__ ratio,
+                            int32_t *__restrict__ err) {
+  extern __shared__ __align__(16) float fr_buf[];  // [2][3][FR_CH][Dp], then 2 mbarriers
+  uint64_t *bar = (uint64_t *)(fr_buf + (size_t)2 * 3 * FR_CH * Dp);
   const int e = blockIdx.x, t = threadIdx.x;
-  const int k0 = epp[e], k1 = epp[e + 1];
-  const int n = k1 - k0, nch = (n + FR_CH - 1) / FR_CH;
+  const int k0 = epp[e], n = epp[e + 1] - k0;
   const float *src[3] = {Tg, Ti, Tf};
   float sg = 0.f, si = 0.f, sf = 0.f;
-  const size_t bw = (size_t)FR_CH * D;
-  if (nch > 0) {
-    float *d0[3] = {fr_buf, fr_buf + bw, fr_buf + 2 * bw};
-    fr_issue(src, d0, 3, k0, min(FR_CH, n), D);
-  }
-  for (int c = 0; c < nch; c++) {
-    if (c + 1 < nch) {
-      float *base = fr_buf + (size_t)((c + 1) & 1) * 3 * bw;
-      float *dn[3] = {base, base + bw, base + 2 * bw};
-      fr_issue(src, dn, 3, k0 + (int64_t)(c + 1) * FR_CH, min(FR_CH, n - (c + 1) * FR_CH), D);
-      __pipeline_wait_prior(1);
-    } else {
-      __pipeline_wait_prior(0);
-    }
-    __syncthreads();
-    if (t < D) {
-      const float *bg = fr_buf + (size_t)(c & 1) * 3 * bw, *bi = bg + bw, *bf = bg + 2 * bw;
-      const int rows = min(FR_CH, n - c * FR_CH);
+  const size_t aw = (size_t)FR_CH * Dp;
+  const bool ok = fr_stream(src, 3, k0, n, FR_CH, Dp, fr_buf, bar, err, [&](int b, int rows, int) {
+    if (t >= D) return;
+    const float *bg = fr_buf + (size_t)b * 3 * aw, *bi = bg + aw, *bf = bg + 2 * aw;
 #pragma unroll 4
-      for (int r = 0; r < rows; r++) {
-        sg = __fadd_rn(sg, bg[r * D + t]);
-        si = __fadd_rn(si, bi[r * D + t]);
-        sf = __fadd_rn(sf, bf[r * D + t]);
-      }
+    for (int r = 0; r < rows; r++) {
+      sg = __fadd_rn(sg, bg[r * Dp + t]);
+      si = __fadd_rn(si, bi[r * Dp + t]);
+      sf = __fadd_rn(sf, bf[r * Dp + t]);
     }
-    __syncthreads();
-  }
-  if (t < D) {
+  });
+  if (ok && t < D) {
     const float cnt = (float)n;
     sg = __fdiv_rn(sg, cnt);
     si = __fdiv_rn(si, cnt);
@@ -353,11 +415,14 @@ __global__ void k_entry_f32(int NE, int D, int FR_CH, const int32_t *__restrict_
 // One block per q ring, thread tau: g2 = mean of the non-NaN entry ratios
 // (corr.cpp:1018-1040); stderr from the running mean / M2 over the ring's
 // pixels in order, NaN counted as 0 (corr.cpp:1043-1087).
-__global__ void k_q_f32(int NQ, int D, int FR_CH, const int32_t *__restrict__ qep,
+__global__ void k_q_f32(int NQ, int D, int Dp, int FR_CH, const int32_t *__restrict__ qep,
                         const int32_t *__restrict__ qrow, const int32_t *__restrict__ epp,
                         const float *__restrict__ ratio, const float *__restrict__ X,
-                        float *__restrict__ g2, float *__restrict__ se) {
-  extern __shared__ float fr_buf[];  // [2][FR_CH][D]
+                        float *__restrict__ g2, float *__restrict__ se,
+                        const int32_t *__restrict__ unsafe, int32_t *__restrict__ err) {
+  extern __shared__ __align__(16) float fr_buf[];  // [2][FR_CH][Dp], then 2 mbarriers
+  const bool all_safe = *unsafe == 0;
+  uint64_t *bar = (uint64_t *)(fr_buf + (size_t)2 * FR_CH * Dp);
   const int qi = blockIdx.x, t = threadIdx.x;
   const int row = qrow[qi];
   if (t < D) {
@@ -369,43 +434,72 @@ __global__ void k_q_f32(int NQ, int D, int FR_CH, const int32_t *__restrict__ qe
     }
     g2[(size_t)t * NQ + row] = __fdiv_rn(acc, cnt);
   }
-  float avg = 0.f, sd = 0.f, samples = 0.f;
-  int ns = 0;
-  const int k0 = epp[qep[qi]], k1 = epp[qep[qi + 1]];
-  const int n = k1 - k0, nch = (n + FR_CH - 1) / FR_CH;
-  const size_t bw = (size_t)FR_CH * D;
+  // The reference's sample count (samples += 1.0f per pixel) is the exact
+  // count below 2^24 and stays at 2^24 from there on.  Its correctly rounded
+  // reciprocal depends on the count only: the block computes each chunk's
+  // into a table, off the chain of dependent operations that each tau's
+  // running mean is.
+  __shared__ float rtab[256];
+  float avg = 0.f, sd = 0.f;
+  const int k0 = epp[qep[qi]], n = epp[qep[qi + 1]] - k0;
   const float *src[1] = {X};
-  if (nch > 0) {
-    float *d0[1] = {fr_buf};
-    fr_issue(src, d0, 1, k0, min(FR_CH, n), D);
-  }
-  for (int c = 0; c < nch; c++) {
-    if (c + 1 < nch) {
-      float *dn[1] = {fr_buf + (size_t)((c + 1) & 1) * bw};
-      fr_issue(src, dn, 1, k0 + (int64_t)(c + 1) * FR_CH, min(FR_CH, n - (c + 1) * FR_CH), D);
-      __pipeline_wait_prior(1);
-    } else {
-      __pipeline_wait_prior(0);
-    }
+  const bool ok = fr_stream(src, 1, k0, n, FR_CH, Dp, fr_buf, bar, err, [&](int b, int rows,
+                                                                          int row0) {
+    for (int r = t; r < rows; r += blockDim.x) rtab[r] = __frcp_rn((float)(row0 + r + 1));
     __syncthreads();
-    if (t < D) {
-      const float *bx = fr_buf + (size_t)(c & 1) * bw;
-      const int rows = min(FR_CH, n - c * FR_CH);
+    if (t >= D) return;
+    const float *bx = fr_buf + (size_t)b * FR_CH * Dp;
+    // When every ratio of the series is 0 or in [2^-20, 2^20] (flagged by
+    // k_f32_transpose), the running mean of non-negative values over at most
+    // 2^20 counts stays 0 or about [2^-40, 2^20] (checked at each chunk):
+    // every difference a is then 0 (which leaves the mean as it is however it
+    // is divided) or finite and at least about 2^-64 in size (the spacing of
+    // floats near 2^-41), far inside the range where the reciprocal-and-
+    // residual quotient is the IEEE one; the quotient is never NaN, and the
+    // chain runs without a branch.
+    if (all_safe && row0 + rows <= (1 << 20) &&
+        (avg == 0.f || (avg >= 0x1p-40f && avg <= 0x1p20f))) {
+      float cnt = (float)row0;
 #pragma unroll 4
       for (int r = 0; r < rows; r++) {
-        const float x = bx[r * D + t];
-        const float tmpAvg = avg;
-        samples = __fadd_rn(samples, 1.f);
-        ns++;
-        float tmp00 = div_count(__fsub_rn(x, tmpAvg), samples, ns, __frcp_rn(samples));
+        const float x = bx[r * Dp + t];
+        cnt = __fadd_rn(cnt, 1.f);  // exact: counts below 2^24
+        const float a = __fsub_rn(x, avg);
+        const float q0 = __fmul_rn(a, rtab[r]);
+        avg = __fadd_rn(avg, __fmaf_rn(__fmaf_rn(-q0, cnt, a), rtab[r], q0));
+        sd = __fadd_rn(sd, __fmul_rn(a, __fsub_rn(x, avg)));
+      }
+    } else if (row0 + rows <= (1 << 20)) {
+#pragma unroll 4
+      for (int r = 0; r < rows; r++) {
+        const float x = bx[r * Dp + t];
+        const float cnt = (float)(row0 + r + 1);
+        const float a = __fsub_rn(x, avg);
+        // a / cnt by the reciprocal and one FMA residual correction: the IEEE
+        // quotient for counts up to 2^20 and 1e-30 <= |a| <= FLT_MAX; zero,
+        // tiny, infinite and NaN operands take the division itself
+        const float q0 = __fmul_rn(a, rtab[r]);
+        float tmp00 = __fmaf_rn(__fmaf_rn(-q0, cnt, a), rtab[r], q0);
+        if (!(fabsf(a) >= 1e-30f && fabsf(a) <= 3.40282347e38f)) tmp00 = __fdiv_rn(a, cnt);
         tmp00 = isnan(tmp00) ? 0.f : tmp00;
         avg = __fadd_rn(avg, tmp00);
-        sd = __fadd_rn(sd, __fmul_rn(__fsub_rn(x, tmpAvg), __fsub_rn(x, avg)));
+        sd = __fadd_rn(sd, __fmul_rn(a, __fsub_rn(x, avg)));
+      }
+    } else {
+      for (int r = 0; r < rows; r++) {
+        const float x = bx[r * Dp + t];
+        const int k = row0 + r + 1;
+        const float cnt = (float)min(k, 1 << 24);
+        const float a = __fsub_rn(x, avg);
+        float tmp00 = k <= (1 << 20) ? div_count(a, cnt, k, rtab[r]) : __fdiv_rn(a, cnt);
+        tmp00 = isnan(tmp00) ? 0.f : tmp00;
+        avg = __fadd_rn(avg, tmp00);
+        sd = __fadd_rn(sd, __fmul_rn(a, __fsub_rn(x, avg)));
       }
     }
-    __syncthreads();
-  }
-  if (t < D) {
+  });
+  if (ok && t < D) {
+    const float samples = (float)min(n, 1 << 24);
     const float stdNorm = __fdiv_rn(sd, samples);
     const float inv = __fdiv_rn(1.f, samples);
     se[(size_t)t * NQ + row] = __fmul_rn(__fsqrt_rn(inv), __fsqrt_rn(stdNorm));
@@ -463,33 +557,40 @@ void run_normalize(Series &s, bool want64, bool want32) {
     s.n_ratio32.reserve((size_t)(NE > 0 ? NE : 1) * D, st);
     s.n_g2f.reserve((size_t)NQ * D, st);
     s.n_sef.reserve((size_t)NQ * D, st);
-    const size_t nt = (size_t)(NK > 0 ? NK : 1) * D;
+    // rows of the transposed arrays padded to a multiple of 4 delays: 16-byte
+    // aligned row ranges for the replay kernels' bulk copies
+    const int Dp = (D + 3) & ~3;
+    const size_t nt = (size_t)(NK > 0 ? NK : 1) * Dp;
     s.n_tg.reserve(nt, st);
     s.n_ti.reserve(nt, st);
     s.n_tf.reserve(nt, st);
     s.n_tx.reserve(nt, st);
+    s.n_unsafe.reserve(1, st);
+    XG_CUDA(cudaMemsetAsync(s.n_unsafe.p, 0, sizeof(int32_t), st));
     if (NK > 0) {
       k_f32_transpose<<<dim3((NK + TR_K - 1) / TR_K, (D + TR_T - 1) / TR_T), 256, 0, st>>>(
-          NK, D, P, s.n_pix.p, s.G2.p, s.IP.p, s.IF.p, s.n_tg.p, s.n_ti.p, s.n_tf.p, s.n_tx.p);
+          NK, D, Dp, P, s.n_pix.p, s.G2.p, s.IP.p, s.IF.p, s.n_tg.p, s.n_ti.p, s.n_tf.p,
+          s.n_tx.p, s.n_unsafe.p);
       XG_CHECK_LAUNCH();
     }
     if (D > 1024) throw Error(XPCS_ERR_INVALID_ARGUMENT, "more than 1024 delays");
     const int bs = (D + 31) / 32 * 32;
-    const int ch_e = std::max(1, std::min(32, FR_SMEM / (24 * D)));
-    const int ch_q = std::max(1, std::min(32, FR_SMEM / (8 * D)));
-    const size_t sm_e = sizeof(float) * 2 * 3 * (size_t)ch_e * D;
-    const size_t sm_q = sizeof(float) * 2 * (size_t)ch_q * D;
+    const int ch_e = std::max(1, std::min(256, (FR_SMEM - 64) / (24 * Dp)));
+    const int ch_q = std::max(1, std::min(256, (FR_SMEM - 64) / (8 * Dp)));
+    const size_t sm_e = sizeof(float) * 2 * 3 * (size_t)ch_e * Dp + 2 * sizeof(uint64_t);
+    const size_t sm_q = sizeof(float) * 2 * (size_t)ch_q * Dp + 2 * sizeof(uint64_t);
     XG_CUDA(cudaFuncSetAttribute(k_entry_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sm_e));
     XG_CUDA(cudaFuncSetAttribute(k_q_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sm_q));
     if (NE > 0) {
-      k_entry_f32<<<NE, bs, sm_e, st>>>(NE, D, ch_e, s.n_entry_pix_ptr.p, s.n_tg.p, s.n_ti.p,
-                                        s.n_tf.p, s.n_ratio32.p);
+      k_entry_f32<<<NE, bs, sm_e, st>>>(NE, D, Dp, ch_e, s.n_entry_pix_ptr.p, s.n_tg.p,
+                                        s.n_ti.p, s.n_tf.p, s.n_ratio32.p, &s.stats.p->error);
       XG_CHECK_LAUNCH();
     }
-    k_q_f32<<<NQ, bs, sm_q, st>>>(NQ, D, ch_q, s.n_q_entry_ptr.p, s.n_q_row.p, s.n_entry_pix_ptr.p,
-                                  s.n_ratio32.p, s.n_tx.p, s.n_g2f.p, s.n_sef.p);
+    k_q_f32<<<NQ, bs, sm_q, st>>>(NQ, D, Dp, ch_q, s.n_q_entry_ptr.p, s.n_q_row.p,
+                                  s.n_entry_pix_ptr.p, s.n_ratio32.p, s.n_tx.p, s.n_g2f.p,
+                                  s.n_sef.p, s.n_unsafe.p, &s.stats.p->error);
     XG_CHECK_LAUNCH();
   }
 }

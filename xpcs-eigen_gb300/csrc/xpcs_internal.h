@@ -37,7 +37,10 @@ extern thread_local int64_t tl_launches;
   } while (0)
 
 // Device error word bits (set by kernels, read at synchronisation points).
-enum : int32_t { DEVERR_PIXEL_INDEX = 1 };
+enum : int32_t {
+  DEVERR_PIXEL_INDEX = 1,
+  DEVERR_WAIT = 2,  // a bounded wait for an asynchronous copy expired
+};
 
 // ------------------------------------------------------------ device buffers
 
@@ -313,6 +316,7 @@ struct Series {
   // normalisation
   DBuf<int32_t> n_q_entry_ptr, n_entry_sbin, n_entry_pix_ptr, n_pix, n_q_row;
   DBuf<float> n_ratio32;
+  DBuf<int32_t> n_unsafe;  // float32 replay: a ratio outside the branch-free range
   DBuf<float> n_tg, n_ti, n_tf, n_tx;  // float32 replay: G2/IP/IF and x, [mapped pixel][D]
   DBuf<int32_t> n_ch_k0, n_ch_k1, n_e_chunk_ptr;  // pixel chunks of every entry
   int32_t n_chunks = 0;
