@@ -533,6 +533,31 @@ def run_corr(args, acq, dq, sq, nnz, idx, val):
             "wall_s": min(walls), "stages_ms": stages}
 
 
+def run_normalize(args, dev):
+    """The headline series' normalisation on its own: the float64 result the
+    bench step reports, and the float32 replay of the reference's own
+    arithmetic that `corr` writes (norm-0-g2 / norm-0-stderr, bit-identical),
+    each the median of 4 timed runs after one untimed."""
+    import xpcs_gpu as xg
+
+    acq, dq, sq, nnz, idx, val = make_series_data(width=args.width, frames=args.frames,
+                                                  mean=args.mean)
+    s = xg.Series(acq.width, acq.height, acq.frames, acq.dpl, dq, sq, device=dev)
+    s.ingest_sparse(nnz, idx, val)
+    s.multitau(xg.MODE_REFERENCE)
+    res = {"workload": f"{acq.width}x{acq.height} x {acq.frames} frames, D = {s.D}, "
+                       f"{s.nq} q rings"}
+    for key, f64, f32 in (("f64_ms", True, False), ("f32_replay_ms", False, True)):
+        ts = []
+        for _ in range(5):
+            s.normalize(f64=f64, f32=f32)
+            s.synchronize()
+            ts.append(s.stage_times()["normalize_ms"])
+        res[key] = statistics.median(ts[1:])
+    s.close()
+    return res
+
+
 def run_dense(args, dev):
     """Dense CCD series: 960x960 x 20,000 int16 frames after 100 dark frames
     (dark ~ N(100, 8^2), read noise 4 ADU, 35 ADU/photon on the speckle
@@ -782,7 +807,8 @@ def main():
     ap.add_argument("--dense-steps", type=int, default=3)
     ap.add_argument("--dense-only", action="store_true",
                     help="run only the dense-frame measure and print its object (profiling)")
-    ap.add_argument("--only", choices=["batch", "serving", "twotime", "dense"], default=None,
+    ap.add_argument("--only", choices=["batch", "serving", "twotime", "dense", "normalize"],
+                    default=None,
                     help="run only this measure and print its object (profiling)")
     ap.add_argument("--serve-streams", type=int, default=16)
     ap.add_argument("--serve-hz", type=float, default=200.0)
@@ -807,7 +833,7 @@ def main():
             run_reference_arm(args, dist)
         elif args.dense_only or args.only:
             fn = {"batch": run_batch, "serving": run_serving, "twotime": run_twotime_bench,
-                  "dense": run_dense}[args.only or "dense"]
+                  "dense": run_dense, "normalize": run_normalize}[args.only or "dense"]
             r = fn(args, dist.local)
             if dist.rank == 0:
                 print(json.dumps(r))
