@@ -376,20 +376,30 @@ bool read_dataset(const Image &im, const std::vector<Msg> &ms, Data &out, std::s
       return false;
     }
   }
+  // the size, checked against the file before anything is allocated
+  constexpr uint64_t MAX_UNWRITTEN = 1ull << 30;  // bytes of zeros for a never-written dataset
   uint64_t n = 1;
-  for (uint64_t x : dims) n *= x;
+  for (uint64_t x : dims) {
+    if (x && n > (~0ull >> 1) / x) fail("dataspace too large");
+    n *= x;
+  }
+  if (t.size && n > (~0ull >> 1) / t.size) fail("dataspace too large");
   const uint64_t nbytes = n * t.size;
+  if (L.compact) {
+    if (L.size < nbytes) fail("compact data shorter than its dataspace");
+    im.need(L.pos, nbytes);
+  } else if (L.addr != UNDEF) {
+    im.need(im.at(L.addr), nbytes);
+  } else if (nbytes > MAX_UNWRITTEN) {
+    why = "storage never allocated";
+    return false;
+  }
   std::vector<unsigned char> raw(nbytes, 0);
   if (nbytes) {
-    if (L.compact) {
-      if (L.size < nbytes) fail("compact data shorter than its dataspace");
-      im.need(L.pos, nbytes);
+    if (L.compact)
       memcpy(raw.data(), &im.b[L.pos], nbytes);
-    } else if (L.addr != UNDEF) {  // an undefined address: never written, zeros
-      const uint64_t a = im.at(L.addr);
-      im.need(a, nbytes);
-      memcpy(raw.data(), &im.b[a], nbytes);
-    }
+    else if (L.addr != UNDEF)  // an undefined address: never written, zeros
+      memcpy(raw.data(), &im.b[im.at(L.addr)], nbytes);
   }
   out.dims = dims;
   out.kind = t.kind;
@@ -400,6 +410,7 @@ bool read_dataset(const Image &im, const std::vector<Msg> &ms, Data &out, std::s
       s[i] = vl_string(im, &raw[16 * i]);
       w = std::max(w, s[i].size());
     }
+    if (n * w > (1ull << 31)) fail("strings too large");
     out.size = (uint32_t)w;
     out.bytes.assign(n * w, 0);
     for (uint64_t i = 0; i < n; i++) memcpy(&out.bytes[i * w], s[i].data(), s[i].size());
