@@ -436,8 +436,18 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
   s_nonint[w][lane] = 0;
   __syncwarp();
   bool dup = false;
+  // each 32-event chunk is loaded one chunk ahead; the previous chunk's last
+  // frame carries over to lane 0
+  int32_t f_nx = e0 + lane < e1 ? fr[e0 + lane] : 0;
+  float x_nx = e0 + lane < e1 ? val[e0 + lane] : 0.f;
+  int32_t carry_f = 0;
   for (int64_t base = e0; base < e1; base += 32) {
     const int64_t e = base + lane;
+    const int32_t f = f_nx;
+    const float x = x_nx;
+    const bool in_nx = base + 32 + lane < e1;
+    f_nx = in_nx ? fr[base + 32 + lane] : 0;
+    x_nx = in_nx ? val[base + 32 + lane] : 0.f;
     int owner = 0;  // last lane whose row starts at or before e
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -447,10 +457,9 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
     }
     const int64_t ob = __shfl_sync(0xffffffffu, my_b, owner);
     const bool in = e < e1;
-    int32_t f = in ? fr[e] : 0;
-    float x = in ? val[e] : 0.f;
     int32_t fprev = __shfl_up_sync(0xffffffffu, f, 1);
-    if (lane == 0 && in && e > e0) fprev = fr[e - 1];
+    if (lane == 0) fprev = carry_f;  // e > e0: the previous chunk's last frame
+    carry_f = __shfl_sync(0xffffffffu, f, 31);
     if (in && e > ob && f == fprev) dup = true;
     const bool nonint = in && !(x == truncf(x) && fabsf(x) < 16777216.f);
     // a row's lanes are one run (owners do not decrease across the lanes)
