@@ -809,7 +809,10 @@ k_mt_float(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
 // ring of two 32-entry tiles holds every partner of the current tile.
 constexpr int FW_WARPS = 4;
 constexpr int FW_MAXC = 32;  // delays per level and largest delay in level units
-constexpr int FW_TSTRIDE = 33;
+// Term rows of 36 floats: 16-byte aligned, so a chain's lane reads its 32
+// terms as 8 float4 loads; lanes 0-7 of such a load (chains 0-7) touch banks
+// 4*chain .. 4*chain+3, distinct, so the loads stay free of bank conflicts.
+constexpr int FW_TSTRIDE = 36;
 constexpr int FW_WIN = 128;  // bins of the per-warp partner window
 
 __device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x) {
@@ -1072,8 +1075,12 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
             const float *tr = (bulk && ch >= cnt) ? vrow : terms + (size_t)ch * FW_TSTRIDE;
             float a = acc[j];
             if (nt == 32) {
-#pragma unroll 8
-              for (int i = 0; i < 32; i++) a = __fadd_rn(a, tr[i]);
+              const float4 *t4 = (const float4 *)tr;
+#pragma unroll
+              for (int i = 0; i < 8; i++) {
+                const float4 y = t4[i];
+                a = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(a, y.x), y.y), y.z), y.w);
+              }
             } else {
               for (int i = 0; i < nt; i++) a = __fadd_rn(a, tr[i]);
             }
