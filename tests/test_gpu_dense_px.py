@@ -111,3 +111,33 @@ def test_dense_pixel_major_device_frames_vs_oracle():
     assert info.raw_events == rows.row_ptr[-1]
     for name, got, want in (("G2", G2, oG2), ("IP", IP, oIP), ("IF", IF, oIF)):
         assert same_bits(got, want), (name, int(np.count_nonzero(got != want)))
+
+
+def test_dense_pixel_major_framesum_and_side_statistics_vs_oracle():
+    """normalize_by_framesum on a pixel-major dense series (the finishing
+    gather forces the float rows; the float kernel scales by the frame sums)
+    and the side statistics' pixel and frame sums, formed from the rows."""
+    acq = _acq(40, 32, 900, seed=5)
+    dq, sq, flat, _ = xs.maps(acq)
+    ds = xs.DenseStream(acq)
+    raw = ds.next(acq.dark_frames + acq.frames)
+    ds.close()
+    nd, F = acq.dark_frames, acq.frames
+    qm = oracle.QMap(dq, sq)
+    da, dsd = oracle.dark_image(raw[:nd], flat.ravel())
+    rows, side = oracle.dense_filter(qm, raw[nd:], F, da, dsd, LLD, SIGMA, flat=flat.ravel())
+    scaled = oracle.framesum_normalize(rows, side["frames_sum"], F)
+    oG2, oIP, oIF = oracle.multitau2(scaled, F, acq.dpl, xg.MODE_REFERENCE)
+    with xg.Series(acq.width, acq.height, F, acq.dpl, dq, sq, flatfield=flat, dense=True,
+                   lld=LLD, sigma=SIGMA, normalize_by_framesum=True) as s:
+        s.set_dark(raw[:nd])
+        for a, b in _calls([3, 400, None], F):
+            s.ingest_dense(raw[nd + a:nd + b])
+        s.multitau(xg.MODE_REFERENCE)
+        G2, IP, IF = s.g2ipif()
+        ps, fs, _, _ = s.side_stats(max(F // 10, 1))
+    for name, got, want in (("G2", G2, oG2), ("IP", IP, oIP), ("IF", IF, oIF)):
+        assert same_bits(got, want), (name, int(np.count_nonzero(got != want)))
+    # the oracle's side outputs are already the reference's pixelSum / frameSum
+    assert same_bits(ps, side["pixels_sum"].astype(np.float32).reshape(ps.shape))
+    assert same_bits(fs, side["frames_sum"].astype(np.float32).reshape(fs.shape))
