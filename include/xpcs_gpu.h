@@ -35,7 +35,9 @@ extern "C" {
 typedef enum {
   XPCS_OK = 0,
   XPCS_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or parameter */
-  XPCS_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  XPCS_ERR_CUDA = 2,             /* a CUDA runtime call failed, or an asynchronous
+                                    copy inside a kernel did not complete within its
+                                    bounded wait */
   XPCS_ERR_OUT_OF_MEMORY = 3,    /* device or pinned host allocation failed */
   XPCS_ERR_STATE = 4,            /* call out of order (e.g. results before compute) */
   XPCS_ERR_QMAP = 5,             /* partition maps the reference would index out of
