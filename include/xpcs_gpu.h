@@ -214,15 +214,19 @@ int xpcs_get_normalized(xpcs_series *s, double *g2, double *stderr_, float *g2_f
 /* Kernel knobs of a series (no reference counterpart).  Results do not
  * depend on them; only the time does.
  *  thread_cap            warps per pixel: rows of up to this many events run
- *                        one thread per pixel (32, 48, 64, 80 or 112; the
- *                        default is 80), longer rows one warp per pixel;
+ *                        one thread per pixel (32, 48, 64, 80 or 112), longer
+ *                        rows one warp per pixel;
  *  scratch_extra         the level-fold schedule: extra scratch words per
  *                        thread (0 or 8 beyond the delays of a level and the
  *                        levels); levels of at most 32 x words bins take the
  *                        bitmask pair search;
  *  radix_items_per_lane  the transpose's event tile: 8 or 16 items per lane
  *                        (tiles of 2,048 or 4,096 events; 0 chooses by series
- *                        size). */
+ *                        size).
+ * Until xpcs_series_set_tuning or xpcs_autotune sets them, each multi-tau
+ * derives the first two from the series: thread_cap the smallest capacity of
+ * at least 1.5 mean rows (events per mapped pixel), scratch_extra 8 from
+ * 16,384 frames on (before the first multi-tau: 80 and 0). */
 typedef struct {
   int32_t thread_cap;
   int32_t scratch_extra;

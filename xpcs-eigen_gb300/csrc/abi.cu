@@ -620,6 +620,7 @@ int xpcs_series_set_tuning(xpcs_series *h, const xpcs_tuning *t) {
     s.thread_cap = t->thread_cap;
     s.scr_extra = t->scratch_extra;
     s.radix_ipt = t->radix_items_per_lane;
+    s.knobs_set = true;
     s.have_multitau = false;
     s.have_norm64 = s.have_norm32 = false;
     s.generation++;

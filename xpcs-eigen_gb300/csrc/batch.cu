@@ -104,6 +104,8 @@ int32_t autotune(Series &s, int mode) {
   XG_CUDA(cudaEventCreate(&e0));
   XG_CUDA(cudaEventCreate(&e1));
   const int32_t cap0 = s.thread_cap, scr0 = s.scr_extra, ipt0 = s.radix_ipt;
+  const bool set0 = s.knobs_set;
+  s.knobs_set = true;  // the candidates below are not replaced by the defaults
   auto time_pass = [&]() {
     float ms = 0.f;
     for (int rep = 0; rep < 2; rep++) {  // the second pass is timed
@@ -142,6 +144,7 @@ int32_t autotune(Series &s, int mode) {
     s.thread_cap = cap0;
     s.scr_extra = scr0;
     s.radix_ipt = ipt0;
+    s.knobs_set = set0;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     throw;
@@ -149,6 +152,7 @@ int32_t autotune(Series &s, int mode) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   s.tuned = true;
+  s.knobs_set = true;
   s.have_multitau = false;
   s.have_norm64 = s.have_norm32 = false;
   s.generation++;

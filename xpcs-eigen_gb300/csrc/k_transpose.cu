@@ -876,10 +876,33 @@ void reset_blocks(Series &s) {
   s.dn_pend_n = 0;
 }
 
+// The thread kernel's row capacity for a series nobody tuned: the smallest
+// capacity of at least 1.5 mean rows, which the autotuner also picks for mean
+// rows of 25, 52 and 100 events (1 Mi pixels, 5,000-20,000 frames), and the
+// extra scratch words it picks from 16,384 frames on.
+void default_knobs(Series &s) {
+  if (s.knobs_set) return;
+  if (s.valid_pixels < 0) {
+    s.valid_pixels = 0;
+    for (uint8_t v : s.qmap.valid) s.valid_pixels += v;
+  }
+  const double mean =
+      (double)s.raw_events / ((double)std::max<int64_t>(s.valid_pixels, 1) * s.R_in);
+  int32_t cap = MT_THREAD_CAPS[MT_THREAD_NCAPS - 1];
+  for (int c : MT_THREAD_CAPS)
+    if (c >= 1.5 * mean) {
+      cap = c;
+      break;
+    }
+  s.thread_cap = cap;
+  s.scr_extra = s.F >= 16384 ? 8 : 0;
+}
+
 void run_filter_transpose(Series &s) {
   cudaStream_t st = s.stream;
   const int32_t P = s.P;
   dense_px_flush(s);  // frames still pending become the last block
+  default_knobs(s);
   reserve_lists(s);
   const size_t nalloc = s.raw_events > 0 ? (size_t)s.raw_events : 1;
   s.ev_frame.reserve(nalloc, st);
@@ -969,6 +992,7 @@ void multitau_rows_upload(Series &s, const int64_t *row_ptr, const int32_t *fram
     XG_CUDA(cudaMemcpyAsync(s.ev_frame.p, frame, sizeof(int32_t) * events, cudaMemcpyHostToDevice, st));
     XG_CUDA(cudaMemcpyAsync(s.ev_val.p, value, sizeof(float) * events, cudaMemcpyHostToDevice, st));
   }
+  default_knobs(s);
   const int bs = 256;
   k_classify_rows<<<(P + bs - 1) / bs, bs, 0, st>>>(P, s.F, s.thread_cap, s.row_ptr.p, s.ev_frame.p,
                                                      s.ev_val.p, s.row_len.p, s.pclass.p,

@@ -308,6 +308,8 @@ struct Series {
   int32_t radix_ipt = 0;    // transpose items per lane (event tile / 256); 0: by series size
   int32_t plan_scr = -1;    // scratch words of the uploaded plan
   bool tuned = false;       // thread_cap, scr_extra, radix_ipt chosen by xpcs_autotune
+  bool knobs_set = false;   // chosen by the caller or the autotuner (else: default_knobs)
+  int64_t valid_pixels = -1;  // pixels of the q-map mask (counted once)
   DBuf<float> G2, IP, IF;
   bool have_multitau = false;
   bool have_norm64 = false, have_norm32 = false;
@@ -428,6 +430,8 @@ void exclusive_scan_i32_i64(const int32_t *in, int64_t *out, int64_t n, void *ws
 
 // Kernel launchers
 void run_filter_transpose(Series &s);                       // k_transpose.cu
+// Knobs for a series the caller has not tuned, from its mean row length.
+void default_knobs(Series &s);
 // Incremental transposes: every complete block of ingested frames (k_transpose.cu)
 void transpose_ready_blocks(Series &s);
 void reset_blocks(Series &s);
