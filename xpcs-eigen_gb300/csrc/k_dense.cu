@@ -382,7 +382,10 @@ __global__ void k_dense_prefix_px(int32_t P, int32_t ns, int32_t *__restrict__ c
 // the lanes' stores of one j fall in distinct banks, then each pixel's next
 // entry in the block, [j][lane].  Every word is private to its lane: shared
 // memory serves as storage that a lane can index by the pixel it is on.
-constexpr size_t KB_PX_SMEM = (size_t)KB_WARPS * KB_WPIX * (KB_SECTOR + 1) * 4;
+// After those, per warp, the raw words of the frames in flight, [frame][lane].
+constexpr size_t KB_PX_WARP =
+    (size_t)KB_WPIX * (KB_SECTOR + 1) * 4 + (size_t)2 * KB_FU * 32 * sizeof(uint4);
+constexpr size_t KB_PX_SMEM = (size_t)KB_WARPS * KB_PX_WARP;
 
 // Stores entries [lo, hi) of the open sector of the lane's pixel j at sector
 // address dst (32-byte aligned): the whole sector at once when lo = 0 and
@@ -404,10 +407,14 @@ __device__ __forceinline__ void px_flush(const uint32_t *stg, int j, int lane, u
 // rp: the rows' starts in the block ([P + 1], from the scan of the padded
 // lengths), pre: each (slice, pixel) run's offset within its row, out: the
 // block's packed entries.  The slice-0 blocks also record each row's start.
-// A lane visits only the kept pixels of each frame (7 % of them on a CCD at
-// 0.02 photons/pixel/frame): their bits come from one compare per pixel, and
-// the pixel index of a kept bit addresses the lane's shared-memory words.
-__global__ void __launch_bounds__(KB_WARPS * 32, 3)
+// A lane visits only the kept pixels of its frames in flight (7 % of them on
+// a CCD at 0.02 photons/pixel/frame): one compare per pixel and frame sets a
+// bit of a 64-bit mask (frame-major), and the lane then walks the mask's set
+// bits in order, so the warp waits on the lane with the most kept pixels over
+// 8 frames rather than over each frame.  A bit's frame addresses the raw
+// words kept in shared memory, its pixel the lane's open sector and offset;
+// a pixel's frames come in frame order.
+__global__ void __launch_bounds__(KB_WARPS * 32, 2)
 k_dense_write_px(ChunkCfg c, const int32_t *__restrict__ pre, const int64_t *__restrict__ rp,
                  uint32_t *__restrict__ out, int32_t *__restrict__ blk_off) {
   extern __shared__ __align__(16) uint32_t px_stg[];
@@ -415,9 +422,10 @@ k_dense_write_px(ChunkCfg c, const int32_t *__restrict__ pre, const int64_t *__r
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int t = blockIdx.x * KB_WARPS + w;
   if (t >= c.T) return;
-  uint32_t *stg = px_stg + (size_t)w * KB_WPIX * KB_SECTOR;
-  int32_t *so = (int32_t *)(px_stg + (size_t)KB_WARPS * KB_WPIX * KB_SECTOR) +
-                (size_t)w * KB_WPIX + lane;  // so[j * 32]: pixel j's next entry
+  uint8_t *wb = (uint8_t *)px_stg + (size_t)w * KB_PX_WARP;
+  uint32_t *stg = (uint32_t *)wb;
+  int32_t *so = (int32_t *)(wb + (size_t)KB_WPIX * KB_SECTOR * 4) + lane;  // so[j * 32]: pixel j's next entry
+  uint4 *rawb = (uint4 *)(wb + (size_t)KB_WPIX * (KB_SECTOR + 1) * 4);  // [frame][lane]
   const int p0 = t * KB_WPIX + lane * KB_LPIX;
   const int32_t *pre_y = pre + (size_t)blockIdx.y * c.P;
   int32_t rm[KB_LPIX];
@@ -448,23 +456,28 @@ k_dense_write_px(ChunkCfg c, const int32_t *__restrict__ pre, const int64_t *__r
       used[u] = fb + u < f1;
       if (used[u]) x[u] = load8(c, fb + u, p0);
     }
+    uint64_t m = 0;  // bit 8u + j: pixel j kept in frame fb + u
 #pragma unroll
     for (int u = 0; u < FU; u++) {
-      unsigned m = used[u] ? keep_mask(x[u], rm) : 0u;
-      const uint32_t fr = (uint32_t)(fb + u) << 16;
-      while (m) {
-        const int j = __ffs(m) - 1;
-        m &= m - 1u;
-        const int32_t raw = raw_at(x[u], j);
-        const int32_t o = so[j * 32];
-        const int slot = o & (KB_SECTOR - 1);
-        stg[(j * KB_SECTOR + slot) * 32 + lane] = fr | (uint32_t)(raw & 0xffff);
-        so[j * 32] = o + 1;
-        if (slot == KB_SECTOR - 1) {
-          const int lo = ((open_first >> j) & 1u) ? (int)((first >> (3 * j)) & 7u) : 0;
-          px_flush(stg, j, lane, out + (o + 1 - KB_SECTOR), lo, KB_SECTOR);
-          open_first &= ~(1u << j);
-        }
+      if (used[u]) {
+        rawb[u * 32 + lane] = x[u];
+        m |= (uint64_t)keep_mask(x[u], rm) << (8 * u);
+      }
+    }
+    while (m) {
+      const int b = __ffsll((long long)m) - 1;
+      m &= m - 1u;
+      const int u = b >> 3, j = b & 7;
+      const uint32_t wd = ((const uint32_t *)&rawb[u * 32 + lane])[j >> 1];
+      const uint32_t raw16 = (j & 1) ? (wd >> 16) : (wd & 0xffffu);
+      const int32_t o = so[j * 32];
+      const int slot = o & (KB_SECTOR - 1);
+      stg[(j * KB_SECTOR + slot) * 32 + lane] = ((uint32_t)(fb + u) << 16) | raw16;
+      so[j * 32] = o + 1;
+      if (slot == KB_SECTOR - 1) {
+        const int lo = ((open_first >> j) & 1u) ? (int)((first >> (3 * j)) & 7u) : 0;
+        px_flush(stg, j, lane, out + (o + 1 - KB_SECTOR), lo, KB_SECTOR);
+        open_first &= ~(1u << j);
       }
     }
   }
