@@ -815,6 +815,13 @@ constexpr int FW_MAXC = 32;  // delays per level and largest delay in level unit
 constexpr int FW_TSTRIDE = 36;
 constexpr int FW_WIN = 128;  // bins of the per-warp partner window
 
+// Shared memory of one warp: ring idx[64], val[64], findable[64]; the bin
+// window's values [FW_WIN]; terms [3 * acc][FW_TSTRIDE] and the shared IP/IF
+// row [FW_TSTRIDE]; rounded up to 16 bytes.
+__host__ __device__ constexpr size_t fw_warp_bytes(int acc_max) {
+  return (64 * 9 + FW_WIN * 4 + (3 * (size_t)acc_max + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
+}
+
 __device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x) {
   int first = 0, len = n;
   while (len > 0) {
@@ -860,7 +867,7 @@ __device__ __forceinline__ void fw_put(int tb, int lane, int L, const FwEntry &e
   }
 }
 
-__global__ void __launch_bounds__(FW_WARPS * 32)
+__global__ void __launch_bounds__(FW_WARPS * 32, 6)
 k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
            DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
            const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
@@ -873,16 +880,16 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   const bool ref = pl->mode == XPCS_MODE_REFERENCE;
   const McArrays ar = mc_arrays(plan_g, D);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // per warp: ring idx[64], val[64], findable[64]; bin window val[128],
-  // flag[128]; terms [3 * acc][33] and the shared IP/IF row [33]
-  const size_t wbytes = 64 * 9 + FW_WIN * 5 + (3 * (size_t)acc_max + 1) * FW_TSTRIDE * 4;
-  uint8_t *wb = fw_smem + (size_t)w * ((wbytes + 15) & ~(size_t)15);
+  uint8_t *wb = fw_smem + (size_t)w * fw_warp_bytes(acc_max);
   int32_t *ridx = (int32_t *)wb;
   float *rval = (float *)(wb + 256);
   uint8_t *rfind = wb + 512;
+  // bin b of the window: the value of the entry at b0 + b when it is
+  // findable, else 0; the G2 term v * 0 = +-0 then leaves its chain
+  // unchanged (the chains start at +0 and x + -x is +0, so no chain is ever
+  // -0, and a + +-0 == a for every other a)
   float *bval = (float *)(wb + 576);
-  uint8_t *bflag = wb + 576 + FW_WIN * 4;
-  float *terms = (float *)(wb + 576 + FW_WIN * 5);
+  float *terms = (float *)(wb + 576 + FW_WIN * 4);
   float *vrow = terms + (size_t)3 * acc_max * FW_TSTRIDE;
   const int nf = stats->nfloat;
   // pixels are handed out one per warp from a counter: rows differ in length
@@ -1017,19 +1024,13 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
         const int32_t b0 = ridx[base & 63];
         const bool use_bins = ridx[(base + nt - 1) & 63] + kmax - b0 < FW_WIN;
         if (use_bins) {
-          ((uint32_t *)bflag)[lane] = 0u;  // FW_WIN = 128 flags
+          ((float4 *)bval)[lane] = make_float4(0.f, 0.f, 0.f, 0.f);  // FW_WIN = 128 bins
           __syncwarp();
-          if (valid) {
-            bval[src - b0] = v;
-            bflag[src - b0] = rfind[r & 63];
-          }
+          if (valid) bval[src - b0] = rfind[r & 63] ? v : 0.f;
           const int q2 = base + 32 + lane;
           if (lane < kmax && q2 < L) {
             const int tb = ridx[q2 & 63] - b0;
-            if (tb < FW_WIN) {
-              bval[tb] = rval[q2 & 63];
-              bflag[tb] = rfind[q2 & 63];
-            }
+            if (tb < FW_WIN) bval[tb] = rfind[q2 & 63] ? rval[q2 & 63] : 0.f;
           }
           __syncwarp();
         }
@@ -1040,20 +1041,25 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
           if (bulk) {
             vrow[lane] = v;
           } else {
-            for (int c = 0; c < cnt; c++) {
+            float *tp = terms + (size_t)cnt * FW_TSTRIDE + lane;
+            float *tf = tp + (size_t)cnt * FW_TSTRIDE;
+#pragma unroll
+            for (int c = 0; c < FW_MAXC; c++) {
+              if (c >= cnt) break;
               const int tau = t0 + c;
-              terms[(size_t)(cnt + c) * FW_TSTRIDE + lane] = src < lastframe - tau ? v : 0.f;
-              terms[(size_t)(2 * cnt + c) * FW_TSTRIDE + lane] =
-                  (src >= tau && src < lastframe) ? v : 0.f;
+              tp[c * FW_TSTRIDE] = src < lastframe - tau ? v : 0.f;
+              tf[c * FW_TSTRIDE] = (src >= tau && src < lastframe) ? v : 0.f;
             }
           }
           // a partner is a prefix entry, so it lies below lastframe and the
           // reference's src < lastframe - tau test holds for every pair found
           if (use_bins) {
-            for (int c = 0; c < cnt; c++) {
-              const int tb = src + t0 + c - b0;
-              const float g = __fmul_rn(v, bval[tb]);
-              terms[(size_t)c * FW_TSTRIDE + lane] = bflag[tb] ? g : 0.f;
+            const float *bw = bval + (src + t0 - b0);  // + c <= src - b0 + kmax < FW_WIN
+            float *tg = terms + lane;
+#pragma unroll
+            for (int c = 0; c < FW_MAXC; c++) {
+              if (c >= cnt) break;
+              tg[c * FW_TSTRIDE] = __fmul_rn(v, bw[c]);
             }
           } else {
             for (int c = 0; c < cnt; c++) terms[(size_t)c * FW_TSTRIDE + lane] = 0.f;
@@ -1082,7 +1088,11 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
                 a = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(a, y.x), y.y), y.z), y.w);
               }
             } else {
-              for (int i = 0; i < nt; i++) a = __fadd_rn(a, tr[i]);
+#pragma unroll
+              for (int i = 0; i < 32; i++) {
+                if (i >= nt) break;
+                a = __fadd_rn(a, tr[i]);
+              }
             }
             acc[j] = a;
           }
@@ -1209,9 +1219,7 @@ void launch_float_rows(Series &s, const McPlan &hp, cudaStream_t st, int sms) {
   int kmax = 0;
   for (int g = 0; g < hp.nlev; g++) kmax = std::max(kmax, hp.lv[g].tau_lo + hp.lv[g].count - 1);
   if (kmax <= FW_MAXC && hp.acc <= FW_MAXC) {
-    const size_t wb =
-        (64 * 9 + FW_WIN * 5 + (3 * (size_t)hp.acc + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
-    const size_t smf = FW_WARPS * wb;
+    const size_t smf = FW_WARPS * fw_warp_bytes(hp.acc);
     XG_CUDA(cudaFuncSetAttribute(k_mt_fwarp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smf));
     int per_sm = 0;
