@@ -11,11 +11,13 @@
 //                  sum IF, sum x and sum (x - mean_chunk)^2 with
 //                  x = G2 / (IP IF), NaN -> 0 and still counted (quirk Q8).
 //                  Per-element arithmetic is double-word ("float-float") on
-//                  the FP32 pipes -- TwoSum, FMA-based TwoProd and the
-//                  double-word add/multiply of Joldes, Muller & Popescu
-//                  (ACM TOMS 2017), ~2^-46 relative -- because GB300's FP64
-//                  rate is a small fraction of its FP32 rate; block totals and
-//                  everything after are FP64.
+//                  the FP32 pipes -- TwoSum, FMA-based TwoProd, the quotient
+//                  of a float by a double-word, and Sum2 compensated sums of
+//                  Ogita, Rump & Oishi (2005) for the per-thread totals --
+//                  because GB300's FP64 rate is a small fraction of its FP32
+//                  rate; the block reductions use the double-word addition of
+//                  Joldes, Muller & Popescu (ACM TOMS 2017), and the block
+//                  totals and everything after are FP64.
 //   k_norm_finish  one thread per (q, tau): entry ratio (G2/n)/((IP/n)(IF/n))
 //                  (:966-1013), g2 = mean of the non-NaN ratios (:1018-1040),
 //                  and the chunks' (n, mean, M2) merged in order with Chan's
@@ -56,22 +58,11 @@ __device__ __forceinline__ dw two_prod(float a, float b) {
   float p = __fmul_rn(a, b);
   return {p, __fmaf_rn(a, b, -p)};
 }
-// double-word + float (DWPlusFP)
-__device__ __forceinline__ dw dw_add_f(dw x, float y) {
-  dw s = two_sum(x.h, y);
-  return fast_two_sum(s.h, __fadd_rn(x.l, s.l));
-}
 // double-word + double-word (AccurateDWPlusDW)
 __device__ __forceinline__ dw dw_add(dw x, dw y) {
   dw s = two_sum(x.h, y.h), t = two_sum(x.l, y.l);
   dw v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
   return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
-}
-// double-word * double-word (DWTimesDW)
-__device__ __forceinline__ dw dw_mul(dw x, dw y) {
-  dw c = two_prod(x.h, y.h);
-  float t = __fmaf_rn(x.l, y.h, __fmaf_rn(x.h, y.l, __fmul_rn(x.l, y.l)));
-  return fast_two_sum(c.h, __fadd_rn(c.l, t));
 }
 // float / double-word: a quotient from the reciprocal of the high word, then
 // the quotient of the FMA remainder a - q (bh + bl) as the low word
@@ -85,6 +76,24 @@ __device__ __forceinline__ dw f_div_dw(float a, dw b) {
   r = __fmaf_rn(-q, b.l, r);
   return fast_two_sum(q, __fmul_rn(r, rb));
 }
+// Sum2 (Ogita, Rump & Oishi, SIAM J. Sci. Comput. 26(6), 2005): a running
+// float sum and, beside it, the float sum of every addition's exact rounding
+// error; as accurate as summing in twice the precision, at one TwoSum and one
+// addition per term.
+struct sum2 {
+  float s, c;
+};
+__device__ __forceinline__ void s2_add(sum2 &a, float x) {
+  const dw t = two_sum(a.s, x);
+  a.s = t.h;
+  a.c = __fadd_rn(a.c, t.l);
+}
+// a double-word term: its low word joins the error sum
+__device__ __forceinline__ void s2_add(sum2 &a, dw x) {
+  s2_add(a, x.h);
+  a.c = __fadd_rn(a.c, x.l);
+}
+__device__ __forceinline__ dw s2_value(const sum2 &a) { return two_sum(a.s, a.c); }
 __device__ __forceinline__ dw dw_from_double(double x) {
   float h = __double2float_rn(x);
   return {h, __double2float_rn(x - (double)h)};
@@ -132,25 +141,25 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
   const int c = blockIdx.x, t = blockIdx.y;
   const int k0 = ch_k0[c], k1 = ch_k1[c];
   const size_t o = (size_t)t * P;
-  dw sg{0.f, 0.f}, si{0.f, 0.f}, sf{0.f, 0.f}, sx{0.f, 0.f};
+  sum2 sg{0.f, 0.f}, si{0.f, 0.f}, sf{0.f, 0.f}, sx{0.f, 0.f};
 #pragma unroll
   for (int j = 0; j < NIPT; j++) {
     const int k = k0 + j * NB + threadIdx.x;
     if (k < k1) {
       const int p = pix[k];
       const float g = G2[o + p], a = IP[o + p], b = IF[o + p];
-      sg = dw_add_f(sg, g);
-      si = dw_add_f(si, a);
-      sf = dw_add_f(sf, b);
+      s2_add(sg, g);
+      s2_add(si, a);
+      s2_add(sf, b);
       dw x = f_div_dw(g, two_prod(a, b));
       if (isnan(x.h) || isnan(x.l)) x = {0.f, 0.f};
-      sx = dw_add(sx, x);
+      s2_add(sx, x);
       xh[j * NB + threadIdx.x] = x.h;
       xl[j * NB + threadIdx.x] = x.l;
     }
   }
   const double n = (double)(k1 - k0);
-  dw parts[4] = {sg, si, sf, sx};
+  dw parts[4] = {s2_value(sg), s2_value(si), s2_value(sf), s2_value(sx)};
   double sums[4];
   block_sum_dw<4>(parts, sums, sh);  // thread 0 holds the sums
   if (threadIdx.x == 0) {
@@ -159,18 +168,21 @@ k_norm_chunk(int D, int P, const int32_t *__restrict__ ch_k0, const int32_t *__r
     s_mean[1] = mu.l;
   }
   __syncthreads();
-  const dw mean{s_mean[0], s_mean[1]};
-  const dw nmean{-mean.h, -mean.l};
-  dw m2{0.f, 0.f};
+  const float mh = -s_mean[0], ml = -s_mean[1];
+  sum2 m2{0.f, 0.f};
 #pragma unroll
   for (int j = 0; j < NIPT; j++) {
     const int k = k0 + j * NB + threadIdx.x;
     if (k < k1) {
-      dw d = dw_add(dw{xh[j * NB + threadIdx.x], xl[j * NB + threadIdx.x]}, nmean);
-      m2 = dw_add(m2, dw_mul(d, d));
+      // d = x - mean as an exact high difference and a low remainder; d^2
+      // as the exact square of the high part and the rest by FMA
+      const dw d0 = two_sum(xh[j * NB + threadIdx.x], mh);
+      const float dl = __fadd_rn(__fadd_rn(d0.l, xl[j * NB + threadIdx.x]), ml);
+      const dw q = two_prod(d0.h, d0.h);
+      s2_add(m2, dw{q.h, __fmaf_rn(__fmul_rn(2.f, d0.h), dl, __fmaf_rn(dl, dl, q.l))});
     }
   }
-  dw mparts[1] = {m2};
+  dw mparts[1] = {s2_value(m2)};
   double msum[1];
   block_sum_dw<1>(mparts, msum, sh);
   if (threadIdx.x == 0) {
