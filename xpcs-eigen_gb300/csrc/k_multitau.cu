@@ -1056,10 +1056,19 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
           if (use_bins) {
             const float *bw = bval + (src + t0 - b0);  // + c <= src - b0 + kmax < FW_WIN
             float *tg = terms + lane;
+            if ((cnt & 3) == 0) {  // e.g. every level of 8 delays: one test per 4 delays
 #pragma unroll
-            for (int c = 0; c < FW_MAXC; c++) {
-              if (c >= cnt) break;
-              tg[c * FW_TSTRIDE] = __fmul_rn(v, bw[c]);
+              for (int c = 0; c < FW_MAXC; c += 4) {
+                if (c >= cnt) break;
+#pragma unroll
+                for (int u = 0; u < 4; u++) tg[(c + u) * FW_TSTRIDE] = __fmul_rn(v, bw[c + u]);
+              }
+            } else {
+#pragma unroll
+              for (int c = 0; c < FW_MAXC; c++) {
+                if (c >= cnt) break;
+                tg[c * FW_TSTRIDE] = __fmul_rn(v, bw[c]);
+              }
             }
           } else {
             for (int c = 0; c < cnt; c++) terms[(size_t)c * FW_TSTRIDE + lane] = 0.f;
