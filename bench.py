@@ -20,6 +20,7 @@ no cross-series exchange); value = frames of all ranks / max time over ranks.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import os
 import shutil
@@ -642,24 +643,28 @@ def run_gpu_arm(args, dist):
         s.multitau(xg.MODE_REFERENCE)
         s.normalize(out=out)
 
-    # end to end, two handles in turn: the frame copy of step k (copy engine,
-    # NVLink-C2C) runs while step k-1 computes; every step still copies its
-    # frames in, computes and reads its g2/stderr back
-    s2 = xg.Series(acq.width, acq.height, F, acq.dpl, dq, sq, device=dev)
-    out2 = (np.empty(shp, np.float64), np.empty(shp, np.float64), None, None)
+    # end to end, H series handles in turn: the frame copy of step k (copy
+    # engine, NVLink-C2C) runs while steps k-H+1 .. k-1 compute; every step
+    # still copies its frames in, computes and reads its g2/stderr back
+    H = max(2, args.e2e_handles)
+    hs = [(s, out)] + [(xg.Series(acq.width, acq.height, F, acq.dpl, dq, sq, device=dev),
+                        (np.empty(shp, np.float64), np.empty(shp, np.float64), None, None))
+                       for _ in range(H - 1)]
 
     def e2e_run(steps):
-        prev = None
+        pend = collections.deque()
         for k in range(steps):
-            cur, o = (s, out) if k % 2 == 0 else (s2, out2)
+            cur, o = hs[k % H]
             cur.reset()
             cur.ingest_sparse(nnz, idx, val)
             cur.multitau(xg.MODE_REFERENCE)
-            if prev is not None:
-                prev[0].normalize(out=prev[1])
-            prev = (cur, o)
-        if prev is not None:
-            prev[0].normalize(out=prev[1])
+            pend.append((cur, o))
+            if len(pend) == H:  # step k-H+1: its handle is reused next
+                h, ho = pend.popleft()
+                h.normalize(out=ho)
+        while pend:
+            h, ho = pend.popleft()
+            h.normalize(out=ho)
 
     # warm-up: full end-to-end steps
     for _ in range(args.warmup):
@@ -687,8 +692,8 @@ def run_gpu_arm(args, dist):
     dist.barrier()
     t0 = time.perf_counter()
     e2e_run(args.steps)
-    s.synchronize()
-    s2.synchronize()
+    for h, _ in hs:
+        h.synchronize()
     t_e2e = dist.max(time.perf_counter() - t0)
     dist.barrier()
     clk = clocks.stop()
@@ -755,8 +760,9 @@ def run_gpu_arm(args, dist):
         "stage_gbs": gbs,
         "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e / args.steps * 1e3,
-                "pipelining": "two series handles in turn: the H2D copy of step k overlaps "
-                              "the compute of step k-1 (H2D is ~180 GB/s over NVLink-C2C)"},
+                "pipelining": f"{H} series handles in turn: the H2D copy of step k overlaps "
+                              "the compute of the steps before it (H2D is ~180 GB/s over "
+                              "NVLink-C2C)"},
         "roofline": {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
@@ -781,8 +787,8 @@ def run_gpu_arm(args, dist):
             "value": F / t_cpu, "unit": "frames/s", "cores": cpu_cores(), "kind": "port",
             "sample": f"the whole {F}-frame {acq.width}x{acq.height} series, once (oracle "
                       "restatement of SparseFilter + multiTau2 + normalizeG2s)"}
-    s.close()
-    s2.close()
+    for h, _ in hs:
+        h.close()
     xg.unpin(idx)
     xg.unpin(val)
     if dist.rank == 0:
@@ -810,6 +816,8 @@ def main():
     ap.add_argument("--only", choices=["batch", "serving", "twotime", "dense", "normalize"],
                     default=None,
                     help="run only this measure and print its object (profiling)")
+    ap.add_argument("--e2e-handles", type=int, default=2,
+                    help="series handles in flight in the end-to-end measure (at least 2)")
     ap.add_argument("--serve-streams", type=int, default=16)
     ap.add_argument("--serve-hz", type=float, default=200.0)
     ap.add_argument("--serve-stagger", type=float, default=0.2, help="seconds between starts")
