@@ -103,28 +103,40 @@ def build_synth_gpu(force: bool = False) -> Path:
     return LIB_SYNTH_GPU
 
 
-def build_corr(force: bool = False) -> Path:
-    """The C++ `corr` driver, linked against libxpcs_gpu.so (rpath $ORIGIN)."""
+# AddressSanitizer + UndefinedBehaviorSanitizer builds of the host programs
+# (tests/test_host_sanitizers.py); every undefined behaviour ends the run.
+SANITIZE = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+            "-fno-omit-frame-pointer", "-g", "-O1"]
+
+
+def build_corr(force: bool = False, sanitize: bool = False) -> Path:
+    """The C++ `corr` driver, linked against libxpcs_gpu.so (rpath $ORIGIN);
+    with sanitize, the host code built with the sanitizers as corr_sanitized."""
     srcs = [HOST / "corr_main.cpp", HOST / "xh5c.cpp", HOST / "h5lite.cpp", HOST / "imm.cpp"]
     deps = srcs + [HOST / "xh5c.h", HOST / "h5lite.h", HOST / "imm.h", INCLUDE / "xpcs_gpu.h",
                    LIB_GPU]
-    if force or _stale(CORR, deps):
-        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", str(INCLUDE), "-o", str(CORR)]
+    out = BUILD / "corr_sanitized" if sanitize else CORR
+    if force or _stale(out, deps):
+        opt = SANITIZE if sanitize else ["-O2"]
+        _run(["g++", "-std=c++17"] + opt + ["-ffp-contract=off", "-I", str(INCLUDE), "-o", str(out)]
              + [str(x) for x in srcs] + ["-L", str(BUILD), "-lxpcs_gpu",
                                          "-Wl,-rpath,$ORIGIN"])
-    return CORR
+    return out
 
 
 H5TOOL = BUILD / "h5lite_tool"
 
 
-def build_h5tool(force: bool = False) -> Path:
-    """The h5lite command line (dump / create / put / from-xh5c) used by the tests."""
+def build_h5tool(force: bool = False, sanitize: bool = False) -> Path:
+    """The h5lite command line (dump / create / put / from-xh5c) used by the
+    tests; with sanitize, built with the sanitizers as h5lite_tool_sanitized."""
     BUILD.mkdir(parents=True, exist_ok=True)
     srcs = [HOST / "h5lite_tool.cpp", HOST / "h5lite.cpp", HOST / "xh5c.cpp"]
-    if force or _stale(H5TOOL, srcs + [HOST / "h5lite.h", HOST / "xh5c.h"]):
-        _run(["g++", "-std=c++17", "-O2", "-Wall", "-o", str(H5TOOL)] + [str(x) for x in srcs])
-    return H5TOOL
+    out = BUILD / "h5lite_tool_sanitized" if sanitize else H5TOOL
+    if force or _stale(out, srcs + [HOST / "h5lite.h", HOST / "xh5c.h"]):
+        opt = SANITIZE if sanitize else ["-O2"]
+        _run(["g++", "-std=c++17"] + opt + ["-Wall", "-o", str(out)] + [str(x) for x in srcs])
+    return out
 
 
 def build_all(force: bool = False) -> None:
