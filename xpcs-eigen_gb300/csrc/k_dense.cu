@@ -419,6 +419,7 @@ k_dense_write_px(ChunkCfg c, const int32_t *__restrict__ pre, const int64_t *__r
                  uint32_t *__restrict__ out, int32_t *__restrict__ blk_off) {
   extern __shared__ __align__(16) uint32_t px_stg[];
   constexpr int FU = 2 * KB_FU;
+  static_assert(FU * KB_LPIX <= 64, "one bit of the kept mask per pixel and frame in flight");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int t = blockIdx.x * KB_WARPS + w;
   if (t >= c.T) return;
