@@ -815,11 +815,13 @@ constexpr int FW_MAXC = 32;  // delays per level and largest delay in level unit
 constexpr int FW_TSTRIDE = 36;
 constexpr int FW_WIN = 128;  // bins of the per-warp partner window
 
-// Shared memory of one warp: ring idx[64], val[64], findable[64]; the bin
-// window's values [FW_WIN]; terms [3 * acc][FW_TSTRIDE] and the shared IP/IF
-// row [FW_TSTRIDE]; rounded up to 16 bytes.
+// Shared memory of one warp: ring idx[64], val[64]; the bin window's values
+// [FW_WIN]; terms [3 * acc][FW_TSTRIDE] and the shared IP/IF row
+// [FW_TSTRIDE]; rounded up to 16 bytes.  (The ring's findable flags are a
+// register mask: at 16 delays in a level this makes 8,080 bytes, and 4 warps
+// per block fit 7 blocks on an SM.)
 __host__ __device__ constexpr size_t fw_warp_bytes(int acc_max) {
-  return (64 * 9 + FW_WIN * 4 + (3 * (size_t)acc_max + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
+  return (64 * 8 + FW_WIN * 4 + (3 * (size_t)acc_max + 1) * FW_TSTRIDE * 4 + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ int lower_bound_g(const int32_t *a, int n, int32_t x) {
@@ -857,17 +859,25 @@ __device__ __forceinline__ FwEntry fw_fetch(int tb, int lane, int L, int n0, boo
   return e;
 }
 
+// The ring's findable flags are one 64-bit mask, the same in every lane: tb is
+// a multiple of 32, so a tile fills one half of the ring, bits (tb & 32) on.
 __device__ __forceinline__ void fw_put(int tb, int lane, int L, const FwEntry &e, int32_t *ridx,
-                                       float *rval, uint8_t *rfind) {
+                                       float *rval, uint64_t &fmask) {
   const int j = tb + lane, slot = j & 63;
   if (j < L) {
     ridx[slot] = e.x;
     rval[slot] = e.v;
-    rfind[slot] = e.f;
   }
+  const uint64_t b = __ballot_sync(0xffffffffu, j < L && e.f);
+  const int sh = tb & 32;
+  fmask = (fmask & ~(0xffffffffull << sh)) | (b << sh);
 }
 
-__global__ void __launch_bounds__(FW_WARPS * 32, 6)
+__device__ __forceinline__ bool fw_findable(uint64_t fmask, int j) {
+  return (fmask >> (j & 63)) & 1u;
+}
+
+__global__ void __launch_bounds__(FW_WARPS * 32, 7)
 k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist,
            DevStats *__restrict__ stats, const int64_t *__restrict__ row_ptr,
            const int32_t *__restrict__ row_len, const int32_t *__restrict__ ev_frame,
@@ -883,13 +893,12 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
   uint8_t *wb = fw_smem + (size_t)w * fw_warp_bytes(acc_max);
   int32_t *ridx = (int32_t *)wb;
   float *rval = (float *)(wb + 256);
-  uint8_t *rfind = wb + 512;
   // bin b of the window: the value of the entry at b0 + b when it is
   // findable, else 0; the G2 term v * 0 = +-0 then leaves its chain
   // unchanged (the chains start at +0 and x + -x is +0, so no chain is ever
   // -0, and a + +-0 == a for every other a)
-  float *bval = (float *)(wb + 576);
-  float *terms = (float *)(wb + 576 + FW_WIN * 4);
+  float *bval = (float *)(wb + 512);
+  float *terms = (float *)(wb + 512 + FW_WIN * 4);
   float *vrow = terms + (size_t)3 * acc_max * FW_TSTRIDE;
   const int nf = stats->nfloat;
   // pixels are handed out one per warp from a counter: rows differ in length
@@ -1007,8 +1016,9 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
       const int nchain = 3 * cnt;
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
       // ring slots past the row end are never read (partners stop at L)
-      fw_put(0, lane, L, fw_fetch(0, lane, L, n0, all_find, idx, val), ridx, rval, rfind);
-      fw_put(32, lane, L, fw_fetch(32, lane, L, n0, all_find, idx, val), ridx, rval, rfind);
+      uint64_t fmask = 0;
+      fw_put(0, lane, L, fw_fetch(0, lane, L, n0, all_find, idx, val), ridx, rval, fmask);
+      fw_put(32, lane, L, fw_fetch(32, lane, L, n0, all_find, idx, val), ridx, rval, fmask);
       for (int base = 0; base < L; base += 32) {
         // the tile after next, in flight while this one is processed
         const FwEntry nx = fw_fetch(base + 64, lane, L, n0, all_find, idx, val);
@@ -1026,11 +1036,11 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
         if (use_bins) {
           ((float4 *)bval)[lane] = make_float4(0.f, 0.f, 0.f, 0.f);  // FW_WIN = 128 bins
           __syncwarp();
-          if (valid) bval[src - b0] = rfind[r & 63] ? v : 0.f;
+          if (valid) bval[src - b0] = fw_findable(fmask, r) ? v : 0.f;
           const int q2 = base + 32 + lane;
           if (lane < kmax && q2 < L) {
             const int tb = ridx[q2 & 63] - b0;
-            if (tb < FW_WIN) bval[tb] = rfind[q2 & 63] ? rval[q2 & 63] : 0.f;
+            if (tb < FW_WIN) bval[tb] = fw_findable(fmask, q2) ? rval[q2 & 63] : 0.f;
           }
           __syncwarp();
         }
@@ -1077,7 +1087,7 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
               if (qk >= L) break;
               const int d = ridx[qk & 63] - src;
               if (d > kmax) break;
-              if (d >= t0 && rfind[qk & 63])
+              if (d >= t0 && fw_findable(fmask, qk))
                 terms[(size_t)(d - t0) * FW_TSTRIDE + lane] = __fmul_rn(v, rval[qk & 63]);
             }
           }
@@ -1108,7 +1118,7 @@ k_mt_fwarp(const uint8_t *__restrict__ plan_g, const int32_t *__restrict__ flist
         }
         __syncwarp();
         // the tile after next replaces this one in the ring
-        fw_put(base + 64, lane, L, nx, ridx, rval, rfind);
+        fw_put(base + 64, lane, L, nx, ridx, rval, fmask);
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {
