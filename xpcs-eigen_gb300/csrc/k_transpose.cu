@@ -412,7 +412,7 @@ __device__ void merge_row(int32_t p, int32_t n, int64_t b, float favg, int32_t *
 // 2^24 every float partial sum of pixelSum is exact, so pixelSum = (float)sum v;
 // otherwise each lane merges its own row / sums it in frame order.  Pixels
 // outside the mask get empty rows.
-__global__ void __launch_bounds__(256, 8)
+__global__ void __launch_bounds__(256, 6)
 k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_float,
                  const int64_t *__restrict__ row_ptr, const uint8_t *__restrict__ mask,
                  int32_t *__restrict__ fr, float *__restrict__ val, int32_t *__restrict__ row_len,
@@ -436,53 +436,66 @@ k_merge_classify(int32_t P, int32_t F, int32_t avg, int32_t tcap, int32_t force_
   s_nonint[w][lane] = 0;
   __syncwarp();
   bool dup = false;
-  // each 32-event chunk is loaded one chunk ahead; the previous chunk's last
-  // frame carries over to lane 0
-  int32_t f_nx = e0 + lane < e1 ? fr[e0 + lane] : 0;
-  float x_nx = e0 + lane < e1 ? val[e0 + lane] : 0.f;
-  int32_t carry_f = 0;
-  for (int64_t base = e0; base < e1; base += 32) {
-    const int64_t e = base + lane;
-    const int32_t f = f_nx;
-    const float x = x_nx;
-    const bool in_nx = base + 32 + lane < e1;
-    f_nx = in_nx ? fr[base + 32 + lane] : 0;
-    x_nx = in_nx ? val[base + 32 + lane] : 0.f;
-    int owner = 0;  // last lane whose row starts at or before e
+  // The chunks of the warp's rows, in positions relative to e0 of type T:
+  // 32-bit when the rows span less than 2^30 events (one shuffle and one
+  // compare per step of the owner search), else 64-bit.  Each 32-event chunk
+  // is loaded one chunk ahead; the previous chunk's last frame carries over
+  // to lane 0.
+  auto chunks = [&](auto zero) {
+    using T = decltype(zero);
+    const int32_t *frw = fr + e0;
+    const float *valw = val + e0;
+    const T n_all = (T)(e1 - e0), my_bt = (T)(my_b - e0);
+    int32_t f_nx = lane < n_all ? frw[lane] : 0;
+    float x_nx = lane < n_all ? valw[lane] : 0.f;
+    int32_t carry_f = 0;
+    for (T base = 0; base < n_all; base += 32) {
+      const T e = base + lane;
+      const int32_t f = f_nx;
+      const float x = x_nx;
+      const bool in_nx = base + 32 + lane < n_all;
+      f_nx = in_nx ? frw[base + 32 + lane] : 0;
+      x_nx = in_nx ? valw[base + 32 + lane] : 0.f;
+      int owner = 0;  // last lane whose row starts at or before e
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const int cand = owner + o;
-      const int64_t cb = __shfl_sync(0xffffffffu, my_b, cand & 31);
-      if (cand < 32 && cb <= e) owner = cand;
+      for (int o = 16; o > 0; o >>= 1) {
+        const int cand = owner + o;  // at most 31
+        const T cb = __shfl_sync(0xffffffffu, my_bt, cand);
+        if (cb <= e) owner = cand;
+      }
+      const T ob = __shfl_sync(0xffffffffu, my_bt, owner);
+      const bool in = e < n_all;
+      int32_t fprev = __shfl_up_sync(0xffffffffu, f, 1);
+      if (lane == 0) fprev = carry_f;  // e > 0: the previous chunk's last frame
+      carry_f = __shfl_sync(0xffffffffu, f, 31);
+      if (in && e > ob && f == fprev) dup = true;
+      const bool nonint = in && !(x == truncf(x) && fabsf(x) < 16777216.f);
+      // a row's lanes are one run (owners do not decrease across the lanes)
+      const int ow = in ? owner : 32;
+      const int oprev = __shfl_up_sync(0xffffffffu, ow, 1);
+      const unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || ow != oprev);
+      const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+      const int rs = 31 - __clz(starts & upto);
+      const unsigned after = starts & ~upto;
+      const unsigned peers =
+          (after ? ((1u << (__ffs(after) - 1)) - 1u) : 0xffffffffu) & ~((1u << rs) - 1u);
+      const unsigned a = in ? (unsigned)fminf(fabsf(x), 16777216.f) : 0u;
+      const int xi = (in && !nonint) ? (int)x : 0;
+      const unsigned sum = __reduce_add_sync(peers, a);
+      const int ssum = __reduce_add_sync(peers, xi);
+      const unsigned anynon = __reduce_or_sync(peers, nonint ? 1u : 0u);
+      if (in && lane == __ffs(peers) - 1) {
+        s_total[w][owner] += sum;
+        s_sum[w][owner] += ssum;
+        s_nonint[w][owner] |= (int)anynon;
+      }
+      __syncwarp();
     }
-    const int64_t ob = __shfl_sync(0xffffffffu, my_b, owner);
-    const bool in = e < e1;
-    int32_t fprev = __shfl_up_sync(0xffffffffu, f, 1);
-    if (lane == 0) fprev = carry_f;  // e > e0: the previous chunk's last frame
-    carry_f = __shfl_sync(0xffffffffu, f, 31);
-    if (in && e > ob && f == fprev) dup = true;
-    const bool nonint = in && !(x == truncf(x) && fabsf(x) < 16777216.f);
-    // a row's lanes are one run (owners do not decrease across the lanes)
-    const int ow = in ? owner : 32;
-    const int oprev = __shfl_up_sync(0xffffffffu, ow, 1);
-    const unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || ow != oprev);
-    const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
-    const int rs = 31 - __clz(starts & upto);
-    const unsigned after = starts & ~upto;
-    const unsigned peers =
-        (after ? ((1u << (__ffs(after) - 1)) - 1u) : 0xffffffffu) & ~((1u << rs) - 1u);
-    const unsigned a = in ? (unsigned)fminf(fabsf(x), 16777216.f) : 0u;
-    const int xi = (in && !nonint) ? (int)x : 0;
-    const unsigned sum = __reduce_add_sync(peers, a);
-    const int ssum = __reduce_add_sync(peers, xi);
-    const unsigned anynon = __reduce_or_sync(peers, nonint ? 1u : 0u);
-    if (in && lane == __ffs(peers) - 1) {
-      s_total[w][owner] += sum;
-      s_sum[w][owner] += ssum;
-      s_nonint[w][owner] |= (int)anynon;
-    }
-    __syncwarp();
-  }
+  };
+  if (e1 - e0 < ((int64_t)1 << 30))
+    chunks(int32_t{0});
+  else
+    chunks(int64_t{0});
   dup = __any_sync(0xffffffffu, dup);
   int32_t out = keep ? my_n : 0;
   bool integral = s_nonint[w][lane] == 0;
